@@ -1,0 +1,186 @@
+/*
+ * vfvm_gb300.h -- C ABI of the GB300-native assembly + Newton library.
+ *
+ * This is the boundary a VoronoiFVM.jl shim binds with `ccall` (see
+ * INTEGRATION.md).  Each entry point replaces one piece of the reference's
+ * hot path (paths relative to the VoronoiFVM.jl project):
+ *
+ *   vfvm_create            SystemState(sys) + update_grid_edgewise!
+ *                          (src/vfvm_state.jl:99-157, src/vfvm_system.jl:690-755)
+ *   vfvm_init_dirichlet    _initialize_dirichlet! (src/vfvm_system.jl:947-1003)
+ *   vfvm_assemble          eval_and_assemble / evaluate_residual_and_jacobian
+ *                          (src/vfvm_assembly.jl:520-643, src/vfvm_solver.jl:224-260)
+ *   vfvm_pattern           the sparsity pattern of state.matrix after flush!
+ *   vfvm_solve             solve_step! (src/vfvm_solver.jl:13-222) with the linear
+ *                          solve of _solve_linear! (src/vfvm_linsolve.jl:6-61)
+ *                          replaced by device Krylov
+ *   vfvm_evolve            solve_transient! (src/vfvm_solver.jl:267-537)
+ *   vfvm_set_params        replacing physics data between solves (the `data`
+ *                          kwarg of solve!, src/vfvm_solver.jl:551-581)
+ *
+ * Conventions
+ *   - all host arrays are caller-owned; the context owns its device buffers;
+ *   - solution/residual vectors are the reference's dense solution layout
+ *     (nspec x nnodes, column-major: dof = inode*nspec + ispec, 0-based,
+ *     src/vfvm_system.jl:808-811);
+ *   - grid index arrays are 0-based, region numbers are 1-based as in the
+ *     reference;
+ *   - return value: VFVM_OK or one of the error codes below, which map to the
+ *     reference's exceptions (src/vfvm_logging_exceptions.jl:6-29).
+ */
+#ifndef VFVM_GB300_H
+#define VFVM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define VFVM_OK 0
+#define VFVM_ERR_CONVERGENCE 1  /* ConvergenceError (src/vfvm_solver.jl:196-198) */
+#define VFVM_ERR_ASSEMBLY 2     /* AssemblyError: NaN assembled (src/vfvm_assembly.jl:10-12) */
+#define VFVM_ERR_LINEAR 3       /* LinearSolverError: Krylov breakdown / no convergence */
+#define VFVM_ERR_TIMEOUT 4      /* a bounded device wait expired */
+#define VFVM_ERR_INPUT 5        /* bad argument (sizes, ids, indices) */
+#define VFVM_ERR_CUDA 6         /* CUDA runtime error */
+#define VFVM_ERR_EMBEDDING 7    /* step size fell below its minimum in vfvm_evolve */
+
+/* physics registry: device functors standing in for the Julia callbacks */
+#define VFVM_PHYS_EX105 1             /* Example105 nonlinear Poisson 1D;     params: eps */
+#define VFVM_PHYS_EX106 2             /* Example106 porous medium (u^m);      params: m */
+#define VFVM_PHYS_EX110 3             /* Example110 two-species RD;           params: eps1, eps2 */
+#define VFVM_PHYS_EX160 4             /* Example160 sedan drift-diffusion;    params: eps, z, V */
+#define VFVM_PHYS_EX207 5             /* Example207 nonlinear Poisson 2D;     params: eps */
+#define VFVM_PHYS_EX301 6             /* Example301 Laplace 3D with source */
+#define VFVM_PHYS_EX440 7             /* Example440 Dirichlet + influx;       params: influx */
+#define VFVM_PHYS_LAPLACE_DIRICHLET 8 /* test030 Laplace, u=0 (region 1), u=1 (region 2) */
+#define VFVM_PHYS_NLPOISSON 11        /* -div grad u + u^3 = 1, u = 0 on the boundary */
+#define VFVM_PHYS_POROUS 12           /* u_t - div grad u^2 = 0 */
+#define VFVM_PHYS_BIPOLAR 13          /* bipolar drift-diffusion (psi,n,p);  params: lambda2,mu_n,mu_p,tau_n,tau_p,doping,V */
+#define VFVM_PHYS_RD2 14              /* two-species reaction-diffusion;    params: D1, D2, k */
+#define VFVM_PHYS_KAPPA_EXP 15        /* -div kappa grad u + exp(u) = f;     params: f; node data: kappa */
+
+/* linear solver / preconditioner / precision selectors */
+#define VFVM_KRYLOV_BICGSTAB 0
+#define VFVM_KRYLOV_GMRES 1
+#define VFVM_PRECON_JACOBI 0   /* (block-)Jacobi: inverse of the nspec x nspec diagonal blocks */
+#define VFVM_PRECON_ILU0 1     /* ILU(0) in multicolour order */
+#define VFVM_PRECISION_FP64 0  /* FP64 Jacobian and FP64 Krylov */
+#define VFVM_PRECISION_MIXED 1 /* FP64 residual/update, FP32 Jacobian + FP32 Krylov (Newton refines) */
+
+typedef struct vfvm_ctx vfvm_ctx;
+
+typedef struct vfvm_grid {
+  int32_t dim, nnodes, ncells, nbfaces;
+  const double* coord;         /* dim x nnodes, column-major */
+  const int32_t* cellnodes;    /* (dim+1) x ncells, column-major, 0-based */
+  const int32_t* cellregions;  /* ncells, 1-based */
+  const int32_t* bfacenodes;   /* dim x nbfaces, column-major, 0-based */
+  const int32_t* bfaceregions; /* nbfaces, 1-based */
+} vfvm_grid;
+
+typedef struct vfvm_physics_desc {
+  int32_t physics_id;
+  int32_t nparams;
+  const double* params;
+  int32_t nnodedata;           /* values per node */
+  const double* nodedata;      /* nnodes x nnodedata, node-major */
+  int32_t nbregions;           /* legacy boundary data (boundary_dirichlet!(sys, ...)): */
+  const double* bfactors;      /* nspec x nbregions, column-major; 1e30 marks Dirichlet */
+  const double* bvalues;       /* nspec x nbregions */
+} vfvm_physics_desc;
+
+/* SolverControl subset (src/vfvm_solvercontrol.jl:13-270) plus device solver settings. */
+typedef struct vfvm_control {
+  double abstol, reltol;       /* Newton update-norm tolerances */
+  int32_t maxiters;
+  double tol_round, tol_mono;
+  double damp_initial, damp_growth;
+  int32_t max_round;
+  int32_t is_linear;           /* one Newton step (System(...; is_linear=true)) */
+  int32_t updatecontrol;       /* 1: norm = max|update| (reference default); 0: norm = max|F|
+                                  over the rows without a Dirichlet penalty, taken before the update */
+  double reltol_linear, abstol_linear;
+  int32_t maxiters_linear;
+  int32_t krylov;              /* VFVM_KRYLOV_* */
+  int32_t precon;              /* VFVM_PRECON_* */
+  int32_t precision;           /* VFVM_PRECISION_* */
+  int32_t gmres_restart;
+  /* time / embedding step control (solve_transient!) */
+  double dt, dt_min, dt_max, dt_grow, dt_decrease;
+  double dp, dp_min, dp_max, dp_grow, dp_decrease;
+  double du_opt, du_max_factor;
+  int32_t num_final_steps, force_first_step, handle_exceptions, store_all;
+} vfvm_control;
+
+/* NewtonSolverHistory (src/vfvm_history.jl:10-37), accumulated over a call. */
+typedef struct vfvm_history {
+  int32_t nnewton;             /* Newton iterations */
+  int32_t nlin;                /* Krylov iterations */
+  int32_t nsteps;              /* accepted time/embedding steps (vfvm_evolve) */
+  int32_t status;
+  double updatenorm;           /* last update norm */
+  double resnorm;              /* max|F| over non-Dirichlet rows at the last Newton iteration */
+  double time_ms, tasm_ms, tlinsolve_ms;
+} vfvm_history;
+
+/* Fill *c with the reference defaults (src/vfvm_solvercontrol.jl:30-257) and the
+ * device solver defaults (BiCGStab, ILU0, FP64). */
+void vfvm_control_default(vfvm_control* c);
+
+/* Create a context on the current CUDA device: tables, form factors, matrix
+ * pattern, work buffers.  Returns NULL on failure with *status set. */
+vfvm_ctx* vfvm_create(const vfvm_grid* grid, const vfvm_physics_desc* phys, int* status);
+void vfvm_destroy(vfvm_ctx* ctx);
+
+/* sizes: out[0]=nspec, out[1]=nnodes, out[2]=nedges, out[3]=nnz of the scalar
+ * pattern, out[4]=number of matrix blocks, out[5]=ncolors of the ILU0 ordering */
+int vfvm_info(vfvm_ctx* ctx, int64_t out[8]);
+
+/* Scalar CSR pattern of the Jacobian (rowptr: n+1, colind: nnz), rows/cols in dof order. */
+int vfvm_pattern(vfvm_ctx* ctx, int64_t* rowptr, int32_t* colind);
+
+/* Node volumes (sum of node factors over regions) and the per-edge form
+ * factors (edge list oriented low -> high node index). */
+int vfvm_geometry(vfvm_ctx* ctx, double* nodevolumes, double* edgefactors, int32_t* edgenodes);
+
+/* Replace the physics parameter block (the `data` of the reference). */
+int vfvm_set_params(vfvm_ctx* ctx, const double* params, int32_t nparams);
+
+/* _initialize_dirichlet!: overwrite Dirichlet values in U (host array, n values). */
+int vfvm_init_dirichlet(vfvm_ctx* ctx, double* U, double time, double lambda);
+
+/* eval_and_assemble at U (Uold for storage terms; tstep = INFINITY is stationary).
+ * F (n values) and Jvals (nnz values in vfvm_pattern order) are optional outputs. */
+int vfvm_assemble(vfvm_ctx* ctx, const double* U, const double* Uold, double time, double tstep,
+                  double lambda, double* F, double* Jvals);
+
+/* solve_step!: one damped Newton solve from inival (also the old time step
+ * solution for storage terms) at (time, tstep, lambda); result in U. */
+int vfvm_solve(vfvm_ctx* ctx, const vfvm_control* control, const double* inival, double* U,
+               double time, double tstep, double lambda, vfvm_history* hist);
+
+/* solve_transient!: implicit Euler (transient != 0) or parameter embedding over
+ * lambdas[0..nlambdas-1].  Stores up to max_store solutions (n values each) in
+ * U_store and their times in t_store; *nstored receives the count. */
+int vfvm_evolve(vfvm_ctx* ctx, const vfvm_control* control, const double* inival,
+                const double* lambdas, int32_t nlambdas, int32_t transient, double time,
+                double* U_store, double* t_store, int32_t max_store, int32_t* nstored,
+                vfvm_history* hist);
+
+/* Device-resident variants: U_dev / inival_dev are device pointers (n doubles).
+ * These run the same device loop without host<->device copies; the stream is
+ * the context's stream (vfvm_stream). */
+int vfvm_solve_device(vfvm_ctx* ctx, const vfvm_control* control, const double* inival_dev,
+                      double* U_dev, double time, double tstep, double lambda, vfvm_history* hist);
+int vfvm_evolve_fixed_device(vfvm_ctx* ctx, const vfvm_control* control, double* U_dev,
+                             double t0, double dt, int32_t nsteps, vfvm_history* hist);
+void* vfvm_stream(vfvm_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

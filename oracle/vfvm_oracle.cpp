@@ -1,0 +1,769 @@
+// VoronoiFVM.jl assembly oracle -- TEST INFRASTRUCTURE ONLY.
+//
+// A plain CPU (FP64) restatement of the reference's edgewise assembly path, used
+// by tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg as the
+// checker.  Nothing in the shipped package links or calls this file.
+//
+// What it restates (paths relative to the reference project):
+//   cellfactors! (Edge1D, Triangle2D, Tetrahedron3D)   src/vfvm_formfactors.jl:12-23,64-100,163-235
+//   bfacefactors! (Vertex0D, Edge1D, Triangle2D)        src/vfvm_formfactors.jl:244-247,263-274,293-332
+//   edgewise factor accumulation                       src/vfvm_system.jl:712-754
+//   Dirichlet constant 1e30                            src/vfvm_system.jl:329
+//   _initialize_dirichlet!                             src/vfvm_system.jl:947-1003
+//   eval_and_assemble (single partition)               src/vfvm_assembly.jl:520-570
+//   assemble_nodes / assemble_edges / assemble_bnodes  src/vfvm_assembly.jl:38-126,128-200,318-407
+//   _addnz (skip exact zeros, NaN is an error)         src/vfvm_assembly.jl:21-28
+//   assemble_res_jac (Node, BNode, Edge)               src/vfvm_assemblydata.jl:245-302,350-382
+//   ResJacEvaluator: forward-mode AD, full chunk       src/vfvm_physics.jl:421-452
+//   boundary_dirichlet!/boundary_neumann!              src/vfvm_physics.jl:487-494,533
+//   fbernoulli_pm / bernoulli_horner                   src/vfvm_functions.jl:1-90
+// The physics callbacks restate the user functions of the reference examples
+// they are named after, and the benchmark workloads (documented per physics).
+//
+// Jacobian pattern: a candidate CSR (node + neighbour blocks, all species) with a
+// per-entry "present" flag set exactly when the reference would create the entry
+// (a nonzero contribution, _addnz).  Only present entries are reported.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#include <limits>
+
+namespace {
+
+const double kDirichlet = 1.0e30;
+
+// ---------------------------------------------------------------- dual numbers
+template <int N>
+struct Dual {
+  double v;
+  double d[N];
+};
+template <int N> inline Dual<N> mk(double v) { Dual<N> r; r.v = v; for (int i = 0; i < N; ++i) r.d[i] = 0; return r; }
+template <int N> inline double val(const Dual<N>& a) { return a.v; }
+inline double val(double a) { return a; }
+template <int N> inline Dual<N> operator+(const Dual<N>& a, const Dual<N>& b) { Dual<N> r; r.v = a.v + b.v; for (int i = 0; i < N; ++i) r.d[i] = a.d[i] + b.d[i]; return r; }
+template <int N> inline Dual<N> operator-(const Dual<N>& a, const Dual<N>& b) { Dual<N> r; r.v = a.v - b.v; for (int i = 0; i < N; ++i) r.d[i] = a.d[i] - b.d[i]; return r; }
+template <int N> inline Dual<N> operator-(const Dual<N>& a) { Dual<N> r; r.v = -a.v; for (int i = 0; i < N; ++i) r.d[i] = -a.d[i]; return r; }
+template <int N> inline Dual<N> operator*(const Dual<N>& a, const Dual<N>& b) { Dual<N> r; r.v = a.v * b.v; for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i]; return r; }
+template <int N> inline Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r; r.v = a.v / b.v; double ib = 1.0 / (b.v * b.v);
+  for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] * b.v - a.v * b.d[i]) * ib;
+  return r;
+}
+template <int N> inline Dual<N> operator+(const Dual<N>& a, double b) { Dual<N> r = a; r.v += b; return r; }
+template <int N> inline Dual<N> operator+(double b, const Dual<N>& a) { Dual<N> r = a; r.v += b; return r; }
+template <int N> inline Dual<N> operator-(const Dual<N>& a, double b) { Dual<N> r = a; r.v -= b; return r; }
+template <int N> inline Dual<N> operator-(double b, const Dual<N>& a) { Dual<N> r; r.v = b - a.v; for (int i = 0; i < N; ++i) r.d[i] = -a.d[i]; return r; }
+template <int N> inline Dual<N> operator*(const Dual<N>& a, double b) { Dual<N> r; r.v = a.v * b; for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b; return r; }
+template <int N> inline Dual<N> operator*(double b, const Dual<N>& a) { return a * b; }
+template <int N> inline Dual<N> operator/(const Dual<N>& a, double b) { Dual<N> r; r.v = a.v / b; for (int i = 0; i < N; ++i) r.d[i] = a.d[i] / b; return r; }
+template <int N> inline Dual<N> operator/(double a, const Dual<N>& b) { return mk<N>(a) / b; }
+template <int N> inline Dual<N> exp(const Dual<N>& a) { Dual<N> r; r.v = std::exp(a.v); for (int i = 0; i < N; ++i) r.d[i] = r.v * a.d[i]; return r; }
+template <int N> inline Dual<N> expm1(const Dual<N>& a) { Dual<N> r; r.v = std::expm1(a.v); double e = std::exp(a.v); for (int i = 0; i < N; ++i) r.d[i] = e * a.d[i]; return r; }
+template <int N> inline Dual<N> log(const Dual<N>& a) { Dual<N> r; r.v = std::log(a.v); for (int i = 0; i < N; ++i) r.d[i] = a.d[i] / a.v; return r; }
+template <int N> inline Dual<N> log1p(const Dual<N>& a) { Dual<N> r; r.v = std::log1p(a.v); for (int i = 0; i < N; ++i) r.d[i] = a.d[i] / (1.0 + a.v); return r; }
+// x^p for real p (ForwardDiff: p*x^(p-1)*dx)
+template <int N> inline Dual<N> pow(const Dual<N>& a, double p) { Dual<N> r; r.v = std::pow(a.v, p); double dp = p * std::pow(a.v, p - 1); for (int i = 0; i < N; ++i) r.d[i] = dp * a.d[i]; return r; }
+template <int N> inline Dual<N> sq(const Dual<N>& a) { return a * a; }
+template <int N> inline Dual<N> cube(const Dual<N>& a) { Dual<N> r; r.v = a.v * a.v * a.v; double dp = 3 * a.v * a.v; for (int i = 0; i < N; ++i) r.d[i] = dp * a.d[i]; return r; }
+template <int N> inline Dual<N> dmax(const Dual<N>& a, double b) { return a.v >= b ? a : mk<N>(b); }
+inline double sq(double a) { return a * a; }
+inline double cube(double a) { return a * a * a; }
+inline double dmax(double a, double b) { return std::max(a, b); }
+using std::exp; using std::expm1; using std::log; using std::log1p; using std::pow;
+
+// Bernoulli function, src/vfvm_functions.jl:2-31,78-90
+const double c1 = 1.0 / 47900160.0, c2 = -1.0 / 1209600.0, c3 = 1.0 / 30240.0,
+             c4 = -1.0 / 720.0, c5 = 1.0 / 12.0, c6 = -1.0 / 2.0;
+template <class T> inline T bernoulli_horner(const T& x) {
+  T y = x * c1;
+  y = x * y;
+  y = x * (c2 + y);
+  y = x * y;
+  y = x * (c3 + y);
+  y = x * y;
+  y = x * (c4 + y);
+  y = x * y;
+  y = x * (c5 + y);
+  y = x * (c6 + y);
+  return 1.0 + y;
+}
+template <class T> inline void fbernoulli_pm(const T& x, T& bp, T& bm) {
+  double xv = val(x);
+  if (xv < -50.0) { bp = -x; bm = x * 0.0; }
+  else if (xv > 50.0) { bp = x * 0.0; bm = x; }
+  else if (std::fabs(xv) < 0.25) { bp = bernoulli_horner(x); bm = x + bp; }
+  else { bp = x / expm1(x); bm = x + bp; }
+}
+template <class T> inline T fbernoulli(const T& x) {
+  double xv = val(x);
+  if (xv < -50.0) return -x;
+  if (xv > 50.0) return x * 0.0;
+  if (std::fabs(xv) < 0.25) return bernoulli_horner(x);
+  return x / expm1(x);
+}
+
+// ramp(t; dt, du), src/vfvm_physics.jl:516-525
+inline double ramp(double t, double t0, double t1, double u0, double u1) {
+  if (t < t0) return u0;
+  if (t < t1) return u0 + (u1 - u0) * (t - t0) / (t1 - t0);
+  return u1;
+}
+
+// ---------------------------------------------------------------- geometry items
+struct NodeInfo { int index, region; const double* x; double time, lambda; const double* ndata; };
+struct EdgeInfo { int K, L, region; const double* xK; const double* xL; double time, lambda; const double* ndataK; const double* ndataL; };
+struct BNodeInfo { int index, region; const double* x; double time, lambda, fac, Dirichlet; double* dirichlet_value; };
+
+// boundary_dirichlet!(y,u,bnode,ispec,ireg,val), src/vfvm_physics.jl:487-494
+template <class T> inline void boundary_dirichlet(T* y, const T* u, BNodeInfo& b, int ispec, int ireg, double v) {
+  if (b.region == ireg) {
+    y[ispec] = y[ispec] + b.Dirichlet * (u[ispec] - v);
+    b.dirichlet_value[ispec] = v;
+  }
+}
+
+// ---------------------------------------------------------------- physics
+// Physics ids follow include/vfvm_gb300.h (VFVM_PHYS_*).
+struct PhysParams { const double* p; int np; };
+
+// Each physics: NS, has_* flags, templated callbacks.
+struct PhysEx105 {  // examples/Example105_NonlinearPoisson1D.jl:41-60
+  static const int NS = 1; double eps;
+  static const bool has_reaction = true, has_storage = false, has_source = true, has_breaction = false;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = eps * (uK[0] - uL[0]); }
+  template <class T> void reaction(T* f, const T* u, const NodeInfo&) const { f[0] = exp(u[0]) - exp(-u[0]); }
+  template <class T> void storage(T*, const T*, const NodeInfo&) const {}
+  void source(double* f, const NodeInfo& n) const { f[0] = (n.x[0] <= 0.5) ? 1.0 : -1.0; }
+  template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
+};
+struct PhysEx106 {  // examples/Example106_NonlinearDiffusion1D.jl:58-68
+  static const int NS = 1; double m;
+  static const bool has_reaction = false, has_storage = true, has_source = false, has_breaction = false;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = pow(uK[0], m) - pow(uL[0], m); }
+  template <class T> void reaction(T*, const T*, const NodeInfo&) const {}
+  template <class T> void storage(T* f, const T* u, const NodeInfo&) const { f[0] = u[0]; }
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
+};
+struct PhysEx110 {  // examples/Example110_ReactionDiffusion1D_TwoSpecies.jl:40-64
+  static const int NS = 2; double eps1, eps2;
+  static const bool has_reaction = true, has_storage = true, has_source = true, has_breaction = false;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
+    f[0] = eps1 * (uK[0] - uL[0]) * (0.01 + uK[1] + uL[1]);
+    f[1] = eps2 * (uK[1] - uL[1]) * (0.01 + uK[0] + uL[0]);
+  }
+  template <class T> void reaction(T* f, const T* u, const NodeInfo&) const { f[0] = u[0] * u[1]; f[1] = -(u[0] * u[1]); }
+  template <class T> void storage(T* f, const T* u, const NodeInfo&) const { f[0] = u[0]; f[1] = u[1]; }
+  void source(double* f, const NodeInfo& n) const { f[0] = 1.0e-4 * (0.01 + n.x[0]); f[1] = 1.0e-4 * (0.01 + 1.0 - n.x[0]); }
+  template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
+};
+struct PhysEx160 {  // examples/Example160_UnipolarDriftDiffusion1D.jl:52-84 (sedan flux; iphi=1, ic=2)
+  static const int NS = 2; double eps, z, V;
+  static const bool has_reaction = true, has_storage = true, has_source = false, has_breaction = true;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
+    f[0] = eps * (uK[0] - uL[0]);
+    const double eps_reg = 1.0e-10;
+    T mu1 = -log1p(dmax(-uK[1], -1.0 + eps_reg));
+    T mu2 = -log1p(dmax(-uL[1], -1.0 + eps_reg));
+    T bp, bm;
+    fbernoulli_pm(z * 2.0 * (uK[0] - uL[0]) + (mu1 - mu2), bp, bm);
+    f[1] = bm * uK[1] - bp * uL[1];
+  }
+  template <class T> void reaction(T* f, const T* u, const NodeInfo&) const { f[0] = z * (1.0 - 2.0 * u[1]); f[1] = u[1] * 0.0; }
+  template <class T> void storage(T* f, const T* u, const NodeInfo&) const { f[0] = u[0] * 0.0; f[1] = u[1]; }
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const {
+    double Vt = ramp(b.time, 0.0, 1.0e-2, 0.0, V);
+    boundary_dirichlet(f, u, b, 0, 1, Vt);
+    boundary_dirichlet(f, u, b, 0, 2, 0.0);
+    boundary_dirichlet(f, u, b, 1, 2, 0.5);
+  }
+};
+struct PhysEx207 {  // examples/Example207_NonlinearPoisson2D.jl:36-50
+  static const int NS = 1; double eps;
+  static const bool has_reaction = true, has_storage = true, has_source = true, has_breaction = false;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = eps * (sq(uK[0]) - sq(uL[0])); }
+  template <class T> void reaction(T* f, const T* u, const NodeInfo&) const { f[0] = sq(u[0]); }
+  template <class T> void storage(T* f, const T* u, const NodeInfo&) const { f[0] = u[0]; }
+  void source(double* f, const NodeInfo& n) const { double x1 = n.x[0] - 0.5, x2 = n.x[1] - 0.5; f[0] = std::exp(-20.0 * (x1 * x1 + x2 * x2)); }
+  template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
+};
+struct PhysEx301 {  // examples/Example301_Laplace3D.jl:15-24
+  static const int NS = 1;
+  static const bool has_reaction = false, has_storage = false, has_source = true, has_breaction = false;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = uK[0] - uL[0]; }
+  template <class T> void reaction(T*, const T*, const NodeInfo&) const {}
+  template <class T> void storage(T*, const T*, const NodeInfo&) const {}
+  void source(double* f, const NodeInfo& n) const { f[0] = n.x[0] * std::sin(5.0 * n.x[1]) * std::exp(n.x[2]); }
+  template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
+};
+struct PhysEx440 {  // examples/Example440_ParallelState.jl:16-25
+  static const int NS = 1; double influx;
+  static const bool has_reaction = false, has_storage = false, has_source = false, has_breaction = true;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = sq(uK[0]) - sq(uL[0]); }
+  template <class T> void reaction(T*, const T*, const NodeInfo&) const {}
+  template <class T> void storage(T*, const T*, const NodeInfo&) const {}
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const {
+    boundary_dirichlet(f, u, b, 0, 1, 0.1);
+    if (b.region == 2) f[0] = f[0] - influx;  // boundary_neumann!, src/vfvm_physics.jl:533
+  }
+};
+struct PhysLaplaceDir {  // test/test030_cachesol.jl:10-18
+  static const int NS = 1;
+  static const bool has_reaction = false, has_storage = false, has_source = false, has_breaction = true;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = uK[0] - uL[0]; }
+  template <class T> void reaction(T*, const T*, const NodeInfo&) const {}
+  template <class T> void storage(T*, const T*, const NodeInfo&) const {}
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const {
+    boundary_dirichlet(f, u, b, 0, 1, 0.0);
+    boundary_dirichlet(f, u, b, 0, 2, 1.0);
+  }
+};
+// Benchmark workload 1: -div(grad u) + u^3 = 1, u = 0 on every boundary region.
+struct PhysNLPoisson {
+  static const int NS = 1;
+  static const bool has_reaction = true, has_storage = false, has_source = false, has_breaction = true;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = uK[0] - uL[0]; }
+  template <class T> void reaction(T* f, const T* u, const NodeInfo&) const { f[0] = cube(u[0]) - 1.0; }
+  template <class T> void storage(T*, const T*, const NodeInfo&) const {}
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const { boundary_dirichlet(f, u, b, 0, b.region, 0.0); }
+};
+// Benchmark workload 2: porous medium u_t - div(grad u^2) = 0, homogeneous Neumann.
+struct PhysPorous {
+  static const int NS = 1;
+  static const bool has_reaction = false, has_storage = true, has_source = false, has_breaction = false;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = sq(uK[0]) - sq(uL[0]); }
+  template <class T> void reaction(T*, const T*, const NodeInfo&) const {}
+  template <class T> void storage(T* f, const T* u, const NodeInfo&) const { f[0] = u[0]; }
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
+};
+// Benchmark workload 3: bipolar drift-diffusion in density variables (psi, n, p),
+// scaled units (thermal voltage 1, intrinsic density 1).
+//   flux_psi = lambda2 (psi_K - psi_L)
+//   flux_n   = mu_n (B(psi_K - psi_L) n_K - B(psi_L - psi_K) n_L)
+//   flux_p   = mu_p (B(psi_L - psi_K) p_K - B(psi_K - psi_L) p_L)
+//   reaction_psi = n - p - C(x),  reaction_n = reaction_p = R,
+//   R = (n p - 1) / (tau_p (n + 1) + tau_n (p + 1))         (SRH)
+//   C = +doping for x < 0.5, -doping otherwise
+//   ohmic contacts: region 4 (x = 0) at bias 0, region 2 (x = 1) at bias V*lambda_embed
+// params: lambda2, mu_n, mu_p, tau_n, tau_p, doping, V
+struct PhysBipolar {
+  static const int NS = 3; double lambda2, mun, mup, taun, taup, doping, V;
+  static const bool has_reaction = true, has_storage = false, has_source = false, has_breaction = true;
+  double C(const double* x) const { return x[0] < 0.5 ? doping : -doping; }
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
+    f[0] = lambda2 * (uK[0] - uL[0]);
+    T bp, bm;
+    fbernoulli_pm(uK[0] - uL[0], bp, bm);
+    f[1] = mun * (bp * uK[1] - bm * uL[1]);
+    f[2] = mup * (bm * uK[2] - bp * uL[2]);
+  }
+  template <class T> void reaction(T* f, const T* u, const NodeInfo& n) const {
+    f[0] = u[1] - u[2] - C(n.x);
+    T r = (u[1] * u[2] - 1.0) / (taup * (u[1] + 1.0) + taun * (u[2] + 1.0));
+    f[1] = r; f[2] = r;
+  }
+  template <class T> void storage(T*, const T*, const NodeInfo&) const {}
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const {
+    if (b.region != 2 && b.region != 4) return;
+    double c = C(b.x);
+    double nn = 0.5 * c + std::sqrt(0.25 * c * c + 1.0);
+    double pp = 1.0 / nn;
+    double bias = (b.region == 2) ? V * b.lambda : 0.0;
+    double psi = std::asinh(0.5 * c) + bias;
+    boundary_dirichlet(f, u, b, 0, b.region, psi);
+    boundary_dirichlet(f, u, b, 1, b.region, nn);
+    boundary_dirichlet(f, u, b, 2, b.region, pp);
+  }
+};
+// Benchmark workload 4: two-species reaction-diffusion
+//   flux_i = D_i (u_i,K - u_i,L);  f1 = k (u1 - u2^2), f2 = -k (u1 - u2^2)
+//   Dirichlet: region 4 (x = 0): u1 = 1, u2 = 0;  region 2 (x = 1): u1 = 0, u2 = 1
+// params: D1, D2, k
+struct PhysRD2 {
+  static const int NS = 2; double D1, D2, k;
+  static const bool has_reaction = true, has_storage = false, has_source = false, has_breaction = true;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
+    f[0] = D1 * (uK[0] - uL[0]);
+    f[1] = D2 * (uK[1] - uL[1]);
+  }
+  template <class T> void reaction(T* f, const T* u, const NodeInfo&) const {
+    T r = k * (u[0] - sq(u[1]));
+    f[0] = r; f[1] = -r;
+  }
+  template <class T> void storage(T*, const T*, const NodeInfo&) const {}
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const {
+    boundary_dirichlet(f, u, b, 0, 4, 1.0);
+    boundary_dirichlet(f, u, b, 1, 4, 0.0);
+    boundary_dirichlet(f, u, b, 0, 2, 0.0);
+    boundary_dirichlet(f, u, b, 1, 2, 1.0);
+  }
+};
+// Benchmark workload 5: -div(kappa grad u) + exp(u) = f, u = 0 on every boundary;
+// node data: kappa; edge coefficient = arithmetic mean of the two node values.
+// params: f
+struct PhysKappaExp {
+  static const int NS = 1; double fsrc;
+  static const bool has_reaction = true, has_storage = false, has_source = true, has_breaction = true;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo& e) const {
+    double kap = 0.5 * (e.ndataK[0] + e.ndataL[0]);
+    f[0] = kap * (uK[0] - uL[0]);
+  }
+  template <class T> void reaction(T* f, const T* u, const NodeInfo&) const { f[0] = exp(u[0]); }
+  template <class T> void storage(T*, const T*, const NodeInfo&) const {}
+  void source(double* f, const NodeInfo&) const { f[0] = fsrc; }
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const { boundary_dirichlet(f, u, b, 0, b.region, 0.0); }
+};
+
+// ---------------------------------------------------------------- system
+struct Oracle {
+  int dim = 0, N = 0, ncells = 0, nbf = 0, ns = 1, phys = 0, nregions = 1, nbregions = 0, nnd = 0;
+  std::vector<double> coord;       // dim x N
+  std::vector<int> cellnodes, cellregions, bfacenodes, bfaceregions;
+  std::vector<double> params, ndata;
+  std::vector<double> bfactors, bvalues;  // legacy BC: ns x nbregions
+  bool has_legacy = false;
+  // edges
+  int E = 0;
+  std::vector<int> edgenodes;      // 2 x E
+  std::vector<int> celledges;      // nedges_per_cell x ncells
+  // edgewise factors: per node/edge, list of (region, fac) sorted by region
+  std::vector<std::vector<std::pair<int, double>>> nodefac, edgefac;
+  std::vector<double> bfacenodefac;  // dim x nbf  (nodes per bface = dim)
+  // candidate CSR over dofs
+  std::vector<int64_t> rowptr;
+  std::vector<int> colind;
+  std::vector<double> vals;
+  std::vector<uint8_t> present;
+  int nerr = 0;
+};
+
+inline int nn_bface(int dim) { return dim; }  // nodes per boundary face: Vertex0D 1, Edge1D 2, Triangle2D 3
+
+// local_celledgenodes: Edge1D (1,2); Triangle2D edges opposite node 1,2,3;
+// Tetrahedron3D [1 2; 1 3; 1 4; 2 3; 2 4; 3 4] (0-based below)
+const int tri_en[3][2] = {{1, 2}, {2, 0}, {0, 1}};
+const int tet_en[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+
+// cellfactors!, src/vfvm_formfactors.jl:12-23 (Edge1D), :64-100 (Triangle2D), :163-235 (Tetrahedron3D)
+void cellfactors(int dim, const double* coord, const int* n, double* npar, double* epar) {
+  if (dim == 1) {
+    double d = std::fabs(coord[n[1]] - coord[n[0]]);
+    npar[0] = d / 2; npar[1] = d / 2; epar[0] = 1 / d;
+  } else if (dim == 2) {
+    double V[2][3];
+    for (int i = 0; i < 3; ++i)
+      for (int c = 0; c < 2; ++c) V[c][i] = coord[c + 2 * n[tri_en[i][0]]] - coord[c + 2 * n[tri_en[i][1]]];
+    double det = V[0][2] * V[1][1] - V[0][1] * V[1][2];
+    double vol = std::fabs(0.5 * det), ivol = 1.0 / vol;
+    double dd[3];
+    for (int i = 0; i < 3; ++i) dd[i] = V[0][i] * V[0][i] + V[1][i] * V[1][i];
+    epar[0] = (dd[1] + dd[2] - dd[0]) * 0.125 * ivol;
+    epar[1] = (dd[2] + dd[0] - dd[1]) * 0.125 * ivol;
+    epar[2] = (dd[0] + dd[1] - dd[2]) * 0.125 * ivol;
+    npar[0] = npar[1] = npar[2] = 0.0;
+    for (int i = 0; i < 3; ++i) {
+      npar[tri_en[i][0]] += epar[i] * dd[i] * 0.25;
+      npar[tri_en[i][1]] += epar[i] * dd[i] * 0.25;
+    }
+  } else {
+    const int pi1[4] = {4, 5, 4, 0}, pi2[4] = {5, 2, 0, 3}, pi3[4] = {3, 1, 2, 1};
+    const int po1[4] = {1, 0, 1, 5}, po2[4] = {0, 3, 5, 2}, po3[4] = {2, 4, 3, 4};
+    double dd[6];
+    for (int i = 0; i < 6; ++i) {
+      int p1 = n[tet_en[i][0]], p2 = n[tet_en[i][1]];
+      double dx = coord[3 * p1] - coord[3 * p2], dy = coord[3 * p1 + 1] - coord[3 * p2 + 1], dz = coord[3 * p1 + 2] - coord[3 * p2 + 2];
+      dd[i] = dx * dx + dy * dy + dz * dz;
+    }
+    for (int i = 0; i < 6; ++i) epar[i] = 0;
+    const double* c0 = coord + 3 * n[0];
+    double x1 = coord[3 * n[1]] - c0[0], y1 = coord[3 * n[1] + 1] - c0[1], z1 = coord[3 * n[1] + 2] - c0[2];
+    double x2 = coord[3 * n[2]] - c0[0], y2 = coord[3 * n[2] + 1] - c0[1], z2 = coord[3 * n[2] + 2] - c0[2];
+    double x3 = coord[3 * n[3]] - c0[0], y3 = coord[3 * n[3] + 1] - c0[1], z3 = coord[3 * n[3] + 2] - c0[2];
+    double det = (x1 * (y2 * z3 - y3 * z2) + x2 * (y3 * z1 - y1 * z3) + x3 * (y1 * z2 - y2 * z1));
+    if (det < 0) det = -det;
+    double vol = det / 6;
+    double vv = 96 * 6 * vol;
+    for (int i = 0; i < 4; ++i) {
+      npar[i] = 0.0;
+      int i1 = pi1[i], i2 = pi2[i], i3 = pi3[i];
+      double h1 = dd[i1] * (dd[i2] + dd[i3] - dd[i1]);
+      double h2 = dd[i2] * (dd[i3] + dd[i1] - dd[i2]);
+      double h3 = dd[i3] * (dd[i1] + dd[i2] - dd[i3]);
+      double df = h1 + h2 + h3;
+      double vf = (h1 * dd[po1[i]] + h2 * dd[po2[i]] + h3 * dd[po3[i]] - 2 * dd[i1] * dd[i2] * dd[i3]) / (vv * df);
+      epar[i1] += h1 * vf;
+      epar[i2] += h2 * vf;
+      epar[i3] += h3 * vf;
+    }
+    for (int i = 0; i < 6; ++i) {
+      npar[tet_en[i][0]] += epar[i];
+      npar[tet_en[i][1]] += epar[i];
+      epar[i] = 6 * epar[i] / dd[i];
+    }
+  }
+}
+
+// bfacefactors!, src/vfvm_formfactors.jl:244-247 (Vertex0D), :263-274 (Edge1D), :293-332 (Triangle2D)
+void bfacefactors(int dim, const double* coord, const int* n, double* npar, double* epar) {
+  if (dim == 1) {
+    npar[0] = 1.0;
+  } else if (dim == 2) {
+    double dx = coord[2 * n[0]] - coord[2 * n[1]], dy = coord[2 * n[0] + 1] - coord[2 * n[1] + 1];
+    double d = std::sqrt(dx * dx + dy * dy);
+    npar[0] = d / 2; npar[1] = d / 2; epar[0] = 1 / d;
+  } else {
+    double e[3] = {0, 0, 0};
+    for (int j = 0; j < 3; ++j) {
+      double d = coord[j + 3 * n[tri_en[0][0]]] - coord[j + 3 * n[tri_en[0][1]]]; e[0] += d * d;
+      d = coord[j + 3 * n[tri_en[1][0]]] - coord[j + 3 * n[tri_en[1][1]]]; e[1] += d * d;
+      d = coord[j + 3 * n[tri_en[2][0]]] - coord[j + 3 * n[tri_en[2][1]]]; e[2] += d * d;
+    }
+    double dd[3] = {e[0], e[1], e[2]};
+    e[0] = (dd[1] + dd[2] - dd[0]) * dd[0];
+    e[1] = (dd[2] + dd[0] - dd[1]) * dd[1];
+    e[2] = (dd[0] + dd[1] - dd[2]) * dd[2];
+    double vol = std::sqrt(e[0] + e[1] + e[2]) * 0.25;
+    double d = 1.0 / (8 * vol);
+    npar[0] = npar[1] = npar[2] = 0.0;
+    for (int i = 0; i < 3; ++i) {
+      npar[tri_en[i][0]] += e[i] * d * 0.25;
+      npar[tri_en[i][1]] += e[i] * d * 0.25;
+    }
+    epar[0] = e[0] * d / dd[0];
+    epar[1] = e[1] * d / dd[1];
+    epar[2] = e[2] * d / dd[2];
+  }
+}
+
+void add_factor(std::vector<std::pair<int, double>>& v, int reg, double f) {
+  for (auto& p : v)
+    if (p.first == reg) { p.second += f; return; }
+  v.emplace_back(reg, f);
+  std::sort(v.begin(), v.end(), [](const std::pair<int, double>& a, const std::pair<int, double>& b) { return a.first < b.first; });
+}
+
+// update_grid_edgewise!, src/vfvm_system.jl:690-755
+void setup(Oracle& o) {
+  const int d = o.dim;
+  const int nen = d == 1 ? 1 : (d == 2 ? 3 : 6);
+  const int nnc = d + 1;
+  // global edges (lo, hi), numbered lexicographically
+  std::vector<int64_t> keys;
+  keys.reserve((size_t)o.ncells * nen);
+  auto ledge = [&](int i, int k) -> int { return d == 1 ? k : (d == 2 ? tri_en[i][k] : tet_en[i][k]); };
+  for (int c = 0; c < o.ncells; ++c)
+    for (int i = 0; i < nen; ++i) {
+      int a = o.cellnodes[ledge(i, 0) + nnc * c], b = o.cellnodes[ledge(i, 1) + nnc * c];
+      if (a > b) std::swap(a, b);
+      keys.push_back((int64_t)a * o.N + b);
+    }
+  std::vector<int64_t> uk = keys;
+  std::sort(uk.begin(), uk.end());
+  uk.erase(std::unique(uk.begin(), uk.end()), uk.end());
+  o.E = (int)uk.size();
+  o.edgenodes.resize(2 * o.E);
+  for (int e = 0; e < o.E; ++e) { o.edgenodes[2 * e] = (int)(uk[e] / o.N); o.edgenodes[2 * e + 1] = (int)(uk[e] % o.N); }
+  o.celledges.resize((size_t)nen * o.ncells);
+  for (size_t i = 0; i < keys.size(); ++i) o.celledges[i] = (int)(std::lower_bound(uk.begin(), uk.end(), keys[i]) - uk.begin());
+  // factors
+  o.nodefac.assign(o.N, {});
+  o.edgefac.assign(o.E, {});
+  double npar[4], epar[6];
+  for (int c = 0; c < o.ncells; ++c) {
+    cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+    int ireg = o.cellregions[c];
+    for (int i = 0; i < nnc; ++i) add_factor(o.nodefac[o.cellnodes[i + nnc * c]], ireg, npar[i]);
+    for (int i = 0; i < nen; ++i) add_factor(o.edgefac[o.celledges[i + nen * c]], ireg, epar[i]);
+  }
+  const int nbn = nn_bface(d);
+  o.bfacenodefac.assign((size_t)nbn * o.nbf, 0.0);
+  for (int b = 0; b < o.nbf; ++b) bfacefactors(d, o.coord.data(), &o.bfacenodes[nbn * b], &o.bfacenodefac[nbn * b], epar);
+  // candidate CSR: rows (K,i), columns (M,j) for M in {K} u neighbours(K)
+  std::vector<std::vector<int>> nb(o.N);
+  for (int e = 0; e < o.E; ++e) { nb[o.edgenodes[2 * e]].push_back(o.edgenodes[2 * e + 1]); nb[o.edgenodes[2 * e + 1]].push_back(o.edgenodes[2 * e]); }
+  const int ns = o.ns;
+  const int64_t n = (int64_t)o.N * ns;
+  o.rowptr.assign(n + 1, 0);
+  o.colind.clear();
+  for (int K = 0; K < o.N; ++K) {
+    nb[K].push_back(K);
+    std::sort(nb[K].begin(), nb[K].end());
+    for (int i = 0; i < ns; ++i) {
+      for (int M : nb[K])
+        for (int j = 0; j < ns; ++j) o.colind.push_back(M * ns + j);
+      o.rowptr[(int64_t)K * ns + i + 1] = (int64_t)o.colind.size();
+    }
+  }
+  o.vals.assign(o.colind.size(), 0.0);
+  o.present.assign(o.colind.size(), 0);
+}
+
+// _addnz, src/vfvm_assembly.jl:21-28
+inline void addnz(Oracle& o, int64_t i, int64_t j, double v, double fac) {
+  if (std::isnan(v)) { o.nerr++; return; }
+  if (v != 0.0) {
+    int64_t lo = o.rowptr[i], hi = o.rowptr[i + 1];
+    const int* p = std::lower_bound(o.colind.data() + lo, o.colind.data() + hi, (int)j);
+    int64_t k = p - o.colind.data();
+    o.vals[k] += v * fac;
+    o.present[k] = 1;
+  }
+}
+
+template <class P>
+int assemble_t(Oracle& o, const P& ph, const double* U, const double* Uold, double time, double tstep, double lambda, double* F) {
+  const int NS = P::NS;
+  const int64_t n = (int64_t)o.N * NS;
+  std::fill(F, F + n, 0.0);                       // F .= 0
+  std::fill(o.vals.begin(), o.vals.end(), 0.0);   // zero!(matrix)
+  o.nerr = 0;
+  const double tstepinv = 1.0 / tstep;
+  const int d = o.dim;
+  const double* nd = o.ndata.empty() ? nullptr : o.ndata.data();
+  // assemble_nodes, src/vfvm_assembly.jl:38-126
+  for (int K = 0; K < o.N; ++K) {
+    for (auto& rf : o.nodefac[K]) {
+      NodeInfo ni{K, rf.first, &o.coord[d * K], time, lambda, nd ? nd + (size_t)o.nnd * K : nullptr};
+      double fac = rf.second;
+      double src[NS] = {0}, oldstor[NS] = {0};
+      Dual<NS> u[NS], rr[NS], rs[NS];
+      for (int i = 0; i < NS; ++i) { u[i] = mk<NS>(U[K * NS + i]); u[i].d[i] = 1.0; rr[i] = mk<NS>(0); rs[i] = mk<NS>(0); }
+      if (P::has_source) ph.source(src, ni);
+      if (P::has_reaction) ph.reaction(rr, u, ni);
+      if (P::has_storage) {
+        ph.storage(rs, u, ni);
+        double uo[NS];
+        for (int i = 0; i < NS; ++i) uo[i] = Uold[K * NS + i];
+        ph.storage(oldstor, uo, ni);
+      }
+      for (int i = 0; i < NS; ++i) {
+        F[K * NS + i] += fac * (rr[i].v - src[i] + (rs[i].v - oldstor[i]) * tstepinv);
+        for (int j = 0; j < NS; ++j) addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + j, rr[i].d[j] + rs[i].d[j] * tstepinv, fac);
+      }
+    }
+  }
+  // assemble_edges, src/vfvm_assembly.jl:128-200
+  for (int e = 0; e < o.E; ++e) {
+    int K = o.edgenodes[2 * e], L = o.edgenodes[2 * e + 1];
+    for (auto& rf : o.edgefac[e]) {
+      EdgeInfo ei{K, L, rf.first, &o.coord[d * K], &o.coord[d * L], time, lambda,
+                  nd ? nd + (size_t)o.nnd * K : nullptr, nd ? nd + (size_t)o.nnd * L : nullptr};
+      double fac = rf.second;
+      Dual<2 * NS> uK[NS], uL[NS], f[NS];
+      for (int i = 0; i < NS; ++i) {
+        uK[i] = mk<2 * NS>(U[K * NS + i]); uK[i].d[i] = 1.0;
+        uL[i] = mk<2 * NS>(U[L * NS + i]); uL[i].d[NS + i] = 1.0;
+        f[i] = mk<2 * NS>(0);
+      }
+      ph.flux(f, uK, uL, ei);
+      for (int i = 0; i < NS; ++i) {
+        double v = fac * f[i].v;
+        F[K * NS + i] += v;
+        F[L * NS + i] += -v;
+        for (int j = 0; j < NS; ++j) {
+          int64_t iK = (int64_t)K * NS + i, iL = (int64_t)L * NS + i, jK = (int64_t)K * NS + j, jL = (int64_t)L * NS + j;
+          addnz(o, iK, jK, +f[i].d[j], fac);
+          addnz(o, iL, jK, -f[i].d[j], fac);
+          addnz(o, iK, jL, +f[i].d[NS + j], fac);
+          addnz(o, iL, jL, -f[i].d[NS + j], fac);
+        }
+      }
+    }
+  }
+  // assemble_bnodes, src/vfvm_assembly.jl:318-407
+  const int nbn = nn_bface(d);
+  double dval[NS];
+  for (int b = 0; b < o.nbf; ++b) {
+    for (int ib = 0; ib < nbn; ++ib) {
+      int K = o.bfacenodes[ib + nbn * b];
+      int reg = o.bfaceregions[b];
+      double fac = o.bfacenodefac[ib + nbn * b];
+      double Dir = kDirichlet;
+      if (o.has_legacy && reg - 1 < o.nbregions) {
+        Dir = kDirichlet / fac;
+        for (int i = 0; i < NS; ++i) {
+          double bf = o.bfactors[i + NS * (reg - 1)], bv = o.bvalues[i + NS * (reg - 1)];
+          if (bf == kDirichlet) {
+            F[K * NS + i] += bf * (U[K * NS + i] - bv);
+            addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + i, bf, 1.0);
+          } else {
+            F[K * NS + i] += fac * (bf * U[K * NS + i] - bv);
+            addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + i, bf, fac);
+          }
+        }
+      }
+      BNodeInfo bi{K, reg, &o.coord[d * K], time, lambda, fac, Dir, dval};
+      Dual<NS> u[NS], y[NS];
+      for (int i = 0; i < NS; ++i) { u[i] = mk<NS>(U[K * NS + i]); u[i].d[i] = 1.0; y[i] = mk<NS>(0); }
+      if (P::has_breaction) ph.breaction(y, u, bi);
+      for (int i = 0; i < NS; ++i) {
+        F[K * NS + i] += fac * (y[i].v - 0.0);
+        for (int j = 0; j < NS; ++j) addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + j, y[i].d[j], fac);
+      }
+    }
+  }
+  return o.nerr ? 2 : 0;
+}
+
+// _initialize_dirichlet!, src/vfvm_system.jl:947-1003
+template <class P>
+void init_dirichlet_t(Oracle& o, const P& ph, double* U, double time, double lambda) {
+  const int NS = P::NS;
+  const int d = o.dim, nbn = nn_bface(d);
+  for (int b = 0; b < o.nbf; ++b)
+    for (int ib = 0; ib < nbn; ++ib) {
+      int K = o.bfacenodes[ib + nbn * b];
+      int reg = o.bfaceregions[b];
+      double dval[NS];
+      for (int i = 0; i < NS; ++i) dval[i] = std::numeric_limits<double>::infinity();
+      BNodeInfo bi{K, reg, &o.coord[d * K], time, lambda, o.bfacenodefac[ib + nbn * b], kDirichlet, dval};
+      double u[NS], y[NS];
+      for (int i = 0; i < NS; ++i) { u[i] = U[K * NS + i]; y[i] = 0.0; }
+      if (P::has_breaction) ph.breaction(y, u, bi);
+      for (int i = 0; i < NS; ++i) {
+        if (!std::isinf(dval[i])) U[K * NS + i] = dval[i];
+        if (o.has_legacy && reg - 1 < o.nbregions) {
+          double bf = o.bfactors[i + NS * (reg - 1)];
+          if (std::fabs(bf - kDirichlet) <= 1.4901161193847656e-8 * std::max(std::fabs(bf), kDirichlet))
+            U[K * NS + i] = o.bvalues[i + NS * (reg - 1)];
+        }
+      }
+    }
+}
+
+template <class F>
+int dispatch(const Oracle& o, F&& fn) {
+  const double* p = o.params.data();
+  auto P = [&](int i) { return i < (int)o.params.size() ? p[i] : 0.0; };
+  switch (o.phys) {
+    case 1: { PhysEx105 ph; ph.eps = P(0); return fn(ph); }
+    case 2: { PhysEx106 ph; ph.m = P(0); return fn(ph); }
+    case 3: { PhysEx110 ph; ph.eps1 = P(0); ph.eps2 = P(1); return fn(ph); }
+    case 4: { PhysEx160 ph; ph.eps = P(0); ph.z = P(1); ph.V = P(2); return fn(ph); }
+    case 5: { PhysEx207 ph; ph.eps = P(0); return fn(ph); }
+    case 6: { PhysEx301 ph; return fn(ph); }
+    case 7: { PhysEx440 ph; ph.influx = P(0); return fn(ph); }
+    case 8: { PhysLaplaceDir ph; return fn(ph); }
+    case 11: { PhysNLPoisson ph; return fn(ph); }
+    case 12: { PhysPorous ph; return fn(ph); }
+    case 13: { PhysBipolar ph; ph.lambda2 = P(0); ph.mun = P(1); ph.mup = P(2); ph.taun = P(3); ph.taup = P(4); ph.doping = P(5); ph.V = P(6); return fn(ph); }
+    case 14: { PhysRD2 ph; ph.D1 = P(0); ph.D2 = P(1); ph.k = P(2); return fn(ph); }
+    case 15: { PhysKappaExp ph; ph.fsrc = P(0); return fn(ph); }
+  }
+  return -1;
+}
+
+int nspec_of(int phys) {
+  switch (phys) {
+    case 3: case 4: case 14: return 2;
+    case 13: return 3;
+    case 1: case 2: case 5: case 6: case 7: case 8: case 11: case 12: case 15: return 1;
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void* oracle_create(int dim, int nnodes, const double* coord, int ncells, const int* cellnodes, const int* cellregions,
+                    int nbfaces, const int* bfacenodes, const int* bfaceregions, int physics_id,
+                    const double* params, int nparams, const double* nodedata, int nnodedata,
+                    const double* bfactors, const double* bvalues, int nbregions) {
+  int ns = nspec_of(physics_id);
+  if (ns == 0 || dim < 1 || dim > 3) return nullptr;
+  Oracle* o = new Oracle;
+  o->dim = dim; o->N = nnodes; o->ncells = ncells; o->nbf = nbfaces; o->ns = ns; o->phys = physics_id;
+  o->coord.assign(coord, coord + (size_t)dim * nnodes);
+  o->cellnodes.assign(cellnodes, cellnodes + (size_t)(dim + 1) * ncells);
+  o->cellregions.assign(cellregions, cellregions + ncells);
+  o->bfacenodes.assign(bfacenodes, bfacenodes + (size_t)dim * nbfaces);
+  o->bfaceregions.assign(bfaceregions, bfaceregions + nbfaces);
+  if (nparams > 0) o->params.assign(params, params + nparams);
+  o->nnd = nnodedata;
+  if (nnodedata > 0) o->ndata.assign(nodedata, nodedata + (size_t)nnodedata * nnodes);
+  o->nbregions = nbregions;
+  if (bfactors && bvalues && nbregions > 0) {
+    o->bfactors.assign(bfactors, bfactors + (size_t)ns * nbregions);
+    o->bvalues.assign(bvalues, bvalues + (size_t)ns * nbregions);
+    for (size_t i = 0; i < o->bfactors.size(); ++i)
+      if (o->bfactors[i] != 0.0 || o->bvalues[i] != 0.0) o->has_legacy = true;
+  }
+  setup(*o);
+  return o;
+}
+
+void oracle_destroy(void* h) { delete static_cast<Oracle*>(h); }
+
+int oracle_nspec(void* h) { return static_cast<Oracle*>(h)->ns; }
+int oracle_nedges(void* h) { return static_cast<Oracle*>(h)->E; }
+int64_t oracle_ncandidates(void* h) { return (int64_t) static_cast<Oracle*>(h)->colind.size(); }
+
+// Node volumes (sum over regions) and edge factors (sum over regions), for geometry tests.
+void oracle_factors(void* h, double* nodevol, double* edgefac, int* edgenodes) {
+  Oracle* o = static_cast<Oracle*>(h);
+  for (int K = 0; K < o->N; ++K) { double s = 0; for (auto& p : o->nodefac[K]) s += p.second; nodevol[K] = s; }
+  for (int e = 0; e < o->E; ++e) {
+    double s = 0; for (auto& p : o->edgefac[e]) s += p.second; edgefac[e] = s;
+    edgenodes[2 * e] = o->edgenodes[2 * e]; edgenodes[2 * e + 1] = o->edgenodes[2 * e + 1];
+  }
+}
+
+void oracle_bfacefactors(void* h, double* out) {
+  Oracle* o = static_cast<Oracle*>(h);
+  std::copy(o->bfacenodefac.begin(), o->bfacenodefac.end(), out);
+}
+
+// Evaluate F and J at U (Uold for storage).  keep_pattern != 0 keeps entries created
+// by earlier calls on this handle (ExtendableSparse keeps them across Newton steps).
+int oracle_assemble(void* h, const double* U, const double* Uold, double time, double tstep, double lambda,
+                    double* F, int keep_pattern) {
+  Oracle* o = static_cast<Oracle*>(h);
+  if (!keep_pattern) std::fill(o->present.begin(), o->present.end(), 0);
+  return dispatch(*o, [&](const auto& ph) { return assemble_t(*o, ph, U, Uold, time, tstep, lambda, F); });
+}
+
+// Copy the present entries of the last assembly as CSR (rowptr n+1, colind, vals).  Returns nnz.
+int64_t oracle_csr(void* h, int64_t* rowptr, int* colind, double* vals) {
+  Oracle* o = static_cast<Oracle*>(h);
+  int64_t n = (int64_t)o->N * o->ns, k = 0;
+  if (rowptr) rowptr[0] = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    for (int64_t p = o->rowptr[i]; p < o->rowptr[i + 1]; ++p)
+      if (o->present[p]) {
+        if (colind) colind[k] = o->colind[p];
+        if (vals) vals[k] = o->vals[p];
+        ++k;
+      }
+    if (rowptr) rowptr[i + 1] = k;
+  }
+  return k;
+}
+
+void oracle_init_dirichlet(void* h, double* U, double time, double lambda) {
+  Oracle* o = static_cast<Oracle*>(h);
+  dispatch(*o, [&](const auto& ph) { init_dirichlet_t(*o, ph, U, time, lambda); return 0; });
+}
+
+// Standalone geometry kernels for the form-factor identity test (test/test020_formfactors.jl).
+void oracle_cellfactors(int dim, const double* coord, const int* nodes, double* npar, double* epar) {
+  cellfactors(dim, coord, nodes, npar, epar);
+}
+void oracle_bfacefactors_raw(int dim, const double* coord, const int* nodes, double* npar, double* epar) {
+  bfacefactors(dim, coord, nodes, npar, epar);
+}
+void oracle_fbernoulli_pm(const double* x, double* bp, double* bm, int64_t n) {
+  for (int64_t i = 0; i < n; ++i) fbernoulli_pm(x[i], bp[i], bm[i]);
+}
+
+}  // extern "C"

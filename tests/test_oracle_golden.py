@@ -1,0 +1,135 @@
+"""Pin the CPU oracle against the reference's own golden values and unit tests.
+
+Each case restates a reference example (physics in oracle/vfvm_oracle.cpp, driver
+here) and compares with the `testval` recorded in the example
+(tests/golden/reference_testvals.json, generated from the reference sources by
+tests/golden/make_fixtures.py).  Tolerance: Julia's default isapprox
+(rtol = sqrt(eps)) unless the example states another one.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+RTOL = math.sqrt(np.finfo(float).eps)
+
+
+@pytest.fixture(scope="module")
+def testvals():
+    with open(os.path.join(GOLDEN, "reference_testvals.json")) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="module")
+def grid(vfvm):
+    return vfvm.simplexgrid
+
+
+def lin(n, a=0.0, b=1.0):
+    # the values of Julia's range a:(b-a)/n:b, each correctly rounded
+    return np.array([a + (b - a) * i / n for i in range(n + 1)]) if a == 0.0 else np.array([(a * n + (b - a) * i) / n for i in range(n + 1)])
+
+
+def test_example105(oracle, grid, testvals):
+    g = grid(lin(10))
+    bf = np.full((1, 2), 1e30)
+    bv = np.array([[0.0, 1.0]])
+    s = oracle.OracleSystem(g, "ex105", [1e-3], bfactors=bf, bvalues=bv)
+    u, _ = oracle.solve_step(s, np.full(g.nnodes, 0.5), oracle.Control())
+    assert u.sum() == pytest.approx(testvals["Example105_NonlinearPoisson1D"]["value"], rel=RTOL)
+
+
+def barenblatt(x, t, m):
+    tx = t ** (-1.0 / (m + 1.0))
+    xx = x * tx
+    xx = xx * xx
+    xx = 1 - xx * (m - 1) / (2.0 * m * (m + 1))
+    xx = max(xx, 0.0)
+    return tx * xx ** (1.0 / (m - 1.0))
+
+
+def test_example106_transient(oracle, grid, testvals):
+    X = np.array([(i - 10) / 10 for i in range(21)])
+    g = grid(X)
+    s = oracle.OracleSystem(g, "ex106", [2.0])
+    c = oracle.Control()
+    c.Δt_min = c.Δt_max = c.Δt = 1e-4
+    c.Δu_opt = 1.0
+    ts, sols, _ = oracle.solve_transient(s, np.array([barenblatt(x, 0.001, 2.0) for x in X]), [0.001, 0.01], c)
+    assert sols[-1].sum() == pytest.approx(testvals["Example106_NonlinearDiffusion1D"]["value"], rel=RTOL)
+
+
+def test_example110_two_species(oracle, grid, testvals):
+    g = grid(lin(100))
+    bf = np.full((2, 2), 1e30)
+    bv = np.array([[1.0, 0.0], [1.0, 0.0]])
+    U = np.zeros(2 * g.nnodes)
+    c = oracle.Control()
+    c.damp_initial = 0.1
+    for xeps in [1.0, 0.5, 0.25, 0.1, 0.05, 0.025, 0.01]:
+        s = oracle.OracleSystem(g, "ex110", [xeps, xeps], bfactors=bf, bvalues=bv)
+        U, _ = oracle.solve_step(s, U, c)
+    assert U[4] == pytest.approx(testvals["Example110_ReactionDiffusion1D_TwoSpecies"]["value"], rel=RTOL)
+
+
+def test_example160_bernoulli_sedan(oracle, grid, testvals):
+    g = grid(lin(20))
+    s = oracle.OracleSystem(g, "ex160", [1e-3, -1.0, 5.0])
+    c = oracle.Control()
+    c.Δt_min = 1e-5; c.Δt = 1e-5; c.Δt_grow = 1.1; c.Δt_max = 0.1; c.Δu_opt = 0.1; c.damp_initial = 0.5
+    inival = np.zeros(2 * g.nnodes)
+    inival[1::2] = 0.5
+    ts, sols, _ = oracle.solve_transient(s, inival, [0.0, 10.0], c)
+    # examples/Example160_UnipolarDriftDiffusion1D.jl:262: rtol = 1e-5
+    assert sols[-1].sum() == pytest.approx(testvals["Example160_UnipolarDriftDiffusion1D"]["value"], rel=1e-5)
+
+
+def test_example207_2d_timesteps(oracle, grid, testvals):
+    g = grid(lin(10), lin(10))
+    bf = np.zeros((1, 4)); bv = np.zeros((1, 4))
+    bf[0, 1] = bf[0, 3] = 1e30
+    bv[0, 1] = bv[0, 3] = 0.1
+    s = oracle.OracleSystem(g, "ex207", [1e-2], bfactors=bf, bvalues=bv)
+    inival = np.full(g.nnodes, 0.5)
+    t = 0.0
+    while t < 1.0:
+        t = t + 0.01
+        U, _ = oracle.solve_step(s, inival, oracle.Control(), 0.0, 0.01)
+        inival = U.copy()
+    assert U[14] == pytest.approx(testvals["Example207_NonlinearPoisson2D"]["value"], rel=RTOL)
+
+
+def test_example301_3d(oracle, grid, testvals):
+    g = grid(lin(5), lin(5), lin(5))
+    bf = np.zeros((1, 6)); bv = np.zeros((1, 6))
+    bf[0, 4] = bf[0, 5] = 1e30
+    s = oracle.OracleSystem(g, "ex301", [], bfactors=bf, bvalues=bv)
+    u, _ = oracle.solve_step(s, np.zeros(g.nnodes), oracle.Control())
+    assert u[42] == pytest.approx(testvals["Example301_Laplace3D"]["value"], rel=RTOL)
+
+
+def test_example440_many_instances(oracle, grid, testvals):
+    g = grid(np.array([i / 320 for i in range(321)]))
+    total = 0.0
+    for i in range(100):
+        s = oracle.OracleSystem(g, "ex440", [i * 10.0 / 99.0])
+        c = oracle.Control()
+        c.abstol = 1e-15
+        c.reltol = 1e-20
+        u, _ = oracle.solve_step(s, np.full(g.nnodes, 0.1), c)
+        total += float(np.dot(s.nodevolumes(), u))
+    assert total == pytest.approx(testvals["Example440_ParallelState"]["value"], rel=RTOL)
+
+
+def test_cachesol_linear_exact(oracle, grid):
+    # test/test030_cachesol.jl: 1D Laplace, solution equals x.  The reference pins
+    # 3e-16 with UMFPACK; SuperLU (the stand-in direct solver) gives a few ulps.
+    X = np.array([i / 9 for i in range(10)])
+    s = oracle.OracleSystem(grid(X), "laplace_dirichlet")
+    F, J = s.assemble(np.zeros(10))
+    x = s.linsolve(J, -F)
+    assert np.max(np.abs(x - X)) <= 1e-15

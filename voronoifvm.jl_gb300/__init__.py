@@ -1,0 +1,18 @@
+"""GB300-native assembly + Newton hot path of VoronoiFVM.jl.
+
+The compute path is the CUDA library built from ``csrc/`` (C ABI in
+``include/vfvm_gb300.h``); this package is its host-side mirror of the
+reference's ``System``/``Physics``/``solve``/``SolverControl`` interface.
+"""
+from .grid import Grid, simplexgrid
+from .system import (AssemblyError, ConvergenceError, EmbeddingError, LinearSolverError, NewtonSolverHistory,
+                     Physics, SolverControl, System, TransientSolution, boundary_dirichlet, edgefactors,
+                     evaluate_residual_and_jacobian, fixed_timesteps, integrate, nodevolumes, num_species, solve,
+                     unknowns)
+from . import _lib
+from .build import build_library
+
+__all__ = ["Grid", "simplexgrid", "Physics", "System", "SolverControl", "NewtonSolverHistory", "TransientSolution",
+           "AssemblyError", "ConvergenceError", "EmbeddingError", "LinearSolverError", "boundary_dirichlet",
+           "edgefactors", "evaluate_residual_and_jacobian", "fixed_timesteps", "integrate", "nodevolumes",
+           "num_species", "solve", "unknowns", "build_library"]

@@ -1,0 +1,194 @@
+// Common device/host definitions for the GB300 assembly + Newton library.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <cmath>
+
+#include "../../include/vfvm_gb300.h"
+
+#define VFVM_HD __host__ __device__ __forceinline__
+
+#define VFVM_CUDA(call)                                                                     \
+  do {                                                                                      \
+    cudaError_t _e = (call);                                                                \
+    if (_e != cudaSuccess) {                                                                \
+      fprintf(stderr, "vfvm: CUDA error %s at %s:%d: %s\n", cudaGetErrorName(_e), __FILE__, \
+              __LINE__, cudaGetErrorString(_e));                                            \
+      return VFVM_ERR_CUDA;                                                                 \
+    }                                                                                       \
+  } while (0)
+
+namespace vfvm {
+
+constexpr double kDirichlet = 1.0e30;  // src/vfvm_system.jl:329
+
+// -----------------------------------------------------------------------------
+// Forward-mode dual number mirroring ForwardDiff.Dual with a full chunk
+// (src/vfvm_physics.jl:438): value + N partials.  The value is always FP64.
+// P is the partials' type: double for the FP64 Jacobian (parity mode) or float
+// for the mixed mode, where the Jacobian feeds an FP32 Krylov solve and only the
+// residual (the value path) must be FP64.  GB300 runs FP64 at 1/57 of the FP32
+// rate, so keeping derivative arithmetic in FP32 removes most FP64 instructions
+// from the assembly.
+// -----------------------------------------------------------------------------
+template <int N, typename P = double>
+struct Dual {
+  double v;
+  P d[N];
+};
+
+template <int N, typename P> VFVM_HD Dual<N, P> dconst(double v) {
+  Dual<N, P> r; r.v = v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = P(0);
+  return r;
+}
+template <int N, typename P> VFVM_HD Dual<N, P> dseed(double v, int k) {
+  Dual<N, P> r; r.v = v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = (i == k) ? P(1) : P(0);
+  return r;
+}
+template <int N, typename P> VFVM_HD double val(const Dual<N, P>& a) { return a.v; }
+VFVM_HD double val(double a) { return a; }
+
+template <int N, typename P> VFVM_HD Dual<N, P> operator+(const Dual<N, P>& a, const Dual<N, P>& b) {
+  Dual<N, P> r; r.v = a.v + b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] + b.d[i];
+  return r;
+}
+template <int N, typename P> VFVM_HD Dual<N, P> operator-(const Dual<N, P>& a, const Dual<N, P>& b) {
+  Dual<N, P> r; r.v = a.v - b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] - b.d[i];
+  return r;
+}
+template <int N, typename P> VFVM_HD Dual<N, P> operator-(const Dual<N, P>& a) {
+  Dual<N, P> r; r.v = -a.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -a.d[i];
+  return r;
+}
+template <int N, typename P> VFVM_HD Dual<N, P> operator*(const Dual<N, P>& a, const Dual<N, P>& b) {
+  Dual<N, P> r; r.v = a.v * b.v;
+  const P av = P(a.v), bv = P(b.v);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * bv + av * b.d[i];
+  return r;
+}
+template <int N, typename P> VFVM_HD Dual<N, P> operator/(const Dual<N, P>& a, const Dual<N, P>& b) {
+  Dual<N, P> r; r.v = a.v / b.v;
+  const P ib = P(1.0 / b.v), q = P(r.v);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - q * b.d[i]) * ib;
+  return r;
+}
+template <int N, typename P> VFVM_HD Dual<N, P> operator+(const Dual<N, P>& a, double b) { Dual<N, P> r = a; r.v = a.v + b; return r; }
+template <int N, typename P> VFVM_HD Dual<N, P> operator+(double b, const Dual<N, P>& a) { Dual<N, P> r = a; r.v = b + a.v; return r; }
+template <int N, typename P> VFVM_HD Dual<N, P> operator-(const Dual<N, P>& a, double b) { Dual<N, P> r = a; r.v = a.v - b; return r; }
+template <int N, typename P> VFVM_HD Dual<N, P> operator-(double b, const Dual<N, P>& a) {
+  Dual<N, P> r; r.v = b - a.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -a.d[i];
+  return r;
+}
+template <int N, typename P> VFVM_HD Dual<N, P> operator*(const Dual<N, P>& a, double b) {
+  Dual<N, P> r; r.v = a.v * b; const P bp = P(b);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * bp;
+  return r;
+}
+template <int N, typename P> VFVM_HD Dual<N, P> operator*(double b, const Dual<N, P>& a) { return a * b; }
+template <int N, typename P> VFVM_HD Dual<N, P> operator/(const Dual<N, P>& a, double b) {
+  Dual<N, P> r; r.v = a.v / b; const P ib = P(1.0 / b);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * ib;
+  return r;
+}
+// chain rule helper: r = f(a) with f'(a) = df
+template <int N, typename P> VFVM_HD Dual<N, P> chain(const Dual<N, P>& a, double fv, double df) {
+  Dual<N, P> r; r.v = fv; const P dp = P(df);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = dp * a.d[i];
+  return r;
+}
+template <int N, typename P> VFVM_HD Dual<N, P> exp(const Dual<N, P>& a) { double e = ::exp(a.v); return chain(a, e, e); }
+template <int N, typename P> VFVM_HD Dual<N, P> expm1(const Dual<N, P>& a) { return chain(a, ::expm1(a.v), ::exp(a.v)); }
+template <int N, typename P> VFVM_HD Dual<N, P> log(const Dual<N, P>& a) { return chain(a, ::log(a.v), 1.0 / a.v); }
+template <int N, typename P> VFVM_HD Dual<N, P> log1p(const Dual<N, P>& a) { return chain(a, ::log1p(a.v), 1.0 / (1.0 + a.v)); }
+template <int N, typename P> VFVM_HD Dual<N, P> pow(const Dual<N, P>& a, double p) { return chain(a, ::pow(a.v, p), p * ::pow(a.v, p - 1.0)); }
+template <int N, typename P> VFVM_HD Dual<N, P> sq(const Dual<N, P>& a) { return a * a; }
+template <int N, typename P> VFVM_HD Dual<N, P> cube(const Dual<N, P>& a) { return chain(a, a.v * a.v * a.v, 3.0 * a.v * a.v); }
+template <int N, typename P> VFVM_HD Dual<N, P> dmax(const Dual<N, P>& a, double b) { return a.v >= b ? a : dconst<N, P>(b); }
+
+VFVM_HD double sq(double a) { return a * a; }
+VFVM_HD double cube(double a) { return a * a * a; }
+VFVM_HD double dmax(double a, double b) { return a > b ? a : b; }
+
+// -----------------------------------------------------------------------------
+// Bernoulli function B(x) = x/(exp(x)-1) and B(-x), with the reference's
+// thresholds and Taylor-Horner branch (src/vfvm_functions.jl:2-31,78-90).
+// -----------------------------------------------------------------------------
+template <class T> VFVM_HD T bernoulli_horner(const T& x) {
+  T y = x * (1.0 / 47900160.0);
+  y = x * y;
+  y = x * ((-1.0 / 1209600.0) + y);
+  y = x * y;
+  y = x * ((1.0 / 30240.0) + y);
+  y = x * y;
+  y = x * ((-1.0 / 720.0) + y);
+  y = x * y;
+  y = x * ((1.0 / 12.0) + y);
+  y = x * ((-1.0 / 2.0) + y);
+  return 1.0 + y;
+}
+template <class T> VFVM_HD void fbernoulli_pm(const T& x, T& bp, T& bm) {
+  const double xv = val(x);
+  if (xv < -50.0) { bp = -x; bm = x * 0.0; }
+  else if (xv > 50.0) { bp = x * 0.0; bm = x; }
+  else if (fabs(xv) < 0.25) { bp = bernoulli_horner(x); bm = x + bp; }
+  else { bp = x / expm1(x); bm = x + bp; }
+}
+
+VFVM_HD double ramp(double t, double t0, double t1, double u0, double u1) {  // src/vfvm_physics.jl:516-525
+  if (t < t0) return u0;
+  if (t < t1) return u0 + (u1 - u0) * (t - t0) / (t1 - t0);
+  return u1;
+}
+
+// -----------------------------------------------------------------------------
+// Geometry item views handed to the physics callbacks (the reference's Node,
+// Edge and BNode, src/vfvm_geometryitems.jl:102-578, flattened to what the
+// device functors read).
+// -----------------------------------------------------------------------------
+struct NodeItem {
+  int index, region;
+  const double* x;       // coordinates of the node (dim values)
+  double time, lambda;   // time and embedding parameter
+  const double* data;    // per-node data (nodedata row) or nullptr
+};
+struct EdgeItem {
+  int K, L, region;      // K = first node, L = second node
+  const double* xK; const double* xL;
+  double time, lambda;
+  const double* dataK; const double* dataL;
+};
+struct BNodeItem {
+  int index, region;
+  const double* x;
+  double time, lambda, fac;
+  double Dirichlet;         // penalty (1e30, or 1e30/fac with legacy boundary data)
+  double* dirichlet_value;  // written by boundary_dirichlet (Dirichlet initialisation)
+};
+
+// boundary_dirichlet!(y,u,bnode,ispec,ireg,val), src/vfvm_physics.jl:487-494
+template <class T> VFVM_HD void boundary_dirichlet(T* y, const T* u, const BNodeItem& b, int ispec, int ireg, double v) {
+  if (b.region == ireg) {
+    y[ispec] = y[ispec] + (u[ispec] - v) * b.Dirichlet;
+    if (b.dirichlet_value) b.dirichlet_value[ispec] = v;
+  }
+}
+
+}  // namespace vfvm

@@ -1,0 +1,112 @@
+// Context: device-resident tables and work buffers of one system.
+#pragma once
+#include <vector>
+#include <string>
+#include "vfvm_common.cuh"
+
+namespace vfvm {
+
+// Device buffer that frees itself.
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { release(); }
+  void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+  cudaError_t alloc(size_t count) {
+    release();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(&p, count * sizeof(T));
+  }
+  cudaError_t upload(const std::vector<T>& h) {
+    cudaError_t e = alloc(h.size());
+    if (e != cudaSuccess || h.empty()) return e;
+    return cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+  }
+};
+
+// Tables handed to the assembly kernels by value.
+struct AsmTables {
+  int N, ns, dim;
+  const double* coord;        // N x dim, node-major
+  const int* browptr;         // N+1 block-row pointers
+  const int* bcol;            // block columns (node index), sorted per row
+  const int* diag;            // slot of the diagonal block per row
+  // single-region fast path
+  int region;                 // the single cell region
+  const double* node_fac;     // N
+  const double* slot_fac;     // per slot: edge factor (0 at the diagonal)
+  // multi-region path (nullptr otherwise)
+  const int* nitem_ptr; const int* nitem_reg; const double* nitem_fac;
+  const int* sitem_ptr; const int* sitem_reg; const double* sitem_fac;
+  // boundary-node items grouped by node (bface order within a node)
+  const int* bn_ptr; const int* bn_reg; const double* bn_fac;
+  // physics data
+  const double* params;
+  const double* nodedata; int nnd;
+  const double* bfactors; const double* bvalues; int nbregions; int has_legacy;
+};
+
+struct Workspace;  // Krylov / Newton work buffers (vfvm_solver.cu)
+
+}  // namespace vfvm
+
+struct vfvm_ctx {
+  int dim = 0, N = 0, ncells = 0, nbf = 0, ns = 1, phys = 0, E = 0;
+  int nregions = 1, nbregions = 0, single_region = 1;
+  bool multireg = false;
+  int nparams = 0, nnd = 0;
+  bool has_legacy = false;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+
+  // host tables
+  std::vector<double> h_coord;              // N x dim node-major
+  std::vector<int> h_browptr, h_bcol, h_diag;
+  std::vector<int> h_edgenodes;             // 2E (lo, hi)
+  std::vector<double> h_edgefac, h_nodevol; // summed over regions
+  std::vector<double> h_params;
+  int64_t nnzb = 0;
+
+  // device tables
+  vfvm::DBuf<double> coord, node_fac, slot_fac, nitem_fac, sitem_fac, bn_fac, params, nodedata, bfactors, bvalues;
+  vfvm::DBuf<int> browptr, bcol, diag, nitem_ptr, nitem_reg, sitem_ptr, sitem_reg, bn_ptr, bn_reg;
+  vfvm::DBuf<uint8_t> dirichlet_dof;       // 1 where a Dirichlet penalty acts on the dof
+
+  // scalar (reference) pattern
+  int64_t nnz = 0;
+  std::vector<int64_t> h_rowptr;
+  std::vector<int32_t> h_colind;
+  vfvm::DBuf<int64_t> pmap;                 // scalar entry -> BSR value index
+
+  // multicolour ordering (ILU0)
+  int ncolors = 0;
+  std::vector<int> h_color_ptr;             // ncolors+1
+  vfvm::DBuf<int> color_nodes;              // nodes sorted by (colour, index)
+  vfvm::DBuf<int> lower_ptr, lower_slots;   // per node: lower-colour slots in factorization order
+
+  // assembly buffers
+  vfvm::DBuf<double> U, Uold, F, J;         // J: nnzb*ns*ns
+  vfvm::DBuf<float> Jf;
+  vfvm::DBuf<int> errflag;
+
+  vfvm::Workspace* ws = nullptr;
+
+  vfvm::AsmTables tables() const;
+};
+
+namespace vfvm {
+// assembly launches (vfvm_assembly.cu)
+// tv: device pointer to {time, 1/tstep, lambda}
+int launch_assemble(vfvm_ctx* c, const double* U, const double* Uold, const double* tv, double* F, double* J,
+                    float* Jf, cudaStream_t s);
+int launch_init_dirichlet(vfvm_ctx* c, double* U, const double* tv, cudaStream_t s);
+int launch_pattern_gather(vfvm_ctx* c, const double* J, double* out, cudaStream_t s);
+int probe_masks(int phys, const double* params, int nparams, int dim, std::vector<uint8_t>& node_mask,
+                std::vector<uint8_t>& edge_mask, std::vector<uint8_t>& bnode_mask);
+void destroy_workspace(Workspace* w);
+}  // namespace vfvm

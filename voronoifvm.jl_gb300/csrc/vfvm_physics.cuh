@@ -1,0 +1,281 @@
+// Device physics functors.
+//
+// The reference passes Julia closures flux!/reaction!/storage!/source!/
+// breaction! (src/vfvm_physics.jl:67-182) and differentiates them with
+// ForwardDiff.  Closures cannot cross a C ABI, so each physics used by this
+// library is a registered functor, selected by VFVM_PHYS_* id plus a parameter
+// block.  Every callback is a template over the number type so the same code
+// runs on plain doubles (residual-only evaluation, Dirichlet initialisation)
+// and on Dual<N,P> (residual + Jacobian).
+//
+// Conventions: f, u are arrays of NS species; flux gets the first-node values
+// uK and the second-node values uL of an edge (the reference's u[ispec,1] and
+// u[ispec,2]).
+#pragma once
+#include "vfvm_common.cuh"
+
+namespace vfvm {
+
+struct PhysBase {
+  static constexpr bool has_reaction = false, has_storage = false, has_source = false, has_breaction = false;
+  template <class T> VFVM_HD void reaction(T*, const T*, const NodeItem&) const {}
+  template <class T> VFVM_HD void storage(T*, const T*, const NodeItem&) const {}
+  VFVM_HD void source(double*, const NodeItem&) const {}
+  template <class T> VFVM_HD void breaction(T*, const T*, const BNodeItem&) const {}
+};
+
+// examples/Example105_NonlinearPoisson1D.jl:41-60;  params: eps
+struct PhysEx105 : PhysBase {
+  static constexpr int NS = 1;
+  static constexpr bool has_reaction = true, has_source = true;
+  double eps;
+  VFVM_HD void load(const double* p) { eps = p[0]; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const { f[0] = (uK[0] - uL[0]) * eps; }
+  template <class T> VFVM_HD void reaction(T* f, const T* u, const NodeItem&) const { f[0] = exp(u[0]) - exp(-u[0]); }
+  VFVM_HD void source(double* f, const NodeItem& n) const { f[0] = (n.x[0] <= 0.5) ? 1.0 : -1.0; }
+};
+
+// examples/Example106_NonlinearDiffusion1D.jl:58-68;  params: m
+struct PhysEx106 : PhysBase {
+  static constexpr int NS = 1;
+  static constexpr bool has_storage = true;
+  double m;
+  VFVM_HD void load(const double* p) { m = p[0]; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const { f[0] = pow(uK[0], m) - pow(uL[0], m); }
+  template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const { f[0] = u[0]; }
+};
+
+// examples/Example110_ReactionDiffusion1D_TwoSpecies.jl:40-64;  params: eps1, eps2
+struct PhysEx110 : PhysBase {
+  static constexpr int NS = 2;
+  static constexpr bool has_reaction = true, has_storage = true, has_source = true;
+  double e1, e2;
+  VFVM_HD void load(const double* p) { e1 = p[0]; e2 = p[1]; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const {
+    f[0] = (uK[0] - uL[0]) * e1 * (0.01 + uK[1] + uL[1]);
+    f[1] = (uK[1] - uL[1]) * e2 * (0.01 + uK[0] + uL[0]);
+  }
+  template <class T> VFVM_HD void reaction(T* f, const T* u, const NodeItem&) const { T r = u[0] * u[1]; f[0] = r; f[1] = -r; }
+  template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const { f[0] = u[0]; f[1] = u[1]; }
+  VFVM_HD void source(double* f, const NodeItem& n) const { f[0] = 1.0e-4 * (0.01 + n.x[0]); f[1] = 1.0e-4 * (0.01 + 1.0 - n.x[0]); }
+};
+
+// examples/Example160_UnipolarDriftDiffusion1D.jl:52-84 (sedan flux, species phi, c);  params: eps, z, V
+struct PhysEx160 : PhysBase {
+  static constexpr int NS = 2;
+  static constexpr bool has_reaction = true, has_storage = true, has_breaction = true;
+  double eps, z, V;
+  VFVM_HD void load(const double* p) { eps = p[0]; z = p[1]; V = p[2]; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const {
+    f[0] = (uK[0] - uL[0]) * eps;
+    const double eps_reg = 1.0e-10;
+    T mu1 = -log1p(dmax(-uK[1], -1.0 + eps_reg));
+    T mu2 = -log1p(dmax(-uL[1], -1.0 + eps_reg));
+    T bp, bm;
+    fbernoulli_pm((uK[0] - uL[0]) * (2.0 * z) + (mu1 - mu2), bp, bm);
+    f[1] = bm * uK[1] - bp * uL[1];
+  }
+  template <class T> VFVM_HD void reaction(T* f, const T* u, const NodeItem&) const { f[0] = (1.0 - 2.0 * u[1]) * z; f[1] = u[1] * 0.0; }
+  template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const { f[0] = u[0] * 0.0; f[1] = u[1]; }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const {
+    const double Vt = ramp(b.time, 0.0, 1.0e-2, 0.0, V);
+    boundary_dirichlet(f, u, b, 0, 1, Vt);
+    boundary_dirichlet(f, u, b, 0, 2, 0.0);
+    boundary_dirichlet(f, u, b, 1, 2, 0.5);
+  }
+};
+
+// examples/Example207_NonlinearPoisson2D.jl:36-50;  params: eps
+struct PhysEx207 : PhysBase {
+  static constexpr int NS = 1;
+  static constexpr bool has_reaction = true, has_storage = true, has_source = true;
+  double eps;
+  VFVM_HD void load(const double* p) { eps = p[0]; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const { f[0] = (sq(uK[0]) - sq(uL[0])) * eps; }
+  template <class T> VFVM_HD void reaction(T* f, const T* u, const NodeItem&) const { f[0] = sq(u[0]); }
+  template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const { f[0] = u[0]; }
+  VFVM_HD void source(double* f, const NodeItem& n) const {
+    const double x1 = n.x[0] - 0.5, x2 = n.x[1] - 0.5;
+    f[0] = ::exp(-20.0 * (x1 * x1 + x2 * x2));
+  }
+};
+
+// examples/Example301_Laplace3D.jl:15-24
+struct PhysEx301 : PhysBase {
+  static constexpr int NS = 1;
+  static constexpr bool has_source = true;
+  VFVM_HD void load(const double*) {}
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const { f[0] = uK[0] - uL[0]; }
+  VFVM_HD void source(double* f, const NodeItem& n) const { f[0] = n.x[0] * ::sin(5.0 * n.x[1]) * ::exp(n.x[2]); }
+};
+
+// examples/Example440_ParallelState.jl:16-25;  params: influx
+struct PhysEx440 : PhysBase {
+  static constexpr int NS = 1;
+  static constexpr bool has_breaction = true;
+  double influx;
+  VFVM_HD void load(const double* p) { influx = p[0]; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const { f[0] = sq(uK[0]) - sq(uL[0]); }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const {
+    boundary_dirichlet(f, u, b, 0, 1, 0.1);
+    if (b.region == 2) f[0] = f[0] - influx;  // boundary_neumann!, src/vfvm_physics.jl:533
+  }
+};
+
+// test/test030_cachesol.jl:10-18
+struct PhysLaplaceDir : PhysBase {
+  static constexpr int NS = 1;
+  static constexpr bool has_breaction = true;
+  VFVM_HD void load(const double*) {}
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const { f[0] = uK[0] - uL[0]; }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const {
+    boundary_dirichlet(f, u, b, 0, 1, 0.0);
+    boundary_dirichlet(f, u, b, 0, 2, 1.0);
+  }
+};
+
+// Workload 1: -div(grad u) + u^3 = 1, u = 0 on every boundary region.
+struct PhysNLPoisson : PhysBase {
+  static constexpr int NS = 1;
+  static constexpr bool has_reaction = true, has_breaction = true;
+  VFVM_HD void load(const double*) {}
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const { f[0] = uK[0] - uL[0]; }
+  template <class T> VFVM_HD void reaction(T* f, const T* u, const NodeItem&) const { f[0] = cube(u[0]) - 1.0; }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const { boundary_dirichlet(f, u, b, 0, b.region, 0.0); }
+};
+
+// Workload 2: porous medium u_t - div(grad u^2) = 0, homogeneous Neumann.
+struct PhysPorous : PhysBase {
+  static constexpr int NS = 1;
+  static constexpr bool has_storage = true;
+  VFVM_HD void load(const double*) {}
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const { f[0] = sq(uK[0]) - sq(uL[0]); }
+  template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const { f[0] = u[0]; }
+};
+
+// Workload 3: bipolar drift-diffusion in density variables (psi, n, p), scaled
+// units (thermal voltage 1, intrinsic density 1):
+//   flux_psi = lambda2 (psi_K - psi_L)
+//   flux_n   = mu_n (B(psi_K - psi_L) n_K - B(psi_L - psi_K) n_L)
+//   flux_p   = mu_p (B(psi_L - psi_K) p_K - B(psi_K - psi_L) p_L)
+//   reaction_psi = n - p - C(x),  reaction_n = reaction_p = R,
+//   R = (n p - 1) / (tau_p (n + 1) + tau_n (p + 1))          (SRH)
+//   C = +doping for x < 0.5, -doping otherwise;
+//   ohmic contacts: region 4 (x = 0) at bias 0, region 2 (x = 1) at bias V*lambda.
+// params: lambda2, mu_n, mu_p, tau_n, tau_p, doping, V
+struct PhysBipolar : PhysBase {
+  static constexpr int NS = 3;
+  static constexpr bool has_reaction = true, has_breaction = true;
+  double lambda2, mun, mup, taun, taup, doping, V;
+  VFVM_HD void load(const double* p) { lambda2 = p[0]; mun = p[1]; mup = p[2]; taun = p[3]; taup = p[4]; doping = p[5]; V = p[6]; }
+  VFVM_HD double C(const double* x) const { return x[0] < 0.5 ? doping : -doping; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const {
+    T dpsi = uK[0] - uL[0];
+    f[0] = dpsi * lambda2;
+    T bp, bm;
+    fbernoulli_pm(dpsi, bp, bm);
+    f[1] = (bp * uK[1] - bm * uL[1]) * mun;
+    f[2] = (bm * uK[2] - bp * uL[2]) * mup;
+  }
+  template <class T> VFVM_HD void reaction(T* f, const T* u, const NodeItem& n) const {
+    f[0] = u[1] - u[2] - C(n.x);
+    T r = (u[1] * u[2] - 1.0) / ((u[1] + 1.0) * taup + (u[2] + 1.0) * taun);
+    f[1] = r; f[2] = r;
+  }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const {
+    if (b.region != 2 && b.region != 4) return;
+    const double c = C(b.x);
+    const double nn = 0.5 * c + ::sqrt(0.25 * c * c + 1.0);
+    const double pp = 1.0 / nn;
+    const double bias = (b.region == 2) ? V * b.lambda : 0.0;
+    const double psi = ::asinh(0.5 * c) + bias;
+    boundary_dirichlet(f, u, b, 0, b.region, psi);
+    boundary_dirichlet(f, u, b, 1, b.region, nn);
+    boundary_dirichlet(f, u, b, 2, b.region, pp);
+  }
+};
+
+// Workload 4: two-species reaction-diffusion,
+//   flux_i = D_i (u_i,K - u_i,L);  f1 = k (u1 - u2^2), f2 = -k (u1 - u2^2);
+//   Dirichlet: region 4 (x = 0): u1 = 1, u2 = 0;  region 2 (x = 1): u1 = 0, u2 = 1.
+// params: D1, D2, k
+struct PhysRD2 : PhysBase {
+  static constexpr int NS = 2;
+  static constexpr bool has_reaction = true, has_breaction = true;
+  double D1, D2, k;
+  VFVM_HD void load(const double* p) { D1 = p[0]; D2 = p[1]; k = p[2]; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const {
+    f[0] = (uK[0] - uL[0]) * D1;
+    f[1] = (uK[1] - uL[1]) * D2;
+  }
+  template <class T> VFVM_HD void reaction(T* f, const T* u, const NodeItem&) const {
+    T r = (u[0] - sq(u[1])) * k;
+    f[0] = r; f[1] = -r;
+  }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const {
+    boundary_dirichlet(f, u, b, 0, 4, 1.0);
+    boundary_dirichlet(f, u, b, 1, 4, 0.0);
+    boundary_dirichlet(f, u, b, 0, 2, 0.0);
+    boundary_dirichlet(f, u, b, 1, 2, 1.0);
+  }
+};
+
+// Workload 5: -div(kappa grad u) + exp(u) = f, u = 0 on every boundary; node data
+// kappa, edge coefficient = arithmetic mean of the two node values.  params: f
+struct PhysKappaExp : PhysBase {
+  static constexpr int NS = 1;
+  static constexpr bool has_reaction = true, has_source = true, has_breaction = true;
+  double fsrc;
+  VFVM_HD void load(const double* p) { fsrc = p[0]; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem& e) const {
+    f[0] = (uK[0] - uL[0]) * (0.5 * (e.dataK[0] + e.dataL[0]));
+  }
+  template <class T> VFVM_HD void reaction(T* f, const T* u, const NodeItem&) const { f[0] = exp(u[0]); }
+  VFVM_HD void source(double* f, const NodeItem&) const { f[0] = fsrc; }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const { boundary_dirichlet(f, u, b, 0, b.region, 0.0); }
+};
+
+inline int physics_nspec(int id) {
+  switch (id) {
+    case VFVM_PHYS_EX105: case VFVM_PHYS_EX106: case VFVM_PHYS_EX207: case VFVM_PHYS_EX301:
+    case VFVM_PHYS_EX440: case VFVM_PHYS_LAPLACE_DIRICHLET: case VFVM_PHYS_NLPOISSON:
+    case VFVM_PHYS_POROUS: case VFVM_PHYS_KAPPA_EXP: return 1;
+    case VFVM_PHYS_EX110: case VFVM_PHYS_EX160: case VFVM_PHYS_RD2: return 2;
+    case VFVM_PHYS_BIPOLAR: return 3;
+  }
+  return 0;
+}
+inline int physics_nparams(int id) {
+  switch (id) {
+    case VFVM_PHYS_EX105: case VFVM_PHYS_EX106: case VFVM_PHYS_EX207: case VFVM_PHYS_EX440:
+    case VFVM_PHYS_KAPPA_EXP: return 1;
+    case VFVM_PHYS_EX110: return 2;
+    case VFVM_PHYS_EX160: case VFVM_PHYS_RD2: return 3;
+    case VFVM_PHYS_BIPOLAR: return 7;
+  }
+  return 0;
+}
+inline int physics_nnodedata(int id) { return id == VFVM_PHYS_KAPPA_EXP ? 1 : 0; }
+
+// Calls fn(PhysType{}) for the physics id (host-side dispatch to templated launches).
+template <class Fn>
+int dispatch_physics(int id, Fn&& fn) {
+  switch (id) {
+    case VFVM_PHYS_EX105: return fn(PhysEx105{});
+    case VFVM_PHYS_EX106: return fn(PhysEx106{});
+    case VFVM_PHYS_EX110: return fn(PhysEx110{});
+    case VFVM_PHYS_EX160: return fn(PhysEx160{});
+    case VFVM_PHYS_EX207: return fn(PhysEx207{});
+    case VFVM_PHYS_EX301: return fn(PhysEx301{});
+    case VFVM_PHYS_EX440: return fn(PhysEx440{});
+    case VFVM_PHYS_LAPLACE_DIRICHLET: return fn(PhysLaplaceDir{});
+    case VFVM_PHYS_NLPOISSON: return fn(PhysNLPoisson{});
+    case VFVM_PHYS_POROUS: return fn(PhysPorous{});
+    case VFVM_PHYS_BIPOLAR: return fn(PhysBipolar{});
+    case VFVM_PHYS_RD2: return fn(PhysRD2{});
+    case VFVM_PHYS_KAPPA_EXP: return fn(PhysKappaExp{});
+  }
+  return VFVM_ERR_INPUT;
+}
+
+}  // namespace vfvm

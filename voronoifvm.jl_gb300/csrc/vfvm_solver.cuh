@@ -1,0 +1,72 @@
+// Device-resident Newton + Krylov solver: state, work buffers, graph cache.
+#pragma once
+#include <map>
+#include "vfvm_context.cuh"
+
+namespace vfvm {
+
+constexpr int kThreads = 256;
+constexpr int kMaxRedBlocks = 608;  // 4 per SM on 152 SMs; bounds the reduction partials
+
+// Solver control as the kernels read it (copied from vfvm_control before a launch).
+struct DevControl {
+  double abstol, reltol, tol_round, tol_mono, damp_initial, damp_growth;
+  double reltol_linear, abstol_linear;
+  int maxiters, max_round, is_linear, updatecontrol, maxiters_linear;
+  int pad;
+};
+
+// Newton (solve_step!, src/vfvm_solver.jl:13-222) and BiCGStab state kept in
+// device memory so the whole loop runs without the host.
+struct DevState {
+  // time, tstep^-1, embedding parameter (read by the assembly kernels), fixed step size
+  double time, tstepinv, lambda, dt;
+  // Newton
+  double damp, oldnorm, tolx, rnorm, norm, resnorm, updnorm, dnorm;
+  int niter, nround, finished, status, nlin, nnewton, abort, tot_newton;
+  int tot_lin, nsteps, pad6, pad7;
+  double maxdiff, pad5;
+  // BiCGStab
+  double rho, alpha, omega, beta, tol2, rr, bnorm2, pad2;
+  int kit, kbreak, pad3, pad4;
+  // reduction scratch: tickets
+  unsigned ticket[8];
+};
+
+struct GraphKey {
+  int precision, precon, kind;
+  bool operator<(const GraphKey& o) const {
+    if (precision != o.precision) return precision < o.precision;
+    if (precon != o.precon) return precon < o.precon;
+    return kind < o.kind;
+  }
+};
+
+template <typename KT>
+struct KVecs {
+  DBuf<KT> b, x, r, r0, p, ph, v, s, sh, t, dinv, ilu;
+};
+
+struct Workspace {
+  KVecs<double> k64;
+  KVecs<float> k32;
+  DBuf<double> partials;        // kMaxRedBlocks * 4
+  DBuf<double> Uinit;           // initial value / old solution for the next solve
+  DBuf<int> node_color;         // colour per node
+  DBuf<int> color_nodes_ptr;    // unused placeholder for symmetry
+  DevState* st = nullptr;       // device
+  DevState* st_host = nullptr;  // pinned mirror
+  DevControl* ctl = nullptr;    // device
+  cudaGraphConditionalHandle ncond{}, kcond{};
+  std::map<GraphKey, cudaGraphExec_t> graphs;
+  std::map<GraphKey, cudaGraph_t> graph_defs;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+int ensure_workspace(vfvm_ctx* c, int precision);
+// cached, instantiated Newton graph; kind 0 = solve from Uinit, kind 1 = fixed implicit Euler step
+int get_graph(vfvm_ctx* c, int precision, int precon, int kind, cudaGraphExec_t* out);
+int launch_maxdiff(vfvm_ctx* c, const double* a, const double* b);
+DevControl make_devcontrol(const vfvm_control& c);
+
+}  // namespace vfvm

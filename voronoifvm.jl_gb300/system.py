@@ -1,0 +1,431 @@
+"""Host-side mirror of the VoronoiFVM.jl interface for the assembly + Newton path.
+
+Names, argument meaning and error behaviour follow the reference:
+
+* ``System(grid, physics; species, ...)``  -- src/vfvm_system.jl:215-261
+* ``Physics(...)``                         -- src/vfvm_physics.jl:67-182; here a
+  registered device functor (``kind``) plus its data, because Julia closures
+  cannot cross the C ABI
+* ``boundary_dirichlet(sys, ispec, ireg, val)`` -- the system-level (legacy)
+  Dirichlet data, src/vfvm_system.jl:329 and src/vfvm_assembly.jl:355-387
+* ``SolverControl``, ``fixed_timesteps``   -- src/vfvm_solvercontrol.jl:13-327
+* ``solve(sys; inival, control, times, embed, tstep, time, data)`` --
+  src/vfvm_solver.jl:551-668
+* ``evaluate_residual_and_jacobian``       -- src/vfvm_solver.jl:224-260
+* ``unknowns``, ``nodevolumes``, ``integrate`` -- dense solution layout
+  (src/vfvm_densesolution.jl:11-49) and src/vfvm_postprocess.jl:18-100,397-412
+* exceptions ``ConvergenceError``, ``AssemblyError``, ``LinearSolverError``,
+  ``EmbeddingError`` -- src/vfvm_logging_exceptions.jl:6-29
+
+Solutions are ``numpy`` arrays of shape ``(nspec, nnodes)`` in Fortran order, so
+their memory is the reference's dof order ``inode*nspec + ispec``.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import math
+from typing import Optional, Sequence
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _lib as L
+from .grid import Grid
+
+__all__ = ["Physics", "System", "SolverControl", "NewtonSolverHistory", "TransientSolution",
+           "ConvergenceError", "AssemblyError", "LinearSolverError", "EmbeddingError",
+           "boundary_dirichlet", "solve", "unknowns", "evaluate_residual_and_jacobian",
+           "fixed_timesteps", "nodevolumes", "integrate", "num_species"]
+
+Dirichlet = 1.0e30  # src/vfvm_system.jl:329
+
+
+class ConvergenceError(RuntimeError):
+    """Newton's method did not converge."""
+
+
+class AssemblyError(RuntimeError):
+    """A NaN was assembled."""
+
+
+class LinearSolverError(RuntimeError):
+    """The linear solver failed."""
+
+
+class EmbeddingError(RuntimeError):
+    """Time/embedding step size fell to its minimum without convergence."""
+
+
+def _raise(status: int, what: str = ""):
+    if status == L.OK:
+        return
+    if status == L.ERR_CONVERGENCE:
+        raise ConvergenceError(what or "Newton did not converge")
+    if status == L.ERR_ASSEMBLY:
+        raise AssemblyError(what or "trying to assemble NaN")
+    if status == L.ERR_LINEAR:
+        raise LinearSolverError(what or "linear solver error")
+    if status == L.ERR_EMBEDDING:
+        raise EmbeddingError(what or "minimal step size reached")
+    if status == L.ERR_INPUT:
+        raise ValueError(what or "invalid input to the CUDA library")
+    raise RuntimeError(f"CUDA library error {status} {what}")
+
+
+@dataclasses.dataclass
+class Physics:
+    """Selects a registered device physics functor and its data.
+
+    ``kind``: one of ``_lib.PHYSICS_IDS``; ``data``: its parameter vector;
+    ``nodedata``: optional per-node values (shape ``(nnodes,)`` or
+    ``(nnodedata, nnodes)``)."""
+    kind: str
+    data: Sequence[float] = ()
+    nodedata: Optional[np.ndarray] = None
+
+    @property
+    def physics_id(self) -> int:
+        try:
+            return L.PHYSICS_IDS[self.kind]
+        except KeyError:
+            raise ValueError(f"unknown physics kind {self.kind!r}; known: {sorted(L.PHYSICS_IDS)}")
+
+
+@dataclasses.dataclass
+class SolverControl:
+    """SolverControl with the reference defaults plus the device solver settings."""
+    verbose: bool = False
+    abstol: float = 1.0e-10
+    reltol: float = 1.0e-10
+    maxiters: int = 100
+    tol_round: float = 1.0e-10
+    tol_mono: float = 1.0e-3
+    damp_initial: float = 1.0
+    damp_growth: float = 1.2
+    max_round: int = 1000
+    updatecontrol: bool = True
+    method_linear: str = "bicgstab"
+    precon_linear: str = "ilu0"
+    precision: str = "fp64"
+    reltol_linear: float = 1.0e-4
+    abstol_linear: float = 1.0e-8
+    maxiters_linear: int = 100
+    gmres_restart: int = 30
+    Δp: float = 1.0
+    Δp_max: float = 1.0
+    Δp_min: float = 1.0e-3
+    Δp_grow: float = 1.0
+    Δp_decrease: float = 0.5
+    Δt: float = 0.1
+    Δt_max: float = 1.0
+    Δt_min: float = 1.0e-3
+    Δt_grow: float = 1.2
+    Δt_decrease: float = 0.5
+    Δu_opt: float = 0.1
+    Δu_max_factor: float = 1.2
+    force_first_step: bool = False
+    num_final_steps: int = 5
+    handle_exceptions: bool = False
+    store_all: bool = True
+    log: bool = False
+
+    def to_c(self, is_linear: bool = False) -> L.Control_t:
+        c = L.Control_t()
+        c.abstol, c.reltol, c.maxiters = self.abstol, self.reltol, int(self.maxiters)
+        c.tol_round, c.tol_mono = self.tol_round, self.tol_mono
+        c.damp_initial, c.damp_growth, c.max_round = self.damp_initial, self.damp_growth, int(self.max_round)
+        c.is_linear = int(bool(is_linear))
+        c.updatecontrol = int(bool(self.updatecontrol))
+        c.reltol_linear, c.abstol_linear, c.maxiters_linear = self.reltol_linear, self.abstol_linear, int(self.maxiters_linear)
+        c.krylov = L.KRYLOV[self.method_linear]
+        c.precon = L.PRECON[self.precon_linear]
+        c.precision = L.PRECISION[self.precision]
+        c.gmres_restart = int(self.gmres_restart)
+        c.dt, c.dt_min, c.dt_max, c.dt_grow, c.dt_decrease = self.Δt, self.Δt_min, self.Δt_max, self.Δt_grow, self.Δt_decrease
+        c.dp, c.dp_min, c.dp_max, c.dp_grow, c.dp_decrease = self.Δp, self.Δp_min, self.Δp_max, self.Δp_grow, self.Δp_decrease
+        c.du_opt = min(self.Δu_opt, np.finfo(np.float64).max)
+        c.du_max_factor = self.Δu_max_factor
+        c.num_final_steps = int(self.num_final_steps)
+        c.force_first_step = int(bool(self.force_first_step))
+        c.handle_exceptions = int(bool(self.handle_exceptions))
+        c.store_all = int(bool(self.store_all))
+        return c
+
+
+def fixed_timesteps(control: SolverControl, Δt: float, grow: float = 1.0) -> SolverControl:
+    """fixed_timesteps!(control, Δt; grow), src/vfvm_solvercontrol.jl:320-327."""
+    control.Δt = Δt
+    control.Δt_max = Δt
+    control.Δt_min = Δt
+    control.Δt_grow = grow
+    control.Δu_opt = np.finfo(np.float64).max
+    return control
+
+
+@dataclasses.dataclass
+class NewtonSolverHistory:
+    """Subset of NewtonSolverHistory (src/vfvm_history.jl:10-37) returned by the device solver."""
+    nnewton: int = 0
+    nlin: int = 0
+    nsteps: int = 0
+    updatenorm: float = 0.0
+    resnorm: float = 0.0
+    time: float = 0.0  # seconds
+
+    @classmethod
+    def from_c(cls, h: L.History_t):
+        return cls(h.nnewton, h.nlin, h.nsteps, h.updatenorm, h.resnorm, h.time_ms * 1e-3)
+
+
+class TransientSolution:
+    """Stored steps of a transient/embedding solve (src/vfvm_transientsolution.jl)."""
+
+    def __init__(self, t, u, history=None):
+        self.t = list(t)
+        self.u = list(u)
+        self.history = history
+
+    def __len__(self):
+        return len(self.t)
+
+    def __getitem__(self, i):
+        return self.u[i]
+
+
+class System:
+    """A finite-volume system on a grid with a registered device physics.
+
+    The device context (tables, form factors, matrix pattern) is created on the
+    first call that needs it and rebuilt when the legacy boundary data change."""
+
+    def __init__(self, grid: Grid, physics: Physics, species: Sequence[int] = (1,), is_linear: bool = False,
+                 assembly: str = "edgewise", unknown_storage: str = "dense"):
+        if assembly not in ("edgewise", "cellwise"):
+            raise ValueError("assembly must be :edgewise or :cellwise")
+        if unknown_storage != "dense":
+            raise ValueError("only dense unknown storage is offloaded")
+        self.grid = grid
+        self.physics = physics
+        self.nspec = L.PHYSICS_NSPEC[physics.physics_id]
+        self.species = list(species)
+        self.is_linear = is_linear
+        self.assembly = assembly
+        nb = max(grid.num_bfaceregions, 1)
+        self.boundary_factors = np.zeros((self.nspec, nb), order="F")
+        self.boundary_values = np.zeros((self.nspec, nb), order="F")
+        self._ctx = None
+        self._ctx_key = None
+        self._keep = None
+
+    # -- context management
+    def _marshal(self):
+        g = self.grid
+        keep = {}
+        keep["coord"] = np.asfortranarray(g.coord)  # dim x nnodes column-major
+        keep["cellnodes"] = np.asfortranarray(g.cellnodes, dtype=np.int32)
+        keep["cellregions"] = np.ascontiguousarray(g.cellregions, dtype=np.int32)
+        keep["bfacenodes"] = np.asfortranarray(g.bfacenodes, dtype=np.int32)
+        keep["bfaceregions"] = np.ascontiguousarray(g.bfaceregions, dtype=np.int32)
+        gt = L.Grid_t(g.dim, g.nnodes, g.ncells, g.nbfaces,
+                      L.ptr(keep["coord"]), L.ptr(keep["cellnodes"], L.c_i32), L.ptr(keep["cellregions"], L.c_i32),
+                      L.ptr(keep["bfacenodes"], L.c_i32), L.ptr(keep["bfaceregions"], L.c_i32))
+        params = np.ascontiguousarray(self.physics.data, dtype=np.float64)
+        if params.size == 0:
+            params = np.zeros(1)
+        keep["params"] = params
+        nd = 0
+        ndp = None
+        if self.physics.nodedata is not None:
+            a = np.asarray(self.physics.nodedata, dtype=np.float64)
+            a = a.reshape(-1, g.nnodes) if a.ndim == 1 else a
+            if a.shape[1] != g.nnodes:
+                raise ValueError("nodedata must have nnodes columns")
+            keep["nodedata"] = np.ascontiguousarray(a.T)  # node-major
+            nd = a.shape[0]
+            ndp = L.ptr(keep["nodedata"])
+        keep["bf"] = np.asfortranarray(self.boundary_factors)
+        keep["bv"] = np.asfortranarray(self.boundary_values)
+        pt = L.Physics_t(self.physics.physics_id, len(self.physics.data), L.ptr(params), nd, ndp,
+                         keep["bf"].shape[1], L.ptr(keep["bf"]), L.ptr(keep["bv"]))
+        return gt, pt, keep
+
+    @property
+    def ctx(self):
+        key = (self.boundary_factors.tobytes(), self.boundary_values.tobytes(),
+               None if self.physics.nodedata is None else id(self.physics.nodedata))
+        if self._ctx is None or key != self._ctx_key:
+            lib = L.load()
+            self.close()
+            gt, pt, keep = self._marshal()
+            status = ctypes.c_int(0)
+            h = lib.vfvm_create(ctypes.byref(gt), ctypes.byref(pt), ctypes.byref(status))
+            if not h:
+                _raise(status.value or L.ERR_INPUT, "vfvm_create failed")
+            self._ctx, self._ctx_key, self._keep = h, key, keep
+            self._params = tuple(self.physics.data)
+        elif tuple(self.physics.data) != self._params:
+            self._set_params(self.physics.data)
+        return self._ctx
+
+    def _set_params(self, data):
+        p = np.ascontiguousarray(data, dtype=np.float64)
+        _raise(L.load().vfvm_set_params(self._ctx, L.ptr(p), p.size), "vfvm_set_params")
+        self._params = tuple(data)
+
+    def close(self):
+        if self._ctx is not None:
+            L.load().vfvm_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- sizes
+    @property
+    def nnodes(self) -> int:
+        return self.grid.nnodes
+
+    @property
+    def ndofs(self) -> int:
+        return self.nspec * self.grid.nnodes
+
+    def info(self) -> dict:
+        out = np.zeros(8, dtype=np.int64)
+        _raise(L.load().vfvm_info(self.ctx, L.ptr(out, L.c_i64)))
+        return dict(nspec=int(out[0]), nnodes=int(out[1]), nedges=int(out[2]), nnz=int(out[3]),
+                    nblocks=int(out[4]), ncolors=int(out[5]), dim=int(out[6]), multiregion=bool(out[7]))
+
+    def pattern(self):
+        inf = self.info()
+        rp = np.zeros(self.ndofs + 1, dtype=np.int64)
+        ci = np.zeros(inf["nnz"], dtype=np.int32)
+        _raise(L.load().vfvm_pattern(self.ctx, L.ptr(rp, L.c_i64), L.ptr(ci, L.c_i32)))
+        return rp, ci
+
+
+def num_species(sys: System) -> int:
+    return sys.nspec
+
+
+def boundary_dirichlet(sys: System, ispec: int, ireg: int, val: float):
+    """boundary_dirichlet!(sys, ispec, ireg, val): system-level Dirichlet data
+    (species and region numbers 1-based as in the reference)."""
+    nb = max(sys.boundary_factors.shape[1], ireg)
+    if nb > sys.boundary_factors.shape[1]:
+        bf = np.zeros((sys.nspec, nb), order="F")
+        bv = np.zeros((sys.nspec, nb), order="F")
+        bf[:, :sys.boundary_factors.shape[1]] = sys.boundary_factors
+        bv[:, :sys.boundary_values.shape[1]] = sys.boundary_values
+        sys.boundary_factors, sys.boundary_values = bf, bv
+    sys.boundary_factors[ispec - 1, ireg - 1] = Dirichlet
+    sys.boundary_values[ispec - 1, ireg - 1] = val
+
+
+def unknowns(sys: System, inival=0.0) -> np.ndarray:
+    """Dense solution array (nspec, nnodes), Fortran order."""
+    U = np.empty((sys.nspec, sys.nnodes), order="F")
+    U[...] = inival
+    return U
+
+
+def _flat(U, sys: System) -> np.ndarray:
+    a = np.asarray(U, dtype=np.float64)
+    if a.ndim == 0:
+        return np.full(sys.ndofs, float(a))
+    if a.shape == (sys.nspec, sys.nnodes):
+        return np.ascontiguousarray(a.ravel(order="F"))
+    if a.size == sys.ndofs:
+        return np.ascontiguousarray(a.ravel())
+    raise ValueError(f"expected {sys.ndofs} unknowns, got shape {a.shape}")
+
+
+def _shape(x: np.ndarray, sys: System) -> np.ndarray:
+    return x.reshape((sys.nspec, sys.nnodes), order="F")
+
+
+def evaluate_residual_and_jacobian(sys: System, u, t: float = 0.0, tstep: float = math.inf, embed: float = 0.0,
+                                   init_dirichlet: bool = False, uold=None):
+    """Residual (nspec, nnodes) and Jacobian (scipy CSR) at u, computed on the GPU."""
+    lib = L.load()
+    h = sys.ctx
+    U = _flat(u, sys).copy()
+    if init_dirichlet:
+        _raise(lib.vfvm_init_dirichlet(h, L.ptr(U), t, embed))
+    Uo = U if uold is None else _flat(uold, sys)
+    rp, ci = sys.pattern()
+    F = np.zeros(sys.ndofs)
+    vals = np.zeros(ci.size)
+    _raise(lib.vfvm_assemble(h, L.ptr(U), L.ptr(Uo), t, tstep, embed, L.ptr(F), L.ptr(vals)))
+    J = sp.csr_matrix((vals, ci, rp), shape=(sys.ndofs, sys.ndofs))
+    return _shape(F, sys), J
+
+
+def nodevolumes(sys: System) -> np.ndarray:
+    """Voronoi node volumes (src/vfvm_postprocess.jl:397-412)."""
+    nv = np.zeros(sys.nnodes)
+    _raise(L.load().vfvm_geometry(sys.ctx, L.ptr(nv), None, None))
+    return nv
+
+
+def edgefactors(sys: System):
+    inf = sys.info()
+    ef = np.zeros(inf["nedges"])
+    en = np.zeros((inf["nedges"], 2), dtype=np.int32)
+    _raise(L.load().vfvm_geometry(sys.ctx, None, L.ptr(ef), L.ptr(en, L.c_i32)))
+    return ef, en
+
+
+def integrate(sys: System, U) -> np.ndarray:
+    """integrate(system, U): per species sum of node volume x value
+    (single cell region), src/vfvm_postprocess.jl:94-100."""
+    nv = nodevolumes(sys)
+    return _shape(_flat(U, sys), sys) @ nv
+
+
+def solve(sys: System, inival=0.0, control: Optional[SolverControl] = None, times=None, embed=None,
+          tstep: float = math.inf, time: float = 0.0, data=None, **kwargs):
+    """solve(system; kwargs...) (src/vfvm_solver.jl:551-668).
+
+    Stationary (or one implicit Euler step with ``tstep``) -> solution array with
+    ``.history``-like attribute via the returned ``(U)``; with ``times`` or
+    ``embed`` -> TransientSolution."""
+    control = control if control is not None else SolverControl()
+    for k, v in kwargs.items():
+        if not hasattr(control, k):
+            raise TypeError(f"unknown solve keyword {k!r}")
+        setattr(control, k, v)
+    if data is not None:
+        sys.physics.data = tuple(data)
+    lib = L.load()
+    h = sys.ctx
+    U0 = _flat(inival, sys)
+    c = control.to_c(sys.is_linear)
+    hist = L.History_t()
+    if times is not None or embed is not None:
+        lambdas = np.ascontiguousarray(times if times is not None else embed, dtype=np.float64)
+        transient = times is not None
+        t0 = float(lambdas[0]) if transient else time
+        max_store = 100000 if control.store_all else max(len(lambdas), 1)
+        max_store = min(max_store, max(16, int(2.0e9 // (8 * sys.ndofs))))
+        store = np.zeros((max_store, sys.ndofs))
+        tst = np.zeros(max_store)
+        nst = ctypes.c_int32(0)
+        rc = lib.vfvm_evolve(h, ctypes.byref(c), L.ptr(U0), L.ptr(lambdas), lambdas.size, int(transient), t0,
+                             L.ptr(store), L.ptr(tst), max_store, ctypes.byref(nst), ctypes.byref(hist))
+        _raise(rc, "vfvm_evolve")
+        n = nst.value
+        return TransientSolution(tst[:n].tolist(), [_shape(store[i].copy(), sys) for i in range(n)],
+                                 NewtonSolverHistory.from_c(hist))
+    U = np.zeros(sys.ndofs)
+    rc = lib.vfvm_solve(h, ctypes.byref(c), L.ptr(U0), L.ptr(U), time, tstep, 0.0, ctypes.byref(hist))
+    _raise(rc, "vfvm_solve")
+    out = _shape(U, sys)
+    solve.last_history = NewtonSolverHistory.from_c(hist)
+    return out
+
+
+solve.last_history = None
