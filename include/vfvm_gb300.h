@@ -128,7 +128,8 @@ typedef struct vfvm_history {
 } vfvm_history;
 
 /* Fill *c with the reference defaults (src/vfvm_solvercontrol.jl:30-257) and the
- * device solver defaults (BiCGStab, ILU0, FP64). */
+ * device solver defaults (BiCGStab, ILU0, FP64, abstol_linear = 0: the Krylov
+ * tolerance is relative to the preconditioned right hand side). */
 void vfvm_control_default(vfvm_control* c);
 
 /* Create a context on the current CUDA device: tables, form factors, matrix
@@ -178,6 +179,11 @@ int vfvm_solve_device(vfvm_ctx* ctx, const vfvm_control* control, const double* 
                       double* U_dev, double time, double tstep, double lambda, vfvm_history* hist);
 int vfvm_evolve_fixed_device(vfvm_ctx* ctx, const vfvm_control* control, double* U_dev,
                              double t0, double dt, int32_t nsteps, vfvm_history* hist);
+/* One assembly launch on device buffers (U_dev, Uold_dev, F_dev: n doubles); the
+ * Jacobian goes to the context's block matrix (FP64, or FP32 with
+ * VFVM_PRECISION_MIXED).  Enqueued on the context stream, not synchronised. */
+int vfvm_assemble_device(vfvm_ctx* ctx, const double* U_dev, const double* Uold_dev, double time,
+                         double tstep, double lambda, double* F_dev, int32_t precision);
 void* vfvm_stream(vfvm_ctx* ctx);
 
 #ifdef __cplusplus

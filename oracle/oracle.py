@@ -357,7 +357,7 @@ def solve_transient(osys: OracleSystem, inival, lambdas, control: Control, trans
                 else:
                     solution = newsol
                 if solved:
-                    du = delta(solution, oldsolution, lam, dl)
+                    du = float(delta(solution, oldsolution, lam, dl))
                     if du > du_max_factor * du_opt:
                         solved = False
                 if not solved:

@@ -47,4 +47,4 @@ def test_control_struct_layout(vfvm):
     c = vfvm._lib.Control_t()
     lib.vfvm_control_default(ctypes.byref(c))
     assert c.abstol == 1e-10 and c.maxiters == 100 and c.damp_growth == 1.2 and c.store_all == 1
-    assert c.reltol_linear == 1e-4 and c.maxiters_linear == 100 and c.dt_grow == 1.2
+    assert c.reltol_linear == 1e-4 and c.abstol_linear == 0.0 and c.maxiters_linear == 100 and c.dt_grow == 1.2

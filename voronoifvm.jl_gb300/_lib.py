@@ -75,6 +75,7 @@ SIGNATURES = {
     "vfvm_solve_device": (ctypes.c_int, [c_vp, P(Control_t), c_vp, c_vp, c_d, c_d, c_d, P(History_t)]),
     "vfvm_evolve_fixed_device": (ctypes.c_int, [c_vp, P(Control_t), c_vp, c_d, c_d, c_i32, P(History_t)]),
     "vfvm_stream": (c_vp, [c_vp]),
+    "vfvm_assemble_device": (ctypes.c_int, [c_vp, c_vp, c_vp, c_d, c_d, c_d, c_vp, c_i32]),
 }
 
 _lib = None

@@ -106,6 +106,18 @@ extern "C" int vfvm_assemble(vfvm_ctx* c, const double* U, const double* Uold, d
   return err ? VFVM_ERR_ASSEMBLY : VFVM_OK;
 }
 
+extern "C" int vfvm_assemble_device(vfvm_ctx* c, const double* U_dev, const double* Uold_dev, double time,
+                                    double tstep, double lambda, double* F_dev, int32_t precision) {
+  if (!c || !U_dev || !F_dev) return VFVM_ERR_INPUT;
+  if (precision != VFVM_PRECISION_FP64 && precision != VFVM_PRECISION_MIXED) return VFVM_ERR_INPUT;
+  int rc = ensure_workspace(c, precision);
+  if (rc) return rc;
+  if ((rc = set_time(c, time, tstep, lambda))) return rc;
+  if (precision == VFVM_PRECISION_FP64)
+    return launch_assemble(c, U_dev, Uold_dev ? Uold_dev : U_dev, &c->ws->st->time, F_dev, c->J.p, nullptr, c->stream);
+  return launch_assemble(c, U_dev, Uold_dev ? Uold_dev : U_dev, &c->ws->st->time, F_dev, nullptr, c->Jf.p, c->stream);
+}
+
 extern "C" int vfvm_solve_device(vfvm_ctx* c, const vfvm_control* ctl, const double* inival_dev, double* U_dev,
                                  double time, double tstep, double lambda, vfvm_history* hist) {
   if (!c || !inival_dev || !U_dev) return VFVM_ERR_INPUT;

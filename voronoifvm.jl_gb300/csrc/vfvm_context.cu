@@ -224,7 +224,7 @@ extern "C" void vfvm_control_default(vfvm_control* c) {
   c->tol_round = 1.0e-10; c->tol_mono = 1.0e-3;
   c->damp_initial = 1.0; c->damp_growth = 1.2; c->max_round = 1000;
   c->is_linear = 0; c->updatecontrol = 1;
-  c->reltol_linear = 1.0e-4; c->abstol_linear = 1.0e-8; c->maxiters_linear = 100;
+  c->reltol_linear = 1.0e-4; c->abstol_linear = 0.0; c->maxiters_linear = 100;
   c->krylov = VFVM_KRYLOV_BICGSTAB; c->precon = VFVM_PRECON_ILU0; c->precision = VFVM_PRECISION_FP64;
   c->gmres_restart = 30;
   c->dt = 0.1; c->dt_min = 1.0e-3; c->dt_max = 1.0; c->dt_grow = 1.2; c->dt_decrease = 0.5;

@@ -153,25 +153,42 @@ __global__ void nt_init_kernel(const double* __restrict__ U, int64_t n, DevState
 }
 
 // ---------------------------------------------------------------------------
-// Krylov init: b = F, r = r0 = b, x = v = p = 0; ||b||^2, max|F| off Dirichlet rows.
+// Krylov preparation: b = F, x = p = v = 0; max|F| over non-Dirichlet rows
+// (the residual norm of the Newton loop) and the NaN check of the assembly.
 // ---------------------------------------------------------------------------
 template <typename KT>
-__global__ void kr_init_kernel(const double* __restrict__ F, const uint8_t* __restrict__ dirdof, int64_t n,
-                               KT* __restrict__ b, KT* __restrict__ x, KT* __restrict__ r, KT* __restrict__ r0,
-                               KT* __restrict__ p, KT* __restrict__ v, DevState* st, const DevControl* ctl,
-                               double* partials, int* errflag, cudaGraphConditionalHandle kcond) {
+__global__ void kr_prep_kernel(const double* __restrict__ F, const uint8_t* __restrict__ dirdof, int64_t n,
+                               KT* __restrict__ b, KT* __restrict__ x, KT* __restrict__ p, KT* __restrict__ v,
+                               DevState* st, const DevControl* ctl, double* partials, int* errflag) {
   double acc[2] = {0.0, 0.0};
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double f = F[i];
-    const KT bf = KT(f);
-    b[i] = bf; r[i] = bf; r0[i] = bf; x[i] = KT(0); p[i] = KT(0); v[i] = KT(0);
-    acc[0] += double(bf) * double(bf);
+    b[i] = KT(f); x[i] = KT(0); p[i] = KT(0); v[i] = KT(0);
+    acc[0] += f * f;
     if (!dirdof[i]) acc[1] = fmax(acc[1], fabs(f));
   }
   double out[2];
   if (grid_reduce<2>(acc, 2u, partials, &st->ticket[1], out) && threadIdx.x == 0) {
-    st->bnorm2 = out[0];
     st->resnorm = out[1];
+    if (!ctl->updatecontrol) st->norm = out[1];
+    if (*errflag || isnan(out[0])) st->status = VFVM_ERR_ASSEMBLY;  // NaN assembled: AssemblyError
+  }
+}
+
+// Krylov start on the preconditioned right hand side r = M^-1 b:
+// r0 = r, rho = r.r, tolerance, loop condition.
+template <typename KT>
+__global__ void kr_start_kernel(int64_t n, const KT* __restrict__ r, KT* __restrict__ r0, DevState* st,
+                                const DevControl* ctl, double* partials, cudaGraphConditionalHandle kcond) {
+  double acc[1] = {0.0};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const KT ri = r[i];
+    r0[i] = ri;
+    acc[0] += double(ri) * double(ri);
+  }
+  double out[1];
+  if (grid_reduce<1>(acc, 0u, partials, &st->ticket[7], out) && threadIdx.x == 0) {
+    st->bnorm2 = out[0];
     st->rho = out[0];
     st->alpha = 1.0;
     st->omega = 1.0;
@@ -181,13 +198,27 @@ __global__ void kr_init_kernel(const double* __restrict__ F, const uint8_t* __re
     const double tol = fmax(ctl->abstol_linear, ctl->reltol_linear * sqrt(out[0]));
     st->tol2 = tol * tol;
     st->rr = out[0];
-    if (!ctl->updatecontrol) st->norm = out[1];
     int go = (out[0] > st->tol2 && ctl->maxiters_linear > 0) ? 1 : 0;
-    if (*errflag || isnan(out[0])) {  // NaN assembled: AssemblyError
-      st->status = VFVM_ERR_ASSEMBLY;
-      go = 0;
-    }
+    if (st->status != VFVM_OK || isnan(out[0])) go = 0;
     cudaGraphSetConditional(kcond, go);
+  }
+}
+
+// z = Dinv y (block-Jacobi application)
+template <int NS, typename KT>
+__global__ void jacobi_apply_kernel(int N, const KT* __restrict__ dinv, const KT* __restrict__ y, KT* __restrict__ z) {
+  const int K = blockIdx.x * blockDim.x + threadIdx.x;
+  if (K >= N) return;
+  KT yy[NS];
+#pragma unroll
+  for (int j = 0; j < NS; ++j) yy[j] = y[(size_t)K * NS + j];
+  const KT* D = dinv + (size_t)K * NS * NS;
+#pragma unroll
+  for (int i = 0; i < NS; ++i) {
+    KT acc = KT(0);
+#pragma unroll
+    for (int j = 0; j < NS; ++j) acc += D[i * NS + j] * yy[j];
+    z[(size_t)K * NS + i] = acc;
   }
 }
 
@@ -347,171 +378,134 @@ __global__ void ilu_bwd_kernel(const int* __restrict__ cnodes, int cbeg, int cen
 }
 
 // ---------------------------------------------------------------------------
-// BiCGStab (right preconditioned), one iteration = the kernels below
+// BiCGStab, left preconditioned: solves M^-1 A x = M^-1 b.  The penalty rows of
+// Dirichlet nodes (diagonal 1e30) keep an O(h) flux residual in b; after M^-1
+// those rows weigh 1e-30 and no longer dominate the shadow residual or the norms.
 // ---------------------------------------------------------------------------
-// p = r + beta (p - omega v); with block-Jacobi also ph = Dinv p
-template <int NS, typename KT, bool JAC>
-__global__ void bi_p_kernel(int N, const KT* __restrict__ r, KT* __restrict__ p, const KT* __restrict__ v,
-                            const KT* __restrict__ dinv, KT* __restrict__ ph, const DevState* st) {
-  const int K = blockIdx.x * blockDim.x + threadIdx.x;
-  if (K >= N) return;
+// p = r + beta (p - omega v)
+template <typename KT>
+__global__ void bi_p_kernel(int64_t n, const KT* __restrict__ r, KT* __restrict__ p, const KT* __restrict__ v,
+                            const DevState* st) {
   const KT beta = KT(st->beta), omega = KT(st->omega);
-  KT pv[NS];
-#pragma unroll
-  for (int i = 0; i < NS; ++i) {
-    const size_t q = (size_t)K * NS + i;
-    pv[i] = r[q] + beta * (p[q] - omega * v[q]);
-    p[q] = pv[i];
-  }
-  if (JAC) {
-    const KT* D = dinv + (size_t)K * NS * NS;
-#pragma unroll
-    for (int i = 0; i < NS; ++i) {
-      KT acc = KT(0);
-#pragma unroll
-      for (int j = 0; j < NS; ++j) acc += D[i * NS + j] * pv[j];
-      ph[(size_t)K * NS + i] = acc;
-    }
-  }
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = r[i] + beta * (p[i] - omega * v[i]);
 }
 
 // y = A x over the block pattern; LPR lanes cooperate on one block row.
-// Returns per-thread contribution to dot(w, y) (and dot(y,y) when SECOND).
 template <int NS, int LPR, typename KT>
-__device__ __forceinline__ void spmv_row(int K, const int* __restrict__ browptr, const int* __restrict__ bcol,
+__device__ __forceinline__ void spmv_row(int K, int N, const int* __restrict__ browptr, const int* __restrict__ bcol,
                                          const KT* __restrict__ A, const KT* __restrict__ x, KT (&yK)[NS], int sub) {
 #pragma unroll
   for (int i = 0; i < NS; ++i) yK[i] = KT(0);
-  const int beg = browptr[K], end = browptr[K + 1];
-  for (int s = beg + sub; s < end; s += LPR) {
-    const int m = bcol[s];
-    const KT* Ab = A + (size_t)s * NS * NS;
-    KT xm[NS];
+  if (K < N) {
+    const int beg = browptr[K], end = browptr[K + 1];
+    for (int s = beg + sub; s < end; s += LPR) {
+      const int m = bcol[s];
+      const KT* Ab = A + (size_t)s * NS * NS;
+      KT xm[NS];
 #pragma unroll
-    for (int j = 0; j < NS; ++j) xm[j] = x[(size_t)m * NS + j];
+      for (int j = 0; j < NS; ++j) xm[j] = x[(size_t)m * NS + j];
 #pragma unroll
-    for (int i = 0; i < NS; ++i)
+      for (int i = 0; i < NS; ++i)
 #pragma unroll
-      for (int j = 0; j < NS; ++j) yK[i] += Ab[i * NS + j] * xm[j];
+        for (int j = 0; j < NS; ++j) yK[i] += Ab[i * NS + j] * xm[j];
+    }
   }
+  // every lane of the warp reaches this reduction (rows past N contribute zeros)
 #pragma unroll
   for (int i = 0; i < NS; ++i)
 #pragma unroll
     for (int o = LPR / 2; o > 0; o >>= 1) yK[i] += __shfl_down_sync(0xffffffffu, yK[i], o, LPR);
 }
 
-// v = A ph;  alpha = rho / (r0 . v)
-template <int NS, int LPR, typename KT>
-__global__ void __launch_bounds__(kThreads) bi_spmv1_kernel(int N, const int* __restrict__ browptr,
-                                                            const int* __restrict__ bcol, const KT* __restrict__ A,
-                                                            const KT* __restrict__ ph, const KT* __restrict__ r0,
-                                                            KT* __restrict__ v, DevState* st, double* partials) {
-  const int sub = threadIdx.x % LPR;
-  const int rows_per_block = kThreads / LPR;
-  double acc[1] = {0.0};
-  for (int K0 = blockIdx.x * rows_per_block; K0 < N; K0 += gridDim.x * rows_per_block) {
-    const int K = K0 + threadIdx.x / LPR;
-    KT y[NS];
-    if (K < N) {
-      spmv_row<NS, LPR, KT>(K, browptr, bcol, A, ph, y, sub);
-      if (sub == 0) {
-#pragma unroll
-        for (int i = 0; i < NS; ++i) {
-          v[(size_t)K * NS + i] = y[i];
-          acc[0] += double(r0[(size_t)K * NS + i]) * double(y[i]);
-        }
-      }
-    } else {
-      // keep all lanes in the shuffle pattern of spmv_row
-#pragma unroll
-      for (int i = 0; i < NS; ++i) y[i] = KT(0);
-#pragma unroll
-      for (int i = 0; i < NS; ++i)
-#pragma unroll
-        for (int o = LPR / 2; o > 0; o >>= 1) y[i] += __shfl_down_sync(0xffffffffu, y[i], o, LPR);
-    }
-  }
-  double out[1];
-  if (grid_reduce<1>(acc, 0u, partials, &st->ticket[2], out) && threadIdx.x == 0) {
-    const double r0v = out[0];
-    if (r0v == 0.0 || isnan(r0v)) { st->kbreak = 1; st->alpha = 0.0; }
-    else st->alpha = st->rho / r0v;
-  }
-}
-
-// s = r - alpha v;  with block-Jacobi also sh = Dinv s
-template <int NS, typename KT, bool JAC>
-__global__ void bi_s_kernel(int N, const KT* __restrict__ r, const KT* __restrict__ v, KT* __restrict__ s,
-                            const KT* __restrict__ dinv, KT* __restrict__ sh, const DevState* st) {
-  const int K = blockIdx.x * blockDim.x + threadIdx.x;
-  if (K >= N) return;
-  const KT alpha = KT(st->alpha);
-  KT sv[NS];
-#pragma unroll
-  for (int i = 0; i < NS; ++i) {
-    const size_t q = (size_t)K * NS + i;
-    sv[i] = r[q] - alpha * v[q];
-    s[q] = sv[i];
-  }
-  if (JAC) {
-    const KT* D = dinv + (size_t)K * NS * NS;
-#pragma unroll
-    for (int i = 0; i < NS; ++i) {
-      KT acc = KT(0);
-#pragma unroll
-      for (int j = 0; j < NS; ++j) acc += D[i * NS + j] * sv[j];
-      sh[(size_t)K * NS + i] = acc;
-    }
-  }
-}
-
-// t = A sh;  omega = (t.s)/(t.t)
-template <int NS, int LPR, typename KT>
-__global__ void __launch_bounds__(kThreads) bi_spmv2_kernel(int N, const int* __restrict__ browptr,
-                                                            const int* __restrict__ bcol, const KT* __restrict__ A,
-                                                            const KT* __restrict__ sh, const KT* __restrict__ s,
-                                                            KT* __restrict__ t, DevState* st, double* partials) {
+// MODE 0: out = A x (no reduction)
+// MODE 1: out = Dinv A x;  alpha = rho / (r0 . out)            (w = r0)
+// MODE 2: out = Dinv A x;  omega = (out . s) / (out . out)      (w = s)
+template <int NS, int LPR, typename KT, int MODE>
+__global__ void __launch_bounds__(kThreads) spmv_kernel(int N, const int* __restrict__ browptr,
+                                                        const int* __restrict__ bcol, const KT* __restrict__ A,
+                                                        const KT* __restrict__ x, const KT* __restrict__ dinv,
+                                                        const KT* __restrict__ w, KT* __restrict__ out, DevState* st,
+                                                        double* partials) {
   const int sub = threadIdx.x % LPR;
   const int rows_per_block = kThreads / LPR;
   double acc[2] = {0.0, 0.0};
   for (int K0 = blockIdx.x * rows_per_block; K0 < N; K0 += gridDim.x * rows_per_block) {
     const int K = K0 + threadIdx.x / LPR;
     KT y[NS];
-    if (K < N) {
-      spmv_row<NS, LPR, KT>(K, browptr, bcol, A, sh, y, sub);
-      if (sub == 0) {
+    spmv_row<NS, LPR, KT>(K, N, browptr, bcol, A, x, y, sub);
+    if (K < N && sub == 0) {
+      if (MODE == 0) {
+#pragma unroll
+        for (int i = 0; i < NS; ++i) out[(size_t)K * NS + i] = y[i];
+      } else {
+        const KT* D = dinv + (size_t)K * NS * NS;
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
-          t[(size_t)K * NS + i] = y[i];
-          acc[0] += double(y[i]) * double(s[(size_t)K * NS + i]);
-          acc[1] += double(y[i]) * double(y[i]);
+          KT z = KT(0);
+#pragma unroll
+          for (int j = 0; j < NS; ++j) z += D[i * NS + j] * y[j];
+          out[(size_t)K * NS + i] = z;
+          const double wz = double(w[(size_t)K * NS + i]);
+          acc[0] += wz * double(z);
+          acc[1] += double(z) * double(z);
         }
       }
-    } else {
-#pragma unroll
-      for (int i = 0; i < NS; ++i) y[i] = KT(0);
-#pragma unroll
-      for (int i = 0; i < NS; ++i)
-#pragma unroll
-        for (int o = LPR / 2; o > 0; o >>= 1) y[i] += __shfl_down_sync(0xffffffffu, y[i], o, LPR);
     }
   }
-  double out[2];
-  if (grid_reduce<2>(acc, 0u, partials, &st->ticket[3], out) && threadIdx.x == 0) {
-    st->omega = (out[1] > 0.0) ? out[0] / out[1] : 0.0;
+  if (MODE == 0) return;
+  double res[2];
+  if (grid_reduce<2>(acc, 0u, partials, &st->ticket[2], res) && threadIdx.x == 0) {
+    if (MODE == 1) {
+      const double r0v = res[0];
+      if (r0v == 0.0 || isnan(r0v)) { st->kbreak = 1; st->alpha = 0.0; }
+      else st->alpha = st->rho / r0v;
+    } else {
+      st->omega = (res[1] > 0.0) ? res[0] / res[1] : 0.0;
+    }
   }
 }
 
-// x += alpha ph + omega sh;  r = s - omega t;  rho_new = r0.r;  convergence test
-template <int NS, typename KT>
+// dot products after an ILU0 application (same outputs as MODE 1 / MODE 2)
+template <typename KT, int MODE>
+__global__ void dot_kernel(int64_t n, const KT* __restrict__ z, const KT* __restrict__ w, DevState* st,
+                           double* partials) {
+  double acc[2] = {0.0, 0.0};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double zz = double(z[i]);
+    acc[0] += double(w[i]) * zz;
+    acc[1] += zz * zz;
+  }
+  double res[2];
+  if (grid_reduce<2>(acc, 0u, partials, &st->ticket[3], res) && threadIdx.x == 0) {
+    if (MODE == 1) {
+      const double r0v = res[0];
+      if (r0v == 0.0 || isnan(r0v)) { st->kbreak = 1; st->alpha = 0.0; }
+      else st->alpha = st->rho / r0v;
+    } else {
+      st->omega = (res[1] > 0.0) ? res[0] / res[1] : 0.0;
+    }
+  }
+}
+
+// s = r - alpha v
+template <typename KT>
+__global__ void bi_s_kernel(int64_t n, const KT* __restrict__ r, const KT* __restrict__ v, KT* __restrict__ s,
+                            const DevState* st) {
+  const KT alpha = KT(st->alpha);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s[i] = r[i] - alpha * v[i];
+}
+
+// x += alpha p + omega s;  r = s - omega t;  rho_new = r0.r;  convergence test
+template <typename KT>
 __global__ void bi_xr_kernel(int64_t n, KT* __restrict__ x, KT* __restrict__ r, const KT* __restrict__ s,
-                             const KT* __restrict__ t, const KT* __restrict__ ph, const KT* __restrict__ sh,
-                             const KT* __restrict__ r0, DevState* st, const DevControl* ctl, double* partials,
-                             cudaGraphConditionalHandle kcond) {
+                             const KT* __restrict__ t, const KT* __restrict__ p, const KT* __restrict__ r0,
+                             DevState* st, const DevControl* ctl, double* partials, cudaGraphConditionalHandle kcond) {
   const KT alpha = KT(st->alpha), omega = KT(st->omega);
   double acc[2] = {0.0, 0.0};
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] += alpha * ph[i] + omega * sh[i];
+    x[i] += alpha * p[i] + omega * s[i];
     const KT rn = s[i] - omega * t[i];
     r[i] = rn;
     acc[0] += double(r0[i]) * double(rn);
@@ -525,7 +519,7 @@ __global__ void bi_xr_kernel(int64_t n, KT* __restrict__ x, KT* __restrict__ r, 
     st->nlin += 1;
     st->tot_lin += 1;
     st->rr = out[1];
-    bool brk = st->kbreak || rho_new == 0.0 || om == 0.0 || isnan(out[1]);
+    const bool brk = st->kbreak || rho_new == 0.0 || om == 0.0 || isnan(out[1]);
     st->beta = brk ? 0.0 : (rho_new / st->rho) * (st->alpha / om);
     st->rho = rho_new;
     const int go = (!brk && out[1] > st->tol2 && st->kit < ctl->maxiters_linear) ? 1 : 0;
@@ -693,49 +687,69 @@ static int choose_lpr(const vfvm_ctx* c) {
   return 32;
 }
 
+template <int NS, typename KT>
+static void record_ilu_apply(vfvm_ctx* c, KVecs<KT>& k, const KT* y, KT* z, cudaStream_t s) {
+  Workspace* w = c->ws;
+  for (int q = 0; q < c->ncolors; ++q) {
+    const int cb = c->h_color_ptr[q], ce = c->h_color_ptr[q + 1];
+    const int b = (ce - cb + 127) / 128;
+    if (b > 0)
+      ilu_fwd_kernel<NS, KT><<<b, 128, 0, s>>>(c->color_nodes.p, cb, ce, c->lower_ptr.p, c->lower_slots.p, c->bcol.p,
+                                              k.ilu.p, y, z);
+  }
+  for (int q = c->ncolors - 1; q >= 0; --q) {
+    const int cb = c->h_color_ptr[q], ce = c->h_color_ptr[q + 1];
+    const int b = (ce - cb + 127) / 128;
+    if (b > 0)
+      ilu_bwd_kernel<NS, KT><<<b, 128, 0, s>>>(c->color_nodes.p, cb, ce, w->node_color.p, c->browptr.p, c->bcol.p,
+                                               k.ilu.p, k.dinv.p, z);
+  }
+}
+
+// z = M^-1 y
+template <int NS, typename KT>
+static void record_precon_apply(vfvm_ctx* c, KVecs<KT>& k, int precon, const KT* y, KT* z, cudaStream_t s) {
+  if (precon == VFVM_PRECON_JACOBI)
+    jacobi_apply_kernel<NS, KT><<<(c->N + 127) / 128, 128, 0, s>>>(c->N, k.dinv.p, y, z);
+  else
+    record_ilu_apply<NS, KT>(c, k, y, z, s);
+}
+
 template <int NS, int LPR, typename KT>
 static void record_krylov_iteration(vfvm_ctx* c, KVecs<KT>& k, const KT* A, int precon, cudaGraphConditionalHandle kcond,
                                     cudaStream_t s) {
   Workspace* w = c->ws;
   const int N = c->N;
   const int64_t n = (int64_t)N * NS;
-  const int nb = (N + kThreads - 1) / kThreads;
   const int rpb = kThreads / LPR;
   int sblocks = (N + rpb - 1) / rpb;
   if (sblocks > kMaxRedBlocks) sblocks = kMaxRedBlocks;
   const bool jac = precon == VFVM_PRECON_JACOBI;
-  auto ilu_apply = [&](const KT* y, KT* z) {
-    for (int q = 0; q < c->ncolors; ++q) {
-      const int cb = c->h_color_ptr[q], ce = c->h_color_ptr[q + 1];
-      const int b = (ce - cb + 127) / 128;
-      if (b > 0)
-        ilu_fwd_kernel<NS, KT><<<b, 128, 0, s>>>(c->color_nodes.p, cb, ce, c->lower_ptr.p, c->lower_slots.p, c->bcol.p,
-                                                k.ilu.p, y, z);
-    }
-    for (int q = c->ncolors - 1; q >= 0; --q) {
-      const int cb = c->h_color_ptr[q], ce = c->h_color_ptr[q + 1];
-      const int b = (ce - cb + 127) / 128;
-      if (b > 0)
-        ilu_bwd_kernel<NS, KT><<<b, 128, 0, s>>>(c->color_nodes.p, cb, ce, w->node_color.p, c->browptr.p, c->bcol.p,
-                                                 k.ilu.p, k.dinv.p, z);
-    }
-  };
-  if (jac) bi_p_kernel<NS, KT, true><<<nb, kThreads, 0, s>>>(N, k.r.p, k.p.p, k.v.p, k.dinv.p, k.ph.p, w->st);
-  else {
-    bi_p_kernel<NS, KT, false><<<nb, kThreads, 0, s>>>(N, k.r.p, k.p.p, k.v.p, k.dinv.p, k.ph.p, w->st);
-    ilu_apply(k.p.p, k.ph.p);
+  const int eb = red_blocks(n);
+  bi_p_kernel<KT><<<eb, kThreads, 0, s>>>(n, k.r.p, k.p.p, k.v.p, w->st);
+  // v = M^-1 A p,  alpha = rho / (r0 . v)
+  if (jac) {
+    spmv_kernel<NS, LPR, KT, 1><<<sblocks, kThreads, 0, s>>>(N, c->browptr.p, c->bcol.p, A, k.p.p, k.dinv.p, k.r0.p,
+                                                             k.v.p, w->st, w->partials.p);
+  } else {
+    spmv_kernel<NS, LPR, KT, 0><<<sblocks, kThreads, 0, s>>>(N, c->browptr.p, c->bcol.p, A, k.p.p, nullptr, nullptr,
+                                                             k.b.p, w->st, w->partials.p);
+    record_ilu_apply<NS, KT>(c, k, k.b.p, k.v.p, s);
+    dot_kernel<KT, 1><<<eb, kThreads, 0, s>>>(n, k.v.p, k.r0.p, w->st, w->partials.p);
   }
-  bi_spmv1_kernel<NS, LPR, KT><<<sblocks, kThreads, 0, s>>>(N, c->browptr.p, c->bcol.p, A, k.ph.p, k.r0.p, k.v.p, w->st,
-                                                            w->partials.p);
-  if (jac) bi_s_kernel<NS, KT, true><<<nb, kThreads, 0, s>>>(N, k.r.p, k.v.p, k.s.p, k.dinv.p, k.sh.p, w->st);
-  else {
-    bi_s_kernel<NS, KT, false><<<nb, kThreads, 0, s>>>(N, k.r.p, k.v.p, k.s.p, k.dinv.p, k.sh.p, w->st);
-    ilu_apply(k.s.p, k.sh.p);
+  bi_s_kernel<KT><<<eb, kThreads, 0, s>>>(n, k.r.p, k.v.p, k.s.p, w->st);
+  // t = M^-1 A s,  omega = (t . s) / (t . t)
+  if (jac) {
+    spmv_kernel<NS, LPR, KT, 2><<<sblocks, kThreads, 0, s>>>(N, c->browptr.p, c->bcol.p, A, k.s.p, k.dinv.p, k.s.p,
+                                                             k.t.p, w->st, w->partials.p);
+  } else {
+    spmv_kernel<NS, LPR, KT, 0><<<sblocks, kThreads, 0, s>>>(N, c->browptr.p, c->bcol.p, A, k.s.p, nullptr, nullptr,
+                                                             k.b.p, w->st, w->partials.p);
+    record_ilu_apply<NS, KT>(c, k, k.b.p, k.t.p, s);
+    dot_kernel<KT, 2><<<eb, kThreads, 0, s>>>(n, k.t.p, k.s.p, w->st, w->partials.p);
   }
-  bi_spmv2_kernel<NS, LPR, KT><<<sblocks, kThreads, 0, s>>>(N, c->browptr.p, c->bcol.p, A, k.sh.p, k.s.p, k.t.p, w->st,
-                                                            w->partials.p);
-  bi_xr_kernel<NS, KT><<<red_blocks(n), kThreads, 0, s>>>(n, k.x.p, k.r.p, k.s.p, k.t.p, k.ph.p, k.sh.p, k.r0.p, w->st,
-                                                           w->ctl, w->partials.p, kcond);
+  bi_xr_kernel<KT><<<eb, kThreads, 0, s>>>(n, k.x.p, k.r.p, k.s.p, k.t.p, k.p.p, k.r0.p, w->st, w->ctl, w->partials.p,
+                                           kcond);
 }
 
 template <int NS, typename KT, typename MT>
@@ -811,10 +825,12 @@ static int build_graph_t(vfvm_ctx* c, int precision, int precon, int kind, cudaG
   VFVM_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   if (precision == VFVM_PRECISION_FP64) launch_assemble(c, c->U.p, c->Uold.p, &w->st->time, c->F.p, c->J.p, nullptr, s);
   else launch_assemble(c, c->U.p, c->Uold.p, &w->st->time, c->F.p, nullptr, c->Jf.p, s);
-  kr_init_kernel<KT><<<red_blocks(n), kThreads, 0, s>>>(c->F.p, c->dirichlet_dof.p, n, k.b.p, k.x.p, k.r.p, k.r0.p, k.p.p,
-                                                         k.v.p, w->st, w->ctl, w->partials.p, c->errflag.p, kcond);
+  kr_prep_kernel<KT><<<red_blocks(n), kThreads, 0, s>>>(c->F.p, c->dirichlet_dof.p, n, k.b.p, k.x.p, k.p.p, k.v.p,
+                                                         w->st, w->ctl, w->partials.p, c->errflag.p);
   const KT* A = precision == VFVM_PRECISION_FP64 ? (const KT*)c->J.p : (const KT*)c->Jf.p;
   record_precon_setup<NS, KT, KT>(c, k, A, precon, s);
+  record_precon_apply<NS, KT>(c, k, precon, k.b.p, k.r.p, s);  // r = M^-1 b
+  kr_start_kernel<KT><<<red_blocks(n), kThreads, 0, s>>>(n, k.r.p, k.r0.p, w->st, w->ctl, w->partials.p, kcond);
   cudaGraph_t bcap;
   VFVM_CUDA(cudaStreamEndCapture(s, &bcap));
   size_t nb_nodes = 0;
