@@ -233,7 +233,7 @@ def run_ours(args, rank, world):
         torch.distributed.barrier()
     forms = {}
     with ClockSampler(dev) as clk:
-        for form in ("fp64", "mixed"):
+        for form in ("mixed", "fp64"):
             forms[form] = run_form(form, args.steps, args.warmup)
     clocks = clk.summary()
     Uh = U_dev.cpu().numpy()
@@ -324,8 +324,31 @@ def run_ours(args, rank, world):
     return line
 
 
+def run_assembly_only(args):
+    """Profiling mode: build the workload and launch the assembly kernel
+    `--steps` times (FP32-Jacobian form), nothing else."""
+    import ctypes
+    import torch
+    import __graft_entry__ as ge
+    vfvm = ge.load_package()
+    lib = vfvm._lib.load()
+    g, u0 = workload(vfvm, args.nx)
+    sysm = vfvm.System(g, vfvm.Physics("porous"))
+    h = sysm.ctx
+    U = torch.from_numpy(u0).cuda()
+    F = torch.empty_like(U)
+    for _ in range(args.warmup + args.steps):
+        rc = lib.vfvm_assemble_device(h, ctypes.c_void_p(U.data_ptr()), ctypes.c_void_p(U.data_ptr()), 0.0, DT, 0.0,
+                                      ctypes.c_void_p(F.data_ptr()), 1)
+        if rc != 0:
+            raise RuntimeError(f"assembly failed: {rc}")
+    torch.cuda.synchronize()
+    print(json.dumps({"mode": "assembly", "nx": args.nx, "launches": args.warmup + args.steps, **sysm.info()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--mode", choices=["bench", "assembly"], default="bench")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -337,6 +360,9 @@ def main():
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.mode == "assembly":
+        run_assembly_only(args)
+        return
     if args.impl == "reference":
         if world > 1 and rank != 0:
             return

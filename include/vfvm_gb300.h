@@ -186,6 +186,21 @@ int vfvm_assemble_device(vfvm_ctx* ctx, const double* U_dev, const double* Uold_
                          double tstep, double lambda, double* F_dev, int32_t precision);
 void* vfvm_stream(vfvm_ctx* ctx);
 
+/* Device linear solve A x = b for a square CSR matrix: the reference's
+ * linear-solver plug point (control.method_linear, src/vfvm_solvercontrol.jl:106,
+ * called from _solve_linear!, src/vfvm_linsolve.jl:6-61), served by
+ * Jacobi-preconditioned BiCGStab in one persistent cooperative launch.
+ * rowptr (n+1), colind (nnz, 0-based), vals (nnz), b (n), x (n) are device
+ * pointers; x receives the solution (initial guess 0).  Stops when the
+ * preconditioned residual is below max(abstol, reltol * its initial value) or
+ * after maxiters iterations.  The structure is validated on the device first
+ * (VFVM_ERR_INPUT for bad row pointers, columns or a missing diagonal).
+ * Allocates its work memory per call; runs on the legacy default stream. */
+int vfvm_linsolve_csr(int32_t n, int64_t nnz, const int32_t* rowptr, const int32_t* colind,
+                      const double* vals, const double* b, double* x, double reltol, double abstol,
+                      int32_t maxiters, int32_t* iters, double* resnorm);
+
+
 #ifdef __cplusplus
 }
 #endif

@@ -131,7 +131,7 @@ def fixed_timesteps(control: Control, dt: float, grow: float = 1.0) -> Control:
     control.Δt_max = dt
     control.Δt_min = dt
     control.Δt_grow = grow
-    control.Δu_opt = np.finfo(np.float64).max
+    control.Δu_opt = float(np.finfo(np.float64).max)
     return control
 
 

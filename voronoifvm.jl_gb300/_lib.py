@@ -76,6 +76,8 @@ SIGNATURES = {
     "vfvm_evolve_fixed_device": (ctypes.c_int, [c_vp, P(Control_t), c_vp, c_d, c_d, c_i32, P(History_t)]),
     "vfvm_stream": (c_vp, [c_vp]),
     "vfvm_assemble_device": (ctypes.c_int, [c_vp, c_vp, c_vp, c_d, c_d, c_d, c_vp, c_i32]),
+    "vfvm_linsolve_csr": (ctypes.c_int, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_d, c_d, c_i32, P(c_i32),
+                                         P(c_d)]),
 }
 
 _lib = None
