@@ -47,6 +47,7 @@ extern "C" {
 #define VFVM_ERR_INPUT 5        /* bad argument (sizes, ids, indices) */
 #define VFVM_ERR_CUDA 6         /* CUDA runtime error */
 #define VFVM_ERR_EMBEDDING 7    /* step size fell below its minimum in vfvm_evolve */
+#define VFVM_ERR_NOALLOC_LIMIT 8 /* system larger than the fixed work memory of a no-allocation entry point */
 
 /* physics registry: device functors standing in for the Julia callbacks */
 #define VFVM_PHYS_EX105 1             /* Example105 nonlinear Poisson 1D;     params: eps */
@@ -200,6 +201,21 @@ int vfvm_linsolve_csr(int32_t n, int64_t nnz, const int32_t* rowptr, const int32
                       const double* vals, const double* b, double* x, double reltol, double abstol,
                       int32_t maxiters, int32_t* iters, double* resnorm);
 
+/* Same solve without any device allocation, for callers that cannot call
+ * cudaMalloc where they solve (device memory owned by a framework's own pool,
+ * allocation forbidden in the calling region, fixed pre-reserved buffers).
+ * There is no counterpart in the reference.  The caller passes the matrix,
+ * b and x as for vfvm_linsolve_csr; the work vectors live in a fixed
+ * file-scope device array (about 7.7 MB, held by every GPU that loads the
+ * library until exit), which limits n to VFVM_NOALLOC_MAX_ROWS rows: larger
+ * systems return VFVM_ERR_NOALLOC_LIMIT.  The first call on a device looks up
+ * the array's device address (once per device), so make that first call before
+ * any stream capture.  All calls share the array: calls that overlap on the GPU
+ * race on it and must be serialised by the caller. */
+#define VFVM_NOALLOC_MAX_ROWS 131072
+int vfvm_linsolve_csr_noalloc(int32_t n, int64_t nnz, const int32_t* rowptr, const int32_t* colind,
+                              const double* vals, const double* b, double* x, double reltol, double abstol,
+                              int32_t maxiters, int32_t* iters, double* resnorm);
 
 #ifdef __cplusplus
 }

@@ -15,6 +15,8 @@ c_d, c_i32, c_i64, c_vp = ctypes.c_double, ctypes.c_int32, ctypes.c_int64, ctype
 
 # status codes (vfvm_gb300.h)
 OK, ERR_CONVERGENCE, ERR_ASSEMBLY, ERR_LINEAR, ERR_TIMEOUT, ERR_INPUT, ERR_CUDA, ERR_EMBEDDING = range(8)
+ERR_NOALLOC_LIMIT = 8
+NOALLOC_MAX_ROWS = 131072  # VFVM_NOALLOC_MAX_ROWS
 
 PHYSICS_IDS = {
     "ex105": 1, "ex106": 2, "ex110": 3, "ex160": 4, "ex207": 5, "ex301": 6, "ex440": 7,
@@ -78,6 +80,8 @@ SIGNATURES = {
     "vfvm_assemble_device": (ctypes.c_int, [c_vp, c_vp, c_vp, c_d, c_d, c_d, c_vp, c_i32]),
     "vfvm_linsolve_csr": (ctypes.c_int, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_d, c_d, c_i32, P(c_i32),
                                          P(c_d)]),
+    "vfvm_linsolve_csr_noalloc": (ctypes.c_int, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_d, c_d, c_i32,
+                                                 P(c_i32), P(c_d)]),
 }
 
 _lib = None
