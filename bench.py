@@ -51,13 +51,18 @@ def workload(vfvm, nx=NX):
     return g, u0
 
 
+ENGINE = "graph"
+PRECON = "ilu0"
+
+
 def control_for(vfvm, form):
     c = vfvm.fixed_timesteps(vfvm.SolverControl(), DT)
     c.updatecontrol = False      # residual control: norm = max|F| (non-Dirichlet rows)
     c.abstol = FTOL
     c.reltol = 0.0
     c.precision = "mixed" if form == "mixed" else "fp64"
-    c.precon_linear = "ilu0"
+    c.precon_linear = PRECON
+    c.engine = ENGINE
     c.reltol_linear = 1.0e-4
     c.maxiters_linear = 200
     c.store_all = True
@@ -357,7 +362,11 @@ def main():
     ap.add_argument("--nsteps", type=int, default=NSTEPS)
     ap.add_argument("--cpu-solves", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--engine", choices=["persistent", "graph"], default="graph")
+    ap.add_argument("--precon", choices=["ilu0", "jacobi", "block_ilu0"], default=PRECON)
     args = ap.parse_args()
+    globals()["ENGINE"] = args.engine
+    globals()["PRECON"] = args.precon
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.mode == "assembly":

@@ -69,6 +69,8 @@ extern "C" {
 #define VFVM_KRYLOV_GMRES 1
 #define VFVM_PRECON_JACOBI 0   /* (block-)Jacobi: inverse of the nspec x nspec diagonal blocks */
 #define VFVM_PRECON_ILU0 1     /* ILU(0) in multicolour order */
+#define VFVM_PRECON_BLOCK_ILU0 2 /* ILU(0) restricted to each CTA's node range (block-Jacobi with ILU0
+                                    blocks; exact ILU0 when one CTA solves the system) */
 #define VFVM_PRECISION_FP64 0  /* FP64 Jacobian and FP64 Krylov */
 #define VFVM_PRECISION_MIXED 1 /* FP64 residual/update, FP32 Jacobian + FP32 Krylov (Newton refines) */
 
@@ -115,7 +117,12 @@ typedef struct vfvm_control {
   double dp, dp_min, dp_max, dp_grow, dp_decrease;
   double du_opt, du_max_factor;
   int32_t num_final_steps, force_first_step, handle_exceptions, store_all;
+  int32_t engine;              /* VFVM_ENGINE_*: how the device Newton loop is driven */
+  int32_t team_ctas;           /* batched solves: CTAs per system (0 = default) */
 } vfvm_control;
+
+#define VFVM_ENGINE_GRAPH 0      /* CUDA graph of kernels with conditional WHILE nodes */
+#define VFVM_ENGINE_PERSISTENT 1 /* one persistent cooperative launch per solve (or per fixed-step run) */
 
 /* NewtonSolverHistory (src/vfvm_history.jl:10-37), accumulated over a call. */
 typedef struct vfvm_history {
@@ -186,6 +193,28 @@ int vfvm_evolve_fixed_device(vfvm_ctx* ctx, const vfvm_control* control, double*
 int vfvm_assemble_device(vfvm_ctx* ctx, const double* U_dev, const double* Uold_dev, double time,
                          double tstep, double lambda, double* F_dev, int32_t precision);
 void* vfvm_stream(vfvm_ctx* ctx);
+
+/* Batched solves: many systems of one physics, uneven grids and parameters,
+ * solved together in one persistent cooperative launch (a group of CTAs per
+ * system, largest systems first).  The reference solves such sweeps with one
+ * SystemState per thread (examples/Example440_ParallelState.jl:36-45); this is
+ * the device counterpart.  Unknowns are packed system after system
+ * (vfvm_batch_offsets gives the ninst+1 dof offsets). */
+typedef struct vfvm_batch vfvm_batch;
+vfvm_batch* vfvm_batch_create(int32_t ninst, const vfvm_grid* grids, const vfvm_physics_desc* phys, int* status);
+void vfvm_batch_destroy(vfvm_batch* batch);
+int vfvm_batch_offsets(vfvm_batch* batch, int64_t* offsets);
+/* One stationary solve (tstep = INFINITY) or implicit Euler step of every
+ * system from inival; hist (optional) receives one record per system. */
+int vfvm_batch_solve(vfvm_batch* batch, const vfvm_control* control, const double* inival, double* U, double time,
+                     double tstep, double lambda, vfvm_history* hist);
+int vfvm_batch_solve_device(vfvm_batch* batch, const vfvm_control* control, const double* inival_dev, double* U_dev,
+                            double time, double tstep, double lambda, vfvm_history* hist);
+/* Autotuner: times the batch from inival_dev (device) for each candidate number
+ * of CTAs per system, keeps the fastest for later solves of this batch and
+ * reports it in *best_ctas; times_ms[k] = -1 for candidates that do not fit. */
+int vfvm_batch_tune(vfvm_batch* batch, const vfvm_control* control, const double* inival_dev, int32_t* best_ctas,
+                    float* times_ms, int32_t ncand, const int32_t* candidates);
 
 /* Device linear solve A x = b for a square CSR matrix: the reference's
  * linear-solver plug point (control.method_linear, src/vfvm_solvercontrol.jl:106,

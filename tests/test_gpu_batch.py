@@ -1,0 +1,60 @@
+"""Batched solves (one persistent launch for many systems of uneven size)."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from gpu_cases import lin
+
+pytestmark = pytest.mark.gpu
+RTOL = math.sqrt(np.finfo(float).eps)
+
+
+def test_example440_as_one_batch(vfvm):
+    # examples/Example440_ParallelState.jl: 100 data values, one system each; the
+    # reference runs one SystemState per thread, here all 100 solve in one launch
+    with open(os.path.join(GOLDEN, "reference_testvals.json")) as f:
+        testval = json.load(f)["Example440_ParallelState"]["value"]
+    g = vfvm.simplexgrid(np.array([i / 320 for i in range(321)]))
+    systems = [vfvm.System(g, vfvm.Physics("ex440", [i * 10.0 / 99.0])) for i in range(100)]
+    batch = vfvm.BatchSolver(systems)
+    control = vfvm.SolverControl(abstol=1e-15, reltol=1e-20, reltol_linear=1e-12, maxiters_linear=1000)
+    sols = batch.solve([np.full(321, 0.1)] * 100, control=control)
+    total = sum(float(vfvm.integrate(s, u)[0]) for s, u in zip(systems, sols))
+    assert total == pytest.approx(testval, rel=RTOL)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precon", ["jacobi", "ilu0", "block_ilu0"])
+def test_rd2_batch_vs_oracle(vfvm, oracle, precision, precon):
+    rng = np.random.default_rng(7)
+    sizes = [9, 25, 13, 17, 21, 11]
+    systems, params = [], []
+    for n in sizes:
+        p = list(10.0 ** rng.uniform(-1, 1, size=3))
+        params.append(p)
+        systems.append(vfvm.System(vfvm.simplexgrid(lin(n - 1), lin(n - 1)), vfvm.Physics("rd2", p), species=[1, 2]))
+    batch = vfvm.BatchSolver(systems)
+    control = vfvm.SolverControl(precision=precision, precon_linear=precon, maxiters_linear=500)
+    sols = batch.solve([np.full(s.ndofs, 0.5) for s in systems], control=control)
+    for s, p, u in zip(systems, params, sols):
+        osys = oracle.OracleSystem(s.grid, "rd2", p)
+        uo, _ = oracle.solve_step(osys, np.full(osys.n, 0.5), oracle.Control())
+        err = np.max(np.abs(u.ravel(order="F") - uo)) / np.max(np.abs(uo))
+        assert err <= 1e-8
+
+
+def test_batch_tune(vfvm):
+    torch = pytest.importorskip("torch")
+    systems = [vfvm.System(vfvm.simplexgrid(lin(n), lin(n)), vfvm.Physics("nlpoisson")) for n in (8, 16, 24, 32)]
+    batch = vfvm.BatchSolver(systems)
+    u0 = torch.zeros(batch.ndofs, dtype=torch.float64, device="cuda")
+    best, times = batch.tune(u0.data_ptr(), candidates=(1, 2, 4))
+    assert best in (1, 2, 4)
+    assert all(t > 0 for t in times.values())
+    sols = batch.solve([np.zeros(s.ndofs) for s in systems])
+    ref = vfvm.solve(systems[-1], inival=0.0)
+    assert np.max(np.abs(sols[-1] - ref)) <= 1e-8 * np.max(np.abs(ref))

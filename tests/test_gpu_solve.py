@@ -120,23 +120,25 @@ def rel_err(a, b):
     return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
-@pytest.mark.parametrize("precon", ["ilu0", "jacobi"])
+@pytest.mark.parametrize("engine", ["persistent", "graph"])
+@pytest.mark.parametrize("precon", ["ilu0", "jacobi", "block_ilu0"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_nlpoisson_vs_oracle(vfvm, oracle, precon, precision):
+def test_nlpoisson_vs_oracle(vfvm, oracle, precon, precision, engine):
     g = vfvm.simplexgrid(lin(32), lin(32))
     sys = vfvm.System(g, vfvm.Physics("nlpoisson"))
-    control = vfvm.SolverControl(precon_linear=precon, precision=precision, maxiters_linear=400)
+    control = vfvm.SolverControl(precon_linear=precon, precision=precision, maxiters_linear=400, engine=engine)
     U = vfvm.solve(sys, inival=0.0, control=control)
     assert rel_err(U, oracle_solution(oracle, g, "nlpoisson", [])) <= SOL_TOL
 
 
+@pytest.mark.parametrize("engine", ["persistent", "graph"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_porous_fixed_steps_vs_oracle(vfvm, oracle, precision):
+def test_porous_fixed_steps_vs_oracle(vfvm, oracle, precision, engine):
     g = vfvm.simplexgrid(lin(32), lin(32))
     x, y = g.coord
     u0 = 1e-3 + np.exp(-((x - 0.5) ** 2 + (y - 0.5) ** 2) / 0.1 ** 2)
     sys = vfvm.System(g, vfvm.Physics("porous"))
-    control = vfvm.fixed_timesteps(vfvm.SolverControl(precision=precision), 1e-3)
+    control = vfvm.fixed_timesteps(vfvm.SolverControl(precision=precision, engine=engine), 1e-3)
     tsol = vfvm.solve(sys, inival=u0.reshape(1, -1), times=[0.0, 0.005], control=control)
     osys = oracle.OracleSystem(g, "porous")
     oc = oracle.fixed_timesteps(oracle.Control(), 1e-3)

@@ -10,6 +10,7 @@ from .system import (AssemblyError, ConvergenceError, EmbeddingError, LinearSolv
                      evaluate_residual_and_jacobian, fixed_timesteps, integrate, nodevolumes, num_species, solve,
                      unknowns)
 from . import _lib
+from .batch import BatchSolver
 from .build import build_library
 
 __all__ = ["Grid", "simplexgrid", "Physics", "System", "SolverControl", "NewtonSolverHistory", "TransientSolution",

@@ -25,8 +25,9 @@ PHYSICS_IDS = {
 PHYSICS_NSPEC = {1: 1, 2: 1, 3: 2, 4: 2, 5: 1, 6: 1, 7: 1, 8: 1, 11: 1, 12: 1, 13: 3, 14: 2, 15: 1}
 
 KRYLOV = {"bicgstab": 0, "gmres": 1}
-PRECON = {"jacobi": 0, "ilu0": 1}
+PRECON = {"jacobi": 0, "ilu0": 1, "block_ilu0": 2}
 PRECISION = {"fp64": 0, "mixed": 1}
+ENGINE = {"graph": 0, "persistent": 1}
 
 
 class Grid_t(ctypes.Structure):
@@ -51,7 +52,7 @@ class Control_t(ctypes.Structure):
                 ("dp", c_d), ("dp_min", c_d), ("dp_max", c_d), ("dp_grow", c_d), ("dp_decrease", c_d),
                 ("du_opt", c_d), ("du_max_factor", c_d),
                 ("num_final_steps", c_i32), ("force_first_step", c_i32), ("handle_exceptions", c_i32),
-                ("store_all", c_i32)]
+                ("store_all", c_i32), ("engine", c_i32), ("team_ctas", c_i32)]
 
 
 class History_t(ctypes.Structure):
@@ -80,6 +81,12 @@ SIGNATURES = {
     "vfvm_assemble_device": (ctypes.c_int, [c_vp, c_vp, c_vp, c_d, c_d, c_d, c_vp, c_i32]),
     "vfvm_linsolve_csr": (ctypes.c_int, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_d, c_d, c_i32, P(c_i32),
                                          P(c_d)]),
+    "vfvm_batch_create": (c_vp, [c_i32, P(Grid_t), P(Physics_t), P(ctypes.c_int)]),
+    "vfvm_batch_destroy": (None, [c_vp]),
+    "vfvm_batch_offsets": (ctypes.c_int, [c_vp, P(c_i64)]),
+    "vfvm_batch_solve": (ctypes.c_int, [c_vp, P(Control_t), P(c_d), P(c_d), c_d, c_d, c_d, P(History_t)]),
+    "vfvm_batch_solve_device": (ctypes.c_int, [c_vp, P(Control_t), c_vp, c_vp, c_d, c_d, c_d, P(History_t)]),
+    "vfvm_batch_tune": (ctypes.c_int, [c_vp, P(Control_t), c_vp, P(c_i32), P(ctypes.c_float), c_i32, P(c_i32)]),
     "vfvm_linsolve_csr_noalloc": (ctypes.c_int, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_d, c_d, c_i32,
                                                  P(c_i32), P(c_d)]),
 }

@@ -1,0 +1,117 @@
+"""Batched solves of many systems of one physics (uneven grids and parameters).
+
+The reference runs such sweeps as one ``SystemState`` per thread
+(``examples/Example440_ParallelState.jl:36-45``).  Here all systems are solved
+together in one persistent cooperative launch on the GPU: a group of CTAs per
+system, largest systems first, the number of CTAs per system chosen by the
+autotuner (``tune``)."""
+from __future__ import annotations
+
+import ctypes
+import math
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib as L
+from .system import NewtonSolverHistory, SolverControl, System, _flat, _raise, _shape
+
+__all__ = ["BatchSolver"]
+
+
+class BatchSolver:
+    def __init__(self, systems: Sequence[System]):
+        if not systems:
+            raise ValueError("empty batch")
+        kinds = {s.physics.kind for s in systems}
+        if len(kinds) != 1:
+            raise ValueError(f"a batch holds one physics kind, got {sorted(kinds)}")
+        lib = L.load()
+        self.systems = list(systems)
+        marshalled = [s._marshal() for s in self.systems]
+        self._keep = [m[2] for m in marshalled]
+        n = len(self.systems)
+        grids = (L.Grid_t * n)(*[m[0] for m in marshalled])
+        phys = (L.Physics_t * n)(*[m[1] for m in marshalled])
+        status = ctypes.c_int(0)
+        self.h = lib.vfvm_batch_create(n, grids, phys, ctypes.byref(status))
+        if not self.h:
+            _raise(status.value or L.ERR_INPUT, "vfvm_batch_create failed")
+        self.offsets = np.zeros(n + 1, dtype=np.int64)
+        _raise(lib.vfvm_batch_offsets(self.h, L.ptr(self.offsets, L.c_i64)))
+        self.history: List[NewtonSolverHistory] = []
+        self.best_ctas: Optional[int] = None
+
+    @property
+    def ninst(self) -> int:
+        return len(self.systems)
+
+    @property
+    def ndofs(self) -> int:
+        return int(self.offsets[-1])
+
+    def pack(self, inivals) -> np.ndarray:
+        out = np.empty(self.ndofs)
+        for i, (s, u) in enumerate(zip(self.systems, inivals)):
+            out[self.offsets[i]:self.offsets[i + 1]] = _flat(u, s)
+        return out
+
+    def unpack(self, U: np.ndarray):
+        return [_shape(U[self.offsets[i]:self.offsets[i + 1]].copy(), s) for i, s in enumerate(self.systems)]
+
+    def _control(self, control):
+        c = (control or SolverControl()).to_c(False)
+        if self.best_ctas and c.team_ctas == 0:
+            c.team_ctas = self.best_ctas
+        return c
+
+    def solve(self, inivals, control: Optional[SolverControl] = None, time: float = 0.0, tstep: float = math.inf,
+              embed: float = 0.0, check: bool = True):
+        """Solve every system from its initial value; returns the list of solutions."""
+        lib = L.load()
+        U0 = self.pack(inivals)
+        U = np.zeros_like(U0)
+        hist = (L.History_t * self.ninst)()
+        c = self._control(control)
+        rc = lib.vfvm_batch_solve(self.h, ctypes.byref(c), L.ptr(U0), L.ptr(U), time, tstep, embed, hist)
+        self.history = [NewtonSolverHistory.from_c(h) for h in hist]
+        self.status = [h.status for h in hist]
+        if check:
+            _raise(rc, "vfvm_batch_solve")
+        return self.unpack(U)
+
+    def solve_device(self, inival_dev: int, U_dev: int, control: Optional[SolverControl] = None, time: float = 0.0,
+                     tstep: float = math.inf, embed: float = 0.0):
+        """Device-resident variant: pointers to packed device arrays of ndofs doubles."""
+        lib = L.load()
+        hist = (L.History_t * self.ninst)()
+        c = self._control(control)
+        rc = lib.vfvm_batch_solve_device(self.h, ctypes.byref(c), ctypes.c_void_p(inival_dev), ctypes.c_void_p(U_dev),
+                                         time, tstep, embed, hist)
+        self.history = [NewtonSolverHistory.from_c(h) for h in hist]
+        _raise(rc, "vfvm_batch_solve_device")
+        return self.history
+
+    def tune(self, inival_dev: int, control: Optional[SolverControl] = None, candidates=(1, 2, 4, 8)):
+        """Autotune the CTAs per system on this batch (device-resident inival)."""
+        lib = L.load()
+        cand = np.ascontiguousarray(candidates, dtype=np.int32)
+        times = np.zeros(cand.size, dtype=np.float32)
+        best = ctypes.c_int32(0)
+        c = (control or SolverControl()).to_c(False)
+        _raise(lib.vfvm_batch_tune(self.h, ctypes.byref(c), ctypes.c_void_p(inival_dev), ctypes.byref(best),
+                                   times.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), cand.size,
+                                   L.ptr(cand, L.c_i32)), "vfvm_batch_tune")
+        self.best_ctas = int(best.value)
+        return self.best_ctas, dict(zip(cand.tolist(), times.tolist()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            L.load().vfvm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

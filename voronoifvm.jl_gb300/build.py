@@ -27,8 +27,25 @@ def _nvcc():
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libvfvm_gb300.so")
 
 
+# The persistent engine's kernels are instantiated once per registered physics
+# from one source (vfvm_persist_inst.cu), each into its own object, so these
+# heavy instantiations compile in parallel.
+INST_SOURCE = "vfvm_persist_inst.cu"
+INST_PHYSICS = ["PhysEx105", "PhysEx106", "PhysEx110", "PhysEx160", "PhysEx207", "PhysEx301", "PhysEx440",
+                "PhysLaplaceDir", "PhysNLPoisson", "PhysPorous", "PhysBipolar", "PhysRD2", "PhysKappaExp"]
+
+
 def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu") and f != INST_SOURCE)
+
+
+def _units():
+    """(source, object, extra flags) for every object of the library."""
+    units = [(s, os.path.join(BUILD, os.path.basename(s)[:-3] + ".o"), []) for s in sources()]
+    inst = os.path.join(CSRC, INST_SOURCE)
+    for ph in INST_PHYSICS:
+        units.append((inst, os.path.join(BUILD, f"vfvm_persist_inst_{ph}.o"), [f"-DVFVM_INST_PHYS=vfvm::{ph}"]))
+    return units
 
 
 def _headers():
@@ -48,13 +65,13 @@ def build_library(force: bool = False, verbose: bool = False, extra_flags=()) ->
     """Compile (if needed) and return the path of the shared library."""
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
-    srcs = sources()
     hdrs = _headers()
-    objs = [os.path.join(BUILD, os.path.basename(s)[:-3] + ".o") for s in srcs]
+    units = _units()
+    objs = [o for _, o, _ in units]
     jobs = []
-    for s, o in zip(srcs, objs):
+    for s, o, flags in units:
         if force or _stale(o, [s] + hdrs):
-            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, *extra_flags, "-c", s, "-o", o])
+            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, *flags, *extra_flags, "-c", s, "-o", o])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

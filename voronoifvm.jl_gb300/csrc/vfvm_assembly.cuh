@@ -1,0 +1,204 @@
+// Per-node assembly and Dirichlet initialisation, shared by the standalone
+// kernels (vfvm_assembly.cu) and the persistent solvers.
+//
+// One call owns node K: node terms (reaction - source + storage/tstep), every
+// edge incident to K in edge order (the block row's columns are sorted by node
+// index), then K's boundary-face items; it writes F[K], K's off-diagonal
+// Jacobian blocks and its diagonal block.  Returns true if a NaN was produced
+// (AssemblyError in the reference, src/vfvm_assembly.jl:10-12).
+#pragma once
+#include "vfvm_context.cuh"
+#include "vfvm_physics.cuh"
+
+namespace vfvm {
+
+template <class Ph, typename P, bool MR>
+__device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, int K, const double* __restrict__ U,
+                                              const double* __restrict__ Uold, double time, double tstepinv,
+                                              double lambda, double* __restrict__ F, P* __restrict__ J) {
+  constexpr int NS = Ph::NS;
+  double uK[NS];
+#pragma unroll
+  for (int i = 0; i < NS; ++i) uK[i] = U[(size_t)K * NS + i];
+  double fK[NS];
+  P jd[NS * NS];
+#pragma unroll
+  for (int i = 0; i < NS; ++i) fK[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < NS * NS; ++i) jd[i] = P(0);
+  const double* xK = t.coord + (size_t)K * t.dim;
+  const double* dK = t.nodedata ? t.nodedata + (size_t)K * t.nnd : nullptr;
+
+  // ---- node terms: reaction - source + (storage - oldstorage)/tstep
+  const int nbeg = MR ? t.nitem_ptr[K] : 0, nend = MR ? t.nitem_ptr[K + 1] : 1;
+  for (int it = nbeg; it < nend; ++it) {
+    const int reg = MR ? t.nitem_reg[it] : t.region;
+    const double fac = MR ? t.nitem_fac[it] : t.node_fac[K];
+    NodeItem ni{K, reg, xK, time, lambda, dK};
+    Dual<NS, P> u[NS], r[NS], s[NS];
+#pragma unroll
+    for (int i = 0; i < NS; ++i) { u[i] = dseed<NS, P>(uK[i], i); r[i] = dconst<NS, P>(0.0); s[i] = dconst<NS, P>(0.0); }
+    double src[NS], ostor[NS];
+#pragma unroll
+    for (int i = 0; i < NS; ++i) { src[i] = 0.0; ostor[i] = 0.0; }
+    if (Ph::has_source) ph.source(src, ni);
+    if (Ph::has_reaction) ph.reaction(r, u, ni);
+    if (Ph::has_storage) {
+      ph.storage(s, u, ni);
+      double uo[NS];
+#pragma unroll
+      for (int i = 0; i < NS; ++i) uo[i] = Uold[(size_t)K * NS + i];
+      ph.storage(ostor, uo, ni);
+    }
+    const P facp = P(fac), tip = P(tstepinv);
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+      fK[i] += fac * (r[i].v - src[i] + (s[i].v - ostor[i]) * tstepinv);
+#pragma unroll
+      for (int j = 0; j < NS; ++j) jd[i * NS + j] += (r[i].d[j] + s[i].d[j] * tip) * facp;
+    }
+  }
+
+  // ---- edges incident to K, in edge order (columns sorted by node index)
+  const int sbeg = t.browptr[K], send = t.browptr[K + 1];
+  for (int s = sbeg; s < send; ++s) {
+    const int M = t.bcol[s];
+    if (M == K) continue;
+    double uM[NS];
+#pragma unroll
+    for (int i = 0; i < NS; ++i) uM[i] = U[(size_t)M * NS + i];
+    const bool kfirst = K < M;
+    const int A = kfirst ? K : M, B = kfirst ? M : K;
+    P jo[NS * NS];
+#pragma unroll
+    for (int i = 0; i < NS * NS; ++i) jo[i] = P(0);
+    const int ebeg = MR ? t.sitem_ptr[s] : 0, eend = MR ? t.sitem_ptr[s + 1] : 1;
+    for (int it = ebeg; it < eend; ++it) {
+      const int reg = MR ? t.sitem_reg[it] : t.region;
+      const double fac = MR ? t.sitem_fac[it] : t.slot_fac[s];
+      EdgeItem ei{A, B, reg, t.coord + (size_t)A * t.dim, t.coord + (size_t)B * t.dim, time, lambda,
+                  t.nodedata ? t.nodedata + (size_t)A * t.nnd : nullptr,
+                  t.nodedata ? t.nodedata + (size_t)B * t.nnd : nullptr};
+      Dual<2 * NS, P> ua[NS], ub[NS], f[NS];
+#pragma unroll
+      for (int i = 0; i < NS; ++i) {
+        ua[i] = dseed<2 * NS, P>(kfirst ? uK[i] : uM[i], i);
+        ub[i] = dseed<2 * NS, P>(kfirst ? uM[i] : uK[i], NS + i);
+        f[i] = dconst<2 * NS, P>(0.0);
+      }
+      ph.flux(f, ua, ub, ei);
+      const P facp = P(fac);
+      if (kfirst) {
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+          fK[i] += fac * f[i].v;
+#pragma unroll
+          for (int j = 0; j < NS; ++j) {
+            jd[i * NS + j] += f[i].d[j] * facp;
+            jo[i * NS + j] += f[i].d[NS + j] * facp;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+          fK[i] += -(fac * f[i].v);
+#pragma unroll
+          for (int j = 0; j < NS; ++j) {
+            jd[i * NS + j] += (-f[i].d[NS + j]) * facp;
+            jo[i * NS + j] += (-f[i].d[j]) * facp;
+          }
+        }
+      }
+    }
+    if (J) {
+      P* Js = J + (size_t)s * NS * NS;
+#pragma unroll
+      for (int i = 0; i < NS * NS; ++i) Js[i] = jo[i];
+    }
+  }
+
+  // ---- boundary-face items of K (bface order): legacy Dirichlet/Robin + breaction
+  const int bbeg = t.bn_ptr[K], bend = t.bn_ptr[K + 1];
+  for (int it = bbeg; it < bend; ++it) {
+    const int reg = t.bn_reg[it];
+    const double fac = t.bn_fac[it];
+    double Dir = kDirichlet;
+    if (t.has_legacy && reg - 1 < t.nbregions) {
+      Dir = kDirichlet / fac;
+#pragma unroll
+      for (int i = 0; i < NS; ++i) {
+        const double bf = t.bfactors[i + NS * (reg - 1)], bv = t.bvalues[i + NS * (reg - 1)];
+        if (bf == kDirichlet) {
+          fK[i] += bf * (uK[i] - bv);
+          jd[i * NS + i] += P(bf);
+        } else {
+          fK[i] += fac * (bf * uK[i] - bv);
+          if (bf != 0.0) jd[i * NS + i] += P(bf) * P(fac);
+        }
+      }
+    }
+    if (Ph::has_breaction) {
+      BNodeItem bi{K, reg, xK, time, lambda, fac, Dir, nullptr};
+      Dual<NS, P> u[NS], y[NS];
+#pragma unroll
+      for (int i = 0; i < NS; ++i) { u[i] = dseed<NS, P>(uK[i], i); y[i] = dconst<NS, P>(0.0); }
+      ph.breaction(y, u, bi);
+      const P facp = P(fac);
+#pragma unroll
+      for (int i = 0; i < NS; ++i) {
+        fK[i] += fac * y[i].v;
+#pragma unroll
+        for (int j = 0; j < NS; ++j) jd[i * NS + j] += y[i].d[j] * facp;
+      }
+    }
+  }
+
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < NS; ++i) {
+    F[(size_t)K * NS + i] = fK[i];
+    bad |= isnan(fK[i]);
+  }
+  if (J) {
+    P* Jd = J + (size_t)t.diag[K] * NS * NS;
+#pragma unroll
+    for (int i = 0; i < NS * NS; ++i) {
+      Jd[i] = jd[i];
+      bad |= isnan((double)jd[i]);
+    }
+  }
+  return bad;
+}
+
+
+template <class Ph>
+__device__ __forceinline__ void init_dirichlet_node(const AsmTables& t, const Ph& ph, int K, double* __restrict__ U,
+                                                    double time, double lambda) {
+  constexpr int NS = Ph::NS;
+  const int bbeg = t.bn_ptr[K], bend = t.bn_ptr[K + 1];
+  if (bbeg == bend) return;
+  const double* xK = t.coord + (size_t)K * t.dim;
+  double u[NS];
+#pragma unroll
+  for (int i = 0; i < NS; ++i) u[i] = U[(size_t)K * NS + i];
+  for (int it = bbeg; it < bend; ++it) {
+    const int reg = t.bn_reg[it];
+    double dv[NS], y[NS];
+#pragma unroll
+    for (int i = 0; i < NS; ++i) { dv[i] = INFINITY; y[i] = 0.0; }
+    BNodeItem bi{K, reg, xK, time, lambda, t.bn_fac[it], kDirichlet, dv};
+    if (Ph::has_breaction) ph.breaction(y, u, bi);
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+      if (!isinf(dv[i])) u[i] = dv[i];
+      if (t.has_legacy && reg - 1 < t.nbregions) {
+        const double bf = t.bfactors[i + NS * (reg - 1)];
+        if (fabs(bf - kDirichlet) <= 1.4901161193847656e-8 * kDirichlet) u[i] = t.bvalues[i + NS * (reg - 1)];
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < NS; ++i) U[(size_t)K * NS + i] = u[i];
+}
+
+}  // namespace vfvm

@@ -23,6 +23,7 @@ int set_time(vfvm_ctx* c, double time, double tstep, double lambda) {
 }
 
 int set_control(vfvm_ctx* c, const vfvm_control* ctl) {
+  if (ctl->precon == VFVM_PRECON_BLOCK_ILU0 && c->ncolors > kMaxBlockIluColors) return VFVM_ERR_INPUT;
   static thread_local DevControl staged;
   staged = make_devcontrol(*ctl);
   VFVM_CUDA(cudaMemcpyAsync(c->ws->ctl, &staged, sizeof(DevControl), cudaMemcpyHostToDevice, c->stream));
@@ -33,15 +34,28 @@ int set_control(vfvm_ctx* c, const vfvm_control* ctl) {
 int check_control(const vfvm_control* ctl) {
   if (!ctl) return VFVM_ERR_INPUT;
   if (ctl->precision != VFVM_PRECISION_FP64 && ctl->precision != VFVM_PRECISION_MIXED) return VFVM_ERR_INPUT;
-  if (ctl->precon != VFVM_PRECON_JACOBI && ctl->precon != VFVM_PRECON_ILU0) return VFVM_ERR_INPUT;
+  if (ctl->precon != VFVM_PRECON_JACOBI && ctl->precon != VFVM_PRECON_ILU0 && ctl->precon != VFVM_PRECON_BLOCK_ILU0)
+    return VFVM_ERR_INPUT;
   if (ctl->krylov != VFVM_KRYLOV_BICGSTAB) return VFVM_ERR_INPUT;
   return VFVM_OK;
 }
 
 // Runs the Newton graph once from ws->Uinit (already on the device) at the time
 // values set in the state; leaves the result in c->U and the state in st_host.
+bool use_persistent(const vfvm_ctx* c, const vfvm_control* ctl) {
+  return ctl->engine == VFVM_ENGINE_PERSISTENT && !c->multireg;
+}
+
 int run_newton(vfvm_ctx* c, const vfvm_control* ctl, float* ms) {
   Workspace* w = c->ws;
+  if (use_persistent(c, ctl)) {
+    const size_t n = (size_t)c->N * c->ns;
+    VFVM_CUDA(cudaMemcpyAsync(c->U.p, w->Uinit.p, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    VFVM_CUDA(cudaMemcpyAsync(c->Uold.p, w->Uinit.p, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    const DevState* h = w->st_host;
+    PersistRunHost run{0, h->time, 1.0 / h->tstepinv, h->lambda, 0.0, 0.0};
+    return persistent_solve(c, ctl, run, nullptr, ms);
+  }
   cudaGraphExec_t exec;
   int rc = get_graph(c, ctl->precision, ctl->precon, 0, &exec);
   if (rc != VFVM_OK) return rc;
@@ -166,6 +180,15 @@ extern "C" int vfvm_evolve_fixed_device(vfvm_ctx* c, const vfvm_control* ctl, do
   Workspace* w = c->ws;
   const size_t n = (size_t)c->N * c->ns;
   if ((rc = set_control(c, ctl))) return rc;
+  if (use_persistent(c, ctl)) {
+    VFVM_CUDA(cudaMemcpyAsync(c->U.p, U_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    PersistRunHost run{nsteps, t0, dt, 0.0, t0, dt};
+    float ms = 0;
+    rc = persistent_solve(c, ctl, run, hist, &ms);
+    VFVM_CUDA(cudaMemcpyAsync(U_dev, c->U.p, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    VFVM_CUDA(cudaStreamSynchronize(c->stream));
+    return rc;
+  }
   cudaGraphExec_t exec;
   if ((rc = get_graph(c, ctl->precision, ctl->precon, 1, &exec))) return rc;
   DevState* h = w->st_host;

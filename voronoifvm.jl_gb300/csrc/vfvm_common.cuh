@@ -22,6 +22,7 @@
 namespace vfvm {
 
 constexpr double kDirichlet = 1.0e30;  // src/vfvm_system.jl:329
+constexpr int kMaxBlockIluColors = 32; // colour limit of the subdomain ILU0 preconditioner
 
 // -----------------------------------------------------------------------------
 // Forward-mode dual number mirroring ForwardDiff.Dual with a full chunk

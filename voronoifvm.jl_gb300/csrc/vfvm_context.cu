@@ -231,6 +231,7 @@ extern "C" void vfvm_control_default(vfvm_control* c) {
   c->dp = 1.0; c->dp_min = 1.0e-3; c->dp_max = 1.0; c->dp_grow = 1.0; c->dp_decrease = 0.5;
   c->du_opt = 0.1; c->du_max_factor = 1.2;
   c->num_final_steps = 5; c->force_first_step = 0; c->handle_exceptions = 0; c->store_all = 1;
+  c->engine = VFVM_ENGINE_PERSISTENT; c->team_ctas = 0;
 }
 
 extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph, int* status) {
@@ -489,6 +490,7 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
     std::vector<int> cn(N), fill(c->h_color_ptr.begin(), c->h_color_ptr.end() - 1);
     for (int k = 0; k < N; ++k) cn[fill[color[k]]++] = k;
     SETUP_CUDA(c->color_nodes.upload(cn));
+    SETUP_CUDA(c->color_ptr.upload(c->h_color_ptr));
     // lower slots per node in factorization order (colour, then node index)
     std::vector<int> lptr(N + 1, 0), lslots;
     std::vector<std::pair<int64_t, int>> tmp;

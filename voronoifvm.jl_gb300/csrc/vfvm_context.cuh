@@ -87,6 +87,7 @@ struct vfvm_ctx {
   int ncolors = 0;
   std::vector<int> h_color_ptr;             // ncolors+1
   vfvm::DBuf<int> color_nodes;              // nodes sorted by (colour, index)
+  vfvm::DBuf<int> color_ptr;                // device copy of h_color_ptr
   vfvm::DBuf<int> lower_ptr, lower_slots;   // per node: lower-colour slots in factorization order
 
   // assembly buffers

@@ -1,5 +1,6 @@
-// Device-resident damped Newton (solve_step!, src/vfvm_solver.jl:13-222) with a
-// preconditioned BiCGStab linear solve in place of the reference's sparse direct
+// Graph engine: device-resident damped Newton (solve_step!, src/vfvm_solver.jl:13-222) with a
+// preconditioned BiCGStab linear solve (one kernel per phase; the subdomain ILU0
+// request uses the global multicolour ILU0 here) in place of the reference's sparse direct
 // solve (_solve_linear!, src/vfvm_linsolve.jl:6-61).
 //
 // Everything between two host calls runs on the device: one CUDA graph holds

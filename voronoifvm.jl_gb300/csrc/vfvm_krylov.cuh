@@ -117,8 +117,10 @@ __device__ __forceinline__ void team_spmv_jac(Team& team, const KrylovData<NS, K
 
 // Solves A x = b (x starts at 0).  Returns false if a team barrier expired.
 template <class Team, int NS, int LPR, typename KT>
-__device__ bool team_bicgstab_jacobi(Team& team, const KrylovData<NS, KT>& d, const KrylovCtl& c, KrylovOut* out) {
+__device__ bool team_bicgstab_jacobi(Team& team, const KrylovData<NS, KT>& d, const KrylovCtl& c, KrylovOut* out,
+                                     int* iters_all = nullptr) {
   const int64_t n = (int64_t)d.N * NS;
+  if (iters_all) *iters_all = 0;
   // block-Jacobi setup, x = 0, r = Dinv b, r0 = r
   double acc1[1] = {0.0};
   for (int K = team.rank(); K < d.N; K += team.size()) {
@@ -189,6 +191,7 @@ __device__ bool team_bicgstab_jacobi(Team& team, const KrylovData<NS, KT>& d, co
     rho = red[0];
   }
   if (team.rank() == 0 && out) { out->iters = it; out->res0 = sqrt(red1[0]); out->res = sqrt(rr); out->breakdown = brk; }
+  if (iters_all) *iters_all = it;
   return true;
 }
 

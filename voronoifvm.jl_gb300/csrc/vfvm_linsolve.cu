@@ -37,7 +37,7 @@ template <int LPR>
 __global__ void __launch_bounds__(kLinThreads) linsolve_kernel(KrylovData<1, double> d, KrylovCtl c, GridSync gs,
                                                                KrylovOut* out, const int* err) {
   if (*err) return;  // invalid input: every block leaves before the first barrier
-  GridTeam team{gs, 0u};
+  GridTeam team = grid_team(gs);
   const bool ok = team_bicgstab_jacobi<GridTeam, 1, LPR, double>(team, d, c, out);
   if (!ok && blockIdx.x == 0 && threadIdx.x == 0) out->status = VFVM_ERR_TIMEOUT;
 }

@@ -1,0 +1,41 @@
+// Declarations of the persistent engine and batched solver templates.  Their
+// definitions (vfvm_persist_impl.cuh) are instantiated once per physics in
+// separate objects (vfvm_persist_inst.cu, compiled with -DVFVM_INST_PHYS=...) so
+// the heavy kernels build in parallel.
+#pragma once
+#include <vector>
+#include "vfvm_solver.cuh"
+
+struct vfvm_batch {
+  // systems of one physics, packed unknowns, instance descriptors, scheduling state
+  int ninst = 0, phys = 0, ns = 1;
+  std::vector<vfvm_ctx*> ctx;
+  std::vector<int64_t> offsets;  // dof offsets, ninst+1
+  vfvm::DBuf<double> U, Uold;
+  vfvm::DBuf<char> desc;               // NewtonData array of the current precision
+  int desc_precision = -1;
+  vfvm::DBuf<int> order;
+  vfvm::DBuf<unsigned> bars;
+  vfvm::DBuf<double> partials;
+  vfvm::DBuf<int> slots;
+  vfvm::DBuf<char> syncs;
+  vfvm::DBuf<unsigned> queue;
+  vfvm::DBuf<char> outs;
+  vfvm::DBuf<int> failed;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int tuned_ctas = 0;
+  ~vfvm_batch() {
+    for (auto* c : ctx) vfvm_destroy(c);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace vfvm {
+template <class Ph>
+int persistent_solve_t(vfvm_ctx* c, const vfvm_control* ctl, const PersistRunHost& run, vfvm_history* hist, float* ms);
+template <class Ph>
+int batch_run_t(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, double tstep, double lambda, float* ms);
+}  // namespace vfvm

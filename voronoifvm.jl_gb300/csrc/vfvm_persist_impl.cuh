@@ -1,0 +1,210 @@
+// Host side of the persistent Newton engine (one system per cooperative launch)
+// and of the batched solver (many systems of uneven size in one cooperative
+// launch, a group of CTAs per system, largest systems first).
+#pragma once
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+#include "vfvm_newton_team.cuh"
+#include "vfvm_persist.cuh"
+
+namespace vfvm {
+
+template <class Ph, typename KT>
+NewtonData<Ph, KT> make_newton_data(vfvm_ctx* c, double* U, double* Uold) {
+  Workspace* w = c->ws;
+  KVecs<KT>& k = *reinterpret_cast<KVecs<KT>*>(std::is_same<KT, double>::value ? (void*)&w->k64 : (void*)&w->k32);
+  KT* J = std::is_same<KT, double>::value ? (KT*)c->J.p : (KT*)c->Jf.p;
+  NewtonData<Ph, KT> nd;
+  nd.t = c->tables();
+  nd.U = U;
+  nd.Uold = Uold;
+  nd.F = c->F.p;
+  nd.J = J;
+  nd.bw = k.b.p;
+  nd.dirdof = c->dirichlet_dof.p;
+  nd.kd.N = c->N;
+  nd.kd.rowptr = c->browptr.p;
+  nd.kd.col = c->bcol.p;
+  nd.kd.A = J;
+  nd.kd.diag = c->diag.p;
+  nd.kd.dinv = k.dinv.p;
+  nd.kd.b = k.b.p;
+  nd.kd.x = k.x.p;
+  nd.kd.r = k.r.p; nd.kd.r0 = k.r0.p; nd.kd.p = k.p.p; nd.kd.v = k.v.p; nd.kd.s = k.s.p; nd.kd.t = k.t.p;
+  nd.il.ncolors = c->ncolors;
+  nd.il.color_ptr = c->color_ptr.p;
+  nd.il.color_nodes = c->color_nodes.p;
+  nd.il.node_color = w->node_color.p;
+  nd.il.lower_ptr = c->lower_ptr.p;
+  nd.il.lower_slots = c->lower_slots.p;
+  nd.il.ilu = k.ilu.p;
+  nd.il.y = k.sh.p;
+  nd.nvals = c->nnzb * (int64_t)c->ns * c->ns;
+  return nd;
+}
+
+inline int sm_count() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  return sms;
+}
+
+template <class Ph, typename KT, int PRECON>
+int persistent_launch(vfvm_ctx* c, const vfvm_control* ctl, const PersistRunHost& rh, vfvm_history* hist,
+                             float* ms) {
+  Workspace* w = c->ws;
+  auto kern = newton_persistent_kernel<Ph, KT, PRECON>;
+  int per_sm = 0;
+  VFVM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPersistThreads, 0));
+  const int sms = sm_count();
+  if (per_sm < 1 || sms < 1) return VFVM_ERR_CUDA;
+  int grid = sms * std::min(per_sm, 2);
+  if (ctl->team_ctas > 0) grid = std::min(ctl->team_ctas, sms * per_sm);
+  const int need = (int)((c->N + kPersistThreads - 1) / kPersistThreads);
+  grid = std::max(1, std::min(grid, need));
+  if (w->pbar.n < 8) VFVM_CUDA(w->pbar.alloc(8));
+  if (w->ppartials.n < (size_t)2 * grid * 8) VFVM_CUDA(w->ppartials.alloc((size_t)2 * grid * 8));
+  if (w->pout.n < sizeof(NewtonOut)) VFVM_CUDA(w->pout.alloc(sizeof(NewtonOut)));
+  VFVM_CUDA(cudaMemsetAsync(w->pbar.p, 0, 8 * sizeof(unsigned), c->stream));
+  NewtonData<Ph, KT> nd = make_newton_data<Ph, KT>(c, c->U.p, c->Uold.p);
+  DevControl dc = make_devcontrol(*ctl);
+  GridSync gs{w->pbar.p, w->ppartials.p};
+  PersistRun run{rh.nsteps, rh.time, 1.0 / rh.tstep, rh.lambda, rh.t0, rh.dt};
+  NewtonOut* out = reinterpret_cast<NewtonOut*>(w->pout.p);
+  void* args[] = {&nd, &dc, &gs, &run, &out};
+  VFVM_CUDA(cudaEventRecord(w->ev0, c->stream));
+  VFVM_CUDA(cudaLaunchCooperativeKernel((void*)kern, dim3(grid), dim3(kPersistThreads), args, 0, c->stream));
+  VFVM_CUDA(cudaEventRecord(w->ev1, c->stream));
+  NewtonOut h;
+  VFVM_CUDA(cudaMemcpyAsync(&h, out, sizeof(NewtonOut), cudaMemcpyDeviceToHost, c->stream));
+  VFVM_CUDA(cudaStreamSynchronize(c->stream));
+  float t = 0;
+  VFVM_CUDA(cudaEventElapsedTime(&t, w->ev0, w->ev1));
+  if (ms) *ms = t;
+  if (hist) {
+    std::memset(hist, 0, sizeof(*hist));
+    hist->nnewton = h.nnewton;
+    hist->nlin = h.nlin;
+    hist->nsteps = h.nsteps;
+    hist->status = h.status;
+    hist->updatenorm = h.updnorm;
+    hist->resnorm = h.resnorm;
+    hist->time_ms = t;
+  }
+  // mirror into the device-state block read by the graph-engine helpers
+  w->st_host->status = h.status;
+  w->st_host->nnewton = h.nnewton;
+  w->st_host->nlin = h.nlin;
+  w->st_host->updnorm = h.updnorm;
+  w->st_host->resnorm = h.resnorm;
+  return h.status;
+}
+
+template <class Ph>
+int persistent_solve_t(vfvm_ctx* c, const vfvm_control* ctl, const PersistRunHost& run, vfvm_history* hist, float* ms) {
+  const bool f64 = ctl->precision == VFVM_PRECISION_FP64;
+  switch (ctl->precon) {
+    case VFVM_PRECON_JACOBI:
+      return f64 ? persistent_launch<Ph, double, VFVM_PRECON_JACOBI>(c, ctl, run, hist, ms)
+                 : persistent_launch<Ph, float, VFVM_PRECON_JACOBI>(c, ctl, run, hist, ms);
+    case VFVM_PRECON_ILU0:
+      return f64 ? persistent_launch<Ph, double, VFVM_PRECON_ILU0>(c, ctl, run, hist, ms)
+                 : persistent_launch<Ph, float, VFVM_PRECON_ILU0>(c, ctl, run, hist, ms);
+    default:
+      return f64 ? persistent_launch<Ph, double, VFVM_PRECON_BLOCK_ILU0>(c, ctl, run, hist, ms)
+                 : persistent_launch<Ph, float, VFVM_PRECON_BLOCK_ILU0>(c, ctl, run, hist, ms);
+  }
+}
+
+}  // namespace vfvm
+
+
+namespace vfvm {
+
+template <class Ph, typename KT, int PRECON>
+int batch_launch(vfvm_batch* b, const vfvm_control* ctl, int ctas_per_system, double time, double tstep,
+                 double lambda, float* ms) {
+  auto kern = newton_batch_kernel<Ph, KT, PRECON>;
+  int per_sm = 0;
+  VFVM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPersistThreads, 0));
+  const int sms = sm_count();
+  if (per_sm < 1 || sms < 1) return VFVM_ERR_CUDA;
+  const int G = std::max(1, ctas_per_system);
+  const int total = sms * std::min(per_sm, 4);
+  int ngroups = std::max(1, total / G);
+  ngroups = std::min(ngroups, b->ninst);
+  const int grid = ngroups * G;
+  if (grid > sms * per_sm) return VFVM_ERR_INPUT;
+  // per-group barrier words and partials
+  if (b->bars.n < (size_t)8 * ngroups) VFVM_CUDA(b->bars.alloc((size_t)8 * ngroups));
+  if (b->partials.n < (size_t)2 * G * 8 * ngroups) VFVM_CUDA(b->partials.alloc((size_t)2 * G * 8 * ngroups));
+  if (b->slots.n < (size_t)ngroups) VFVM_CUDA(b->slots.alloc(ngroups));
+  std::vector<BatchSync> hs(ngroups);
+  for (int g = 0; g < ngroups; ++g)
+    hs[g] = BatchSync{GridSync{b->bars.p + 8 * (size_t)g, b->partials.p + (size_t)2 * G * 8 * g}, b->slots.p + g};
+  if (b->syncs.n < sizeof(BatchSync) * ngroups) VFVM_CUDA(b->syncs.alloc(sizeof(BatchSync) * ngroups));
+  VFVM_CUDA(cudaMemcpyAsync(b->syncs.p, hs.data(), sizeof(BatchSync) * ngroups, cudaMemcpyHostToDevice, b->stream));
+  VFVM_CUDA(cudaMemsetAsync(b->bars.p, 0, 8 * sizeof(unsigned) * ngroups, b->stream));
+  VFVM_CUDA(cudaMemsetAsync(b->queue.p, 0, sizeof(unsigned), b->stream));
+  VFVM_CUDA(cudaMemsetAsync(b->failed.p, 0, sizeof(int), b->stream));
+  VFVM_CUDA(cudaMemsetAsync(b->outs.p, 0, sizeof(NewtonOut) * b->ninst, b->stream));
+  const NewtonData<Ph, KT>* insts = reinterpret_cast<const NewtonData<Ph, KT>*>(b->desc.p);
+  const int* order = b->order.p;
+  DevControl dc = make_devcontrol(*ctl);
+  const BatchSync* groups = reinterpret_cast<const BatchSync*>(b->syncs.p);
+  unsigned* queue = b->queue.p;
+  NewtonOut* outs = reinterpret_cast<NewtonOut*>(b->outs.p);
+  int* failed = b->failed.p;
+  int ninst = b->ninst;
+  double tinv = 1.0 / tstep;
+  int gsz = G;
+  void* args[] = {&insts, &ninst, &order, &dc, &groups, &gsz, &queue, &time, &tinv, &lambda, &outs, &failed};
+  VFVM_CUDA(cudaEventRecord(b->e0, b->stream));
+  VFVM_CUDA(cudaLaunchCooperativeKernel((void*)kern, dim3(grid), dim3(kPersistThreads), args, 0, b->stream));
+  VFVM_CUDA(cudaEventRecord(b->e1, b->stream));
+  VFVM_CUDA(cudaStreamSynchronize(b->stream));
+  if (ms) VFVM_CUDA(cudaEventElapsedTime(ms, b->e0, b->e1));
+  int hfailed = 0;
+  VFVM_CUDA(cudaMemcpy(&hfailed, failed, sizeof(int), cudaMemcpyDeviceToHost));
+  return hfailed ? VFVM_ERR_TIMEOUT : VFVM_OK;
+}
+
+template <class Ph, typename KT>
+int batch_prepare(vfvm_batch* b, int precision) {
+  if (b->desc_precision == precision) return VFVM_OK;
+  std::vector<NewtonData<Ph, KT>> d(b->ninst);
+  for (int i = 0; i < b->ninst; ++i) {
+    int rc = ensure_workspace(b->ctx[i], precision);
+    if (rc) return rc;
+    d[i] = make_newton_data<Ph, KT>(b->ctx[i], b->U.p + b->offsets[i], b->Uold.p + b->offsets[i]);
+  }
+  VFVM_CUDA(b->desc.alloc(sizeof(NewtonData<Ph, KT>) * b->ninst));
+  VFVM_CUDA(cudaMemcpy(b->desc.p, d.data(), sizeof(NewtonData<Ph, KT>) * b->ninst, cudaMemcpyHostToDevice));
+  b->desc_precision = precision;
+  return VFVM_OK;
+}
+
+template <class Ph>
+int batch_run_t(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, double tstep, double lambda, float* ms) {
+  const bool f64 = ctl->precision == VFVM_PRECISION_FP64;
+  const bool jac = ctl->precon == VFVM_PRECON_JACOBI;
+  int rc = f64 ? batch_prepare<Ph, double>(b, ctl->precision) : batch_prepare<Ph, float>(b, ctl->precision);
+  if (rc) return rc;
+  (void)jac;
+  switch (ctl->precon) {
+    case VFVM_PRECON_JACOBI:
+      return f64 ? batch_launch<Ph, double, VFVM_PRECON_JACOBI>(b, ctl, ctas, time, tstep, lambda, ms)
+                 : batch_launch<Ph, float, VFVM_PRECON_JACOBI>(b, ctl, ctas, time, tstep, lambda, ms);
+    case VFVM_PRECON_ILU0:
+      return f64 ? batch_launch<Ph, double, VFVM_PRECON_ILU0>(b, ctl, ctas, time, tstep, lambda, ms)
+                 : batch_launch<Ph, float, VFVM_PRECON_ILU0>(b, ctl, ctas, time, tstep, lambda, ms);
+    default:
+      return f64 ? batch_launch<Ph, double, VFVM_PRECON_BLOCK_ILU0>(b, ctl, ctas, time, tstep, lambda, ms)
+                 : batch_launch<Ph, float, VFVM_PRECON_BLOCK_ILU0>(b, ctl, ctas, time, tstep, lambda, ms);
+  }
+}
+
+}  // namespace vfvm

@@ -61,7 +61,18 @@ struct Workspace {
   std::map<GraphKey, cudaGraphExec_t> graphs;
   std::map<GraphKey, cudaGraph_t> graph_defs;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // persistent engine: barrier words, reduction partials, result record
+  DBuf<unsigned> pbar;
+  DBuf<double> ppartials;
+  DBuf<char> pout;
 };
+
+// persistent engine (vfvm_persist.cu): one solve (nsteps == 0) or a fixed-step run
+struct PersistRunHost {
+  int nsteps;
+  double time, tstep, lambda, t0, dt;
+};
+int persistent_solve(vfvm_ctx* c, const vfvm_control* ctl, const PersistRunHost& run, vfvm_history* hist, float* ms);
 
 int ensure_workspace(vfvm_ctx* c, int precision);
 // cached, instantiated Newton graph; kind 0 = solve from Uinit, kind 1 = fixed implicit Euler step

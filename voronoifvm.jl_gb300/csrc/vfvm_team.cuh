@@ -39,8 +39,8 @@ __device__ __forceinline__ void block_allreduce(double (&v)[NV], unsigned maxmas
   __syncthreads();
 }
 
-// Barrier/reduction scratch of a grid team (device memory, zero-initialised):
-//   bar[0] arrival counter, bar[1] generation, bar[2] error flag, bar[3] reduction parity
+// Barrier/reduction scratch of a team (device memory, zero-initialised):
+//   bar[0] arrival counter, bar[1] generation, bar[2] error flag
 //   partials: 2 * nblocks * 8 doubles (double-buffered)
 struct GridSync {
   unsigned* bar;
@@ -49,15 +49,17 @@ struct GridSync {
 
 constexpr long long kBarrierSpinLimit = 1ll << 24;  // ~0.5-1 s of polling, then VFVM_ERR_TIMEOUT
 
-struct GridTeam {
+// A team of `nblk` co-resident CTAs (a whole cooperative grid, or a group of
+// CTAs inside one); `bid` is this CTA's index in the team.
+struct GroupTeam {
   GridSync gs;
+  int nblk, bid;
   unsigned parity;  // alternates the partials buffer between consecutive reductions
-  __device__ __forceinline__ int rank() const { return blockIdx.x * blockDim.x + threadIdx.x; }
-  __device__ __forceinline__ int size() const { return gridDim.x * blockDim.x; }
-  __device__ __forceinline__ int nblocks() const { return gridDim.x; }
+  __device__ __forceinline__ int rank() const { return bid * blockDim.x + threadIdx.x; }
+  __device__ __forceinline__ int size() const { return nblk * blockDim.x; }
 
-  // Bounded sense-free generation barrier.  Returns false (on every thread of
-  // every block that observes it) once any block's wait expired.
+  // Bounded generation barrier over the team's CTAs.  Returns false (on every
+  // thread of every CTA that observes it) once any CTA's wait expired.
   __device__ __forceinline__ bool sync() {
     __shared__ int ok_sh;
     __syncthreads();
@@ -67,7 +69,7 @@ struct GridTeam {
       __threadfence();
       const unsigned arrived = atomicAdd(&gs.bar[0], 1u);
       int ok = 1;
-      if (arrived == gridDim.x - 1) {
+      if (arrived == (unsigned)nblk - 1u) {
         gs.bar[0] = 0u;
         __threadfence();
         atomicAdd(&gs.bar[1], 1u);
@@ -75,7 +77,7 @@ struct GridTeam {
         long long spins = 0;
         while (vbar[1] == gen) {
           if (vbar[2] != 0u || ++spins > kBarrierSpinLimit) { ok = 0; break; }
-          __nanosleep(64);
+          if (spins > 64) __nanosleep(32);
         }
         if (!ok) atomicExch(&gs.bar[2], 1u);
       }
@@ -90,22 +92,30 @@ struct GridTeam {
   __device__ __forceinline__ bool reduce(double (&v)[NV], unsigned maxmask, double (&out)[NV]) {
     __shared__ double sh[NV][kTeamMaxWarps];
     block_allreduce<NV>(v, maxmask, sh);
-    double* buf = gs.partials + (size_t)parity * gridDim.x * 8;
+    double* buf = gs.partials + (size_t)parity * nblk * 8;
     parity ^= 1u;
     if (threadIdx.x == 0) {
 #pragma unroll
-      for (int k = 0; k < NV; ++k) buf[blockIdx.x * 8 + k] = v[k];
+      for (int k = 0; k < NV; ++k) buf[bid * 8 + k] = v[k];
     }
     if (!sync()) return false;
-    // every block sums the partials in block order (deterministic, identical on all blocks)
+    // every CTA sums the partials in CTA order (deterministic, identical everywhere);
+    // L2 loads (ld.global.cg) see the other CTAs' fenced writes and can all be in flight
     __shared__ double tot[NV];
     if (threadIdx.x < 32) {
 #pragma unroll
       for (int k = 0; k < NV; ++k) {
         double a = 0.0;
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) {
-          const double pv = *((volatile double*)&buf[b * 8 + k]);
-          a = ((maxmask >> k) & 1) ? fmax(a, pv) : a + pv;
+        constexpr int kChunk = 8;
+        for (int b0 = threadIdx.x; b0 < nblk; b0 += 32 * kChunk) {
+          double pv[kChunk];
+#pragma unroll
+          for (int j = 0; j < kChunk; ++j) {
+            const int b = b0 + 32 * j;
+            pv[j] = b < nblk ? __ldcg(&buf[b * 8 + k]) : 0.0;
+          }
+#pragma unroll
+          for (int j = 0; j < kChunk; ++j) a = ((maxmask >> k) & 1) ? fmax(a, pv[j]) : a + pv[j];
         }
         for (int o = 16; o > 0; o >>= 1) {
           const double bb = __shfl_down_sync(0xffffffffu, a, o);
@@ -121,6 +131,10 @@ struct GridTeam {
     return true;
   }
 };
+
+// The whole cooperative grid as one team.
+__device__ __forceinline__ GroupTeam grid_team(const GridSync& gs) { return GroupTeam{gs, (int)gridDim.x, (int)blockIdx.x, 0u}; }
+using GridTeam = GroupTeam;
 
 struct CtaTeam {
   __device__ __forceinline__ int rank() const { return threadIdx.x; }

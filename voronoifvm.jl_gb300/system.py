@@ -132,6 +132,10 @@ class SolverControl:
     handle_exceptions: bool = False
     store_all: bool = True
     log: bool = False
+    # device loop driver: "persistent" (one cooperative launch per solve) or "graph"
+    engine: str = "persistent"
+    # batched solves: CTAs per system (0: library default)
+    team_ctas: int = 0
 
     def to_c(self, is_linear: bool = False) -> L.Control_t:
         c = L.Control_t()
@@ -153,6 +157,8 @@ class SolverControl:
         c.force_first_step = int(bool(self.force_first_step))
         c.handle_exceptions = int(bool(self.handle_exceptions))
         c.store_all = int(bool(self.store_all))
+        c.engine = L.ENGINE[self.engine]
+        c.team_ctas = int(self.team_ctas)
         return c
 
 
