@@ -123,6 +123,7 @@ typedef struct vfvm_control {
 
 #define VFVM_ENGINE_GRAPH 0      /* CUDA graph of kernels with conditional WHILE nodes */
 #define VFVM_ENGINE_PERSISTENT 1 /* one persistent cooperative launch per solve (or per fixed-step run) */
+#define VFVM_ENGINE_AUTO 2       /* persistent for small systems (<= 16384 unknowns), graph otherwise */
 
 /* NewtonSolverHistory (src/vfvm_history.jl:10-37), accumulated over a call. */
 typedef struct vfvm_history {
@@ -158,6 +159,9 @@ int vfvm_geometry(vfvm_ctx* ctx, double* nodevolumes, double* edgefactors, int32
 
 /* Replace the physics parameter block (the `data` of the reference). */
 int vfvm_set_params(vfvm_ctx* ctx, const double* params, int32_t nparams);
+
+/* Replace the per-node physics data (nnodes x nnodedata values, node-major). */
+int vfvm_set_nodedata(vfvm_ctx* ctx, const double* nodedata, int32_t nnodedata);
 
 /* _initialize_dirichlet!: overwrite Dirichlet values in U (host array, n values). */
 int vfvm_init_dirichlet(vfvm_ctx* ctx, double* U, double time, double lambda);
@@ -204,12 +208,29 @@ typedef struct vfvm_batch vfvm_batch;
 vfvm_batch* vfvm_batch_create(int32_t ninst, const vfvm_grid* grids, const vfvm_physics_desc* phys, int* status);
 void vfvm_batch_destroy(vfvm_batch* batch);
 int vfvm_batch_offsets(vfvm_batch* batch, int64_t* offsets);
+/* Replace system `inst`'s parameters and/or node data (NULL keeps them).  When
+ * every grid passed to vfvm_batch_create used the same arrays, the systems share
+ * one set of device grid tables. */
+int vfvm_batch_set_instance(vfvm_batch* batch, int32_t inst, const double* params, int32_t nparams,
+                            const double* nodedata, int32_t nnodedata);
 /* One stationary solve (tstep = INFINITY) or implicit Euler step of every
  * system from inival; hist (optional) receives one record per system. */
 int vfvm_batch_solve(vfvm_batch* batch, const vfvm_control* control, const double* inival, double* U, double time,
                      double tstep, double lambda, vfvm_history* hist);
 int vfvm_batch_solve_device(vfvm_batch* batch, const vfvm_control* control, const double* inival_dev, double* U_dev,
                             double time, double tstep, double lambda, vfvm_history* hist);
+/* Guarded start for a proposed initial value (e.g. a learned prediction):
+ * every system runs Newton from guess_dev for as long as each iteration reduces
+ * the FP64 residual max-norm; where an iteration does not (or Newton fails
+ * otherwise: NaN, no convergence) it restarts with plain Newton from
+ * inival_dev.  Convergence is judged by the same FP64 residual test as
+ * vfvm_batch_solve_device.  There is no counterpart in the reference, whose
+ * solve() (src/vfvm_solver.jl:551-668) always starts from inival.
+ * from_guess (optional, one per system) = 1 where the result came from the
+ * guess; the Newton and Krylov counts in hist include abandoned iterations. */
+int vfvm_batch_solve_guarded_device(vfvm_batch* batch, const vfvm_control* control, const double* guess_dev,
+                                    const double* inival_dev, double* U_dev, double time, double tstep,
+                                    double lambda, vfvm_history* hist, int32_t* from_guess);
 /* Autotuner: times the batch from inival_dev (device) for each candidate number
  * of CTAs per system, keeps the fastest for later solves of this batch and
  * reports it in *best_ctas; times_ms[k] = -1 for candidates that do not fit. */
@@ -245,6 +266,38 @@ int vfvm_linsolve_csr(int32_t n, int64_t nnz, const int32_t* rowptr, const int32
 int vfvm_linsolve_csr_noalloc(int32_t n, int64_t nnz, const int32_t* rowptr, const int32_t* colind,
                               const double* vals, const double* b, double* x, double reltol, double abstol,
                               int32_t maxiters, int32_t* iters, double* resnorm);
+
+/* ---- learned initial iterate: a small multilayer perceptron ----
+ * There is no counterpart in the reference: the network predicts a coarse
+ * initial iterate for solve() (src/vfvm_solver.jl:551-668, argument inival),
+ * and every solve started from it is still judged by the FP64 residual of the
+ * Newton loop (src/vfvm_solver.jl:43-198).
+ * Layers: sizes[0] inputs -> sizes[1] -> ... -> sizes[nlayers] outputs, ReLU on
+ * hidden layers, linear output.  Operands BF16, accumulation FP32 (tensor-core
+ * MMA), FP32 master weights, Adam (beta1 0.9, beta2 0.999, eps 1e-8), loss =
+ * mean squared error.  X, T, Y are device pointers to row-major FP32 arrays of
+ * batch rows; batch <= max_batch.  Calls are serial per network. */
+typedef struct vfvm_mlp vfvm_mlp;
+vfvm_mlp* vfvm_mlp_create(int32_t nlayers, const int32_t* sizes, int32_t max_batch, uint64_t seed, int* status);
+void vfvm_mlp_destroy(vfvm_mlp* net);
+/* number of parameters: sum over layers of sizes[l]*sizes[l+1] + sizes[l+1] */
+int vfvm_mlp_nparams(vfvm_mlp* net, int64_t* n);
+/* host copy of the parameters in the order W0 (sizes[0] x sizes[1], row-major),
+ * b0, W1, b1, ...: out != NULL reads them, in != NULL replaces them */
+int vfvm_mlp_params(vfvm_mlp* net, float* out, const float* in);
+/* Y = net(X) */
+int vfvm_mlp_forward(vfvm_mlp* net, int32_t batch, const float* X, float* Y);
+/* gradients of the loss against T (host array in vfvm_mlp_params order) and the loss */
+int vfvm_mlp_gradients(vfvm_mlp* net, int32_t batch, const float* X, const float* T, float* grads, float* loss);
+/* one Adam step with learning rate lr; loss (optional) before the step */
+int vfvm_mlp_train_step(vfvm_mlp* net, int32_t batch, const float* X, const float* T, float lr, float* loss);
+/* fine = scale * (bilinear prolongation of coarse) + shift for batch coarse
+ * fields (nc x nc nodes, x fastest, FP32) onto nested fine grids
+ * ((nc-1)*ratio+1 nodes per side, FP64, the node order of simplexgrid);
+ * instance b reads coarse + b*coarse_stride and writes fine + b*fine_stride
+ * (device pointers), enqueued on stream (NULL: the legacy default stream). */
+int vfvm_prolong_bilinear(int32_t batch, int32_t nc, int32_t ratio, const float* coarse, int64_t coarse_stride,
+                          double scale, double shift, double* fine, int64_t fine_stride, void* stream);
 
 #ifdef __cplusplus
 }

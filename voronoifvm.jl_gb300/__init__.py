@@ -11,6 +11,7 @@ from .system import (AssemblyError, ConvergenceError, EmbeddingError, LinearSolv
                      unknowns)
 from . import _lib
 from .batch import BatchSolver
+from . import learned
 from .build import build_library
 
 __all__ = ["Grid", "simplexgrid", "Physics", "System", "SolverControl", "NewtonSolverHistory", "TransientSolution",

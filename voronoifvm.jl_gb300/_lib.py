@@ -27,7 +27,7 @@ PHYSICS_NSPEC = {1: 1, 2: 1, 3: 2, 4: 2, 5: 1, 6: 1, 7: 1, 8: 1, 11: 1, 12: 1, 1
 KRYLOV = {"bicgstab": 0, "gmres": 1}
 PRECON = {"jacobi": 0, "ilu0": 1, "block_ilu0": 2}
 PRECISION = {"fp64": 0, "mixed": 1}
-ENGINE = {"graph": 0, "persistent": 1}
+ENGINE = {"graph": 0, "persistent": 1, "auto": 2}
 
 
 class Grid_t(ctypes.Structure):
@@ -84,11 +84,23 @@ SIGNATURES = {
     "vfvm_batch_create": (c_vp, [c_i32, P(Grid_t), P(Physics_t), P(ctypes.c_int)]),
     "vfvm_batch_destroy": (None, [c_vp]),
     "vfvm_batch_offsets": (ctypes.c_int, [c_vp, P(c_i64)]),
+    "vfvm_batch_set_instance": (ctypes.c_int, [c_vp, c_i32, P(c_d), c_i32, P(c_d), c_i32]),
+    "vfvm_set_nodedata": (ctypes.c_int, [c_vp, P(c_d), c_i32]),
     "vfvm_batch_solve": (ctypes.c_int, [c_vp, P(Control_t), P(c_d), P(c_d), c_d, c_d, c_d, P(History_t)]),
     "vfvm_batch_solve_device": (ctypes.c_int, [c_vp, P(Control_t), c_vp, c_vp, c_d, c_d, c_d, P(History_t)]),
+    "vfvm_batch_solve_guarded_device": (ctypes.c_int, [c_vp, P(Control_t), c_vp, c_vp, c_vp, c_d, c_d, c_d,
+                                                       P(History_t), P(c_i32)]),
     "vfvm_batch_tune": (ctypes.c_int, [c_vp, P(Control_t), c_vp, P(c_i32), P(ctypes.c_float), c_i32, P(c_i32)]),
     "vfvm_linsolve_csr_noalloc": (ctypes.c_int, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_d, c_d, c_i32,
                                                  P(c_i32), P(c_d)]),
+    "vfvm_mlp_create": (c_vp, [c_i32, P(c_i32), c_i32, ctypes.c_uint64, P(ctypes.c_int)]),
+    "vfvm_mlp_destroy": (None, [c_vp]),
+    "vfvm_mlp_nparams": (ctypes.c_int, [c_vp, P(c_i64)]),
+    "vfvm_mlp_params": (ctypes.c_int, [c_vp, P(ctypes.c_float), P(ctypes.c_float)]),
+    "vfvm_mlp_forward": (ctypes.c_int, [c_vp, c_i32, c_vp, c_vp]),
+    "vfvm_mlp_gradients": (ctypes.c_int, [c_vp, c_i32, c_vp, c_vp, P(ctypes.c_float), P(ctypes.c_float)]),
+    "vfvm_mlp_train_step": (ctypes.c_int, [c_vp, c_i32, c_vp, c_vp, ctypes.c_float, P(ctypes.c_float)]),
+    "vfvm_prolong_bilinear": (ctypes.c_int, [c_i32, c_i32, c_i32, c_vp, c_i64, c_d, c_d, c_vp, c_i64, c_vp]),
 }
 
 _lib = None

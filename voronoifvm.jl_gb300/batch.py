@@ -28,7 +28,13 @@ class BatchSolver:
             raise ValueError(f"a batch holds one physics kind, got {sorted(kinds)}")
         lib = L.load()
         self.systems = list(systems)
-        marshalled = [s._marshal() for s in self.systems]
+        # systems built on one Grid object pass the same grid arrays, so the
+        # library keeps a single copy of the grid tables for them
+        marshalled, first = [], {}
+        for s in self.systems:
+            gt, pt, keep = s._marshal()
+            gt = first.setdefault(id(s.grid), gt)
+            marshalled.append((gt, pt, keep))
         self._keep = [m[2] for m in marshalled]
         n = len(self.systems)
         grids = (L.Grid_t * n)(*[m[0] for m in marshalled])
@@ -58,6 +64,21 @@ class BatchSolver:
 
     def unpack(self, U: np.ndarray):
         return [_shape(U[self.offsets[i]:self.offsets[i + 1]].copy(), s) for i, s in enumerate(self.systems)]
+
+    def set_instance(self, i: int, data=None, nodedata=None):
+        """Replace the parameters and/or node data of instance i (same sizes)."""
+        s = self.systems[i]
+        if data is not None:
+            s.physics.data = list(np.atleast_1d(np.asarray(data, dtype=np.float64)))
+        p = np.ascontiguousarray(s.physics.data, dtype=np.float64)
+        nd, ndp = 0, None
+        if nodedata is not None:
+            a = np.asarray(nodedata, dtype=np.float64)
+            a = a.reshape(-1, s.grid.nnodes) if a.ndim == 1 else a
+            s.physics.nodedata = a
+            nda = np.ascontiguousarray(a.T)
+            nd, ndp = a.shape[0], L.ptr(nda)
+        _raise(L.load().vfvm_batch_set_instance(self.h, i, L.ptr(p), p.size, ndp, nd), "vfvm_batch_set_instance")
 
     def _control(self, control):
         c = (control or SolverControl()).to_c(False)

@@ -11,6 +11,10 @@ using namespace vfvm;
 
 namespace {
 
+// Below this many unknowns a solve is launch-latency bound: the one-launch
+// persistent engine wins; above it the per-phase graph kernels (full occupancy) win.
+constexpr int64_t kAutoPersistentDofs = 16384;
+
 // Write {time, 1/tstep, lambda} (and abort = 0) into the device state.
 int set_time(vfvm_ctx* c, double time, double tstep, double lambda) {
   Workspace* w = c->ws;
@@ -43,7 +47,9 @@ int check_control(const vfvm_control* ctl) {
 // Runs the Newton graph once from ws->Uinit (already on the device) at the time
 // values set in the state; leaves the result in c->U and the state in st_host.
 bool use_persistent(const vfvm_ctx* c, const vfvm_control* ctl) {
-  return ctl->engine == VFVM_ENGINE_PERSISTENT && !c->multireg;
+  if (c->multireg) return false;
+  if (ctl->engine == VFVM_ENGINE_AUTO) return (int64_t)c->N * c->ns <= kAutoPersistentDofs;
+  return ctl->engine == VFVM_ENGINE_PERSISTENT;
 }
 
 int run_newton(vfvm_ctx* c, const vfvm_control* ctl, float* ms) {

@@ -11,11 +11,13 @@ template <class T>
 struct DBuf {
   T* p = nullptr;
   size_t n = 0;
+  bool own = true;  // false: a view of another context's buffer (shared grid tables)
   DBuf() = default;
   DBuf(const DBuf&) = delete;
   DBuf& operator=(const DBuf&) = delete;
   ~DBuf() { release(); }
-  void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+  void release() { if (p && own) cudaFree(p); p = nullptr; n = 0; own = true; }
+  void view(const DBuf& o) { release(); p = o.p; n = o.n; own = false; }
   cudaError_t alloc(size_t count) {
     release();
     n = count;
@@ -110,4 +112,10 @@ int launch_pattern_gather(vfvm_ctx* c, const double* J, double* out, cudaStream_
 int probe_masks(int phys, const double* params, int nparams, int dim, std::vector<uint8_t>& node_mask,
                 std::vector<uint8_t>& edge_mask, std::vector<uint8_t>& bnode_mask);
 void destroy_workspace(Workspace* w);
+// A context on the same grid as `base` with other physics data: grid tables are
+// shared views of base's device buffers (base must outlive the clone); unknowns,
+// Jacobian, parameters, node data and legacy boundary data are its own.
+vfvm_ctx* clone_context(const vfvm_ctx* base, const vfvm_physics_desc* ph, int* status);
+// replace the per-node physics data (nnodes x nnodedata values, host)
+int set_nodedata(vfvm_ctx* c, const double* data, int nnd);
 }  // namespace vfvm

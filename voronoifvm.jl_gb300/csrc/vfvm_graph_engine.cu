@@ -146,6 +146,7 @@ __global__ void nt_init_kernel(const double* __restrict__ U, int64_t n, DevState
     st->norm = 0.0;
     st->resnorm = 0.0;
     st->updnorm = 0.0;
+    st->early = 0;
     const int go = (ctl->maxiters >= 1 && !st->abort) ? 1 : 0;
     st->finished = go ? 0 : 1;
     if (!go && !st->abort) st->status = VFVM_ERR_CONVERGENCE;
@@ -173,6 +174,8 @@ __global__ void kr_prep_kernel(const double* __restrict__ F, const uint8_t* __re
     st->resnorm = out[1];
     if (!ctl->updatecontrol) st->norm = out[1];
     if (*errflag || isnan(out[0])) st->status = VFVM_ERR_ASSEMBLY;  // NaN assembled: AssemblyError
+    // residual control: the iterate already meets the tolerance, no linear solve
+    else if (!ctl->updatecontrol && !ctl->is_linear && (out[1] < ctl->abstol || out[1] < st->tolx)) st->early = 1;
   }
 }
 
@@ -200,7 +203,7 @@ __global__ void kr_start_kernel(int64_t n, const KT* __restrict__ r, KT* __restr
     st->tol2 = tol * tol;
     st->rr = out[0];
     int go = (out[0] > st->tol2 && ctl->maxiters_linear > 0) ? 1 : 0;
-    if (st->status != VFVM_OK || isnan(out[0])) go = 0;
+    if (st->status != VFVM_OK || st->early || isnan(out[0])) go = 0;
     cudaGraphSetConditional(kcond, go);
   }
 }
@@ -535,7 +538,8 @@ template <typename KT>
 __global__ void nt_update_kernel(int64_t n, double* __restrict__ U, const KT* __restrict__ x, DevState* st,
                                  const DevControl* ctl, double* partials, cudaGraphConditionalHandle ncond) {
   const double damp = st->damp;
-  const bool skip = st->status != VFVM_OK;
+  const bool early = st->early != 0;
+  const bool skip = st->status != VFVM_OK || early;
   double acc[2] = {0.0, 0.0};
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double dx = double(x[i]);
@@ -546,10 +550,12 @@ __global__ void nt_update_kernel(int64_t n, double* __restrict__ U, const KT* __
   }
   double out[2];
   if (grid_reduce<2>(acc, 1u, partials, &st->ticket[5], out) && threadIdx.x == 0) {
-    st->nnewton += 1;
-    st->tot_newton += 1;
-    st->updnorm = out[0];
     int go = 1;
+    if (!skip) {
+      st->nnewton += 1;
+      st->tot_newton += 1;
+      st->updnorm = out[0];
+    }
     if (skip) {
       go = 0;
     } else if (ctl->is_linear) {

@@ -17,6 +17,7 @@ constexpr int kPersistLPR = 8;
 struct NewtonOut {
   int status, nnewton, nlin, nsteps;
   double updnorm, resnorm;
+  int from_guess, pad_;  // guarded batch solves: 1 if the result was reached from the guess
 };
 
 template <class Ph, typename KT>
@@ -35,9 +36,11 @@ struct NewtonData {
 
 // One Newton solve at (time, 1/tstep, lambda) from the values in nd.U (old
 // time-step values in nd.Uold).  Returns false if a team barrier expired.
+// guard: give up (VFVM_ERR_CONVERGENCE) as soon as an iteration fails to reduce
+// the FP64 residual max-norm below that of the iteration before.
 template <class Team, class Ph, typename KT, int PRECON>
 __device__ bool team_newton(Team& team, const NewtonData<Ph, KT>& nd, const DevControl& ctl, double time,
-                            double tstepinv, double lambda, NewtonOut& res) {
+                            double tstepinv, double lambda, NewtonOut& res, bool guard = false) {
   constexpr int NS = Ph::NS;
   const int N = nd.t.N;
   const int64_t n = (int64_t)N * NS;
@@ -54,7 +57,7 @@ __device__ bool team_newton(Team& team, const NewtonData<Ph, KT>& nd, const DevC
   if (!team.template reduce<1>(a1, 0u, r1)) return false;
   double rnorm = r1[0];
   double damp = ctl.is_linear ? 1.0 : ctl.damp_initial;
-  double oldnorm = 1.0, tolx = 0.0, norm = 0.0;
+  double oldnorm = 1.0, tolx = 0.0, norm = 0.0, prev_resnorm = INFINITY;
   int nround = 0, niter = 1;
   if (ctl.maxiters < 1) { res.status = VFVM_ERR_CONVERGENCE; return true; }
   const KrylovCtl kctl{ctl.reltol_linear, ctl.abstol_linear, ctl.maxiters_linear};
@@ -75,6 +78,12 @@ __device__ bool team_newton(Team& team, const NewtonData<Ph, KT>& nd, const DevC
     res.resnorm = r3[1];
     if (r3[2] != 0.0 || isnan(r3[0])) { res.status = VFVM_ERR_ASSEMBLY; return true; }
     const double resnorm = r3[1];
+    // residual control: the iterate already meets the tolerance, no linear solve
+    if (!ctl.updatecontrol && !ctl.is_linear && (resnorm < ctl.abstol || resnorm < tolx)) break;
+    if (guard) {
+      if (res.nnewton > 0 && !(resnorm < prev_resnorm)) { res.status = VFVM_ERR_CONVERGENCE; return true; }
+      prev_resnorm = resnorm;
+    }
     // linear solve J x = F
     int kit = 0;
     bool ok;
@@ -112,6 +121,12 @@ __device__ bool team_newton(Team& team, const NewtonData<Ph, KT>& nd, const DevC
     if (niter > ctl.maxiters) { res.status = VFVM_ERR_CONVERGENCE; break; }
   }
   return true;
+}
+
+template <class Team>
+__device__ __forceinline__ bool team_copy(Team& team, double* dst, const double* src, int64_t n) {
+  for (int64_t q = team.rank(); q < n; q += team.size()) dst[q] = src[q];
+  return team.sync();
 }
 
 // Fixed run of one system: nsteps == 0 -> one solve at (time, tstepinv, lambda);
@@ -167,7 +182,8 @@ __global__ void __launch_bounds__(kPersistThreads) newton_batch_kernel(const New
                                                                        DevControl ctl, const BatchSync* __restrict__ groups,
                                                                        int gsize, unsigned* queue, double time,
                                                                        double tstepinv, double lambda, NewtonOut* outs,
-                                                                       int* failed) {
+                                                                       int* failed, const double* guess,
+                                                                       const double* fallback, const double* ubase) {
   const int group = blockIdx.x / gsize;
   const BatchSync bs = groups[group];
   GroupTeam team{bs.gs, gsize, (int)(blockIdx.x % gsize), 0u};
@@ -182,8 +198,30 @@ __global__ void __launch_bounds__(kPersistThreads) newton_batch_kernel(const New
     if (!team.sync()) { if (threadIdx.x == 0) atomicExch(failed, 1); return; }
     if (pos >= ninst) return;
     const int inst = order[pos];
+    const NewtonData<Ph, KT>& nd = insts[inst];
     NewtonOut res;
-    const bool ok = team_newton<GroupTeam, Ph, KT, PRECON>(team, insts[inst], ctl, time, tstepinv, lambda, res);
+    bool ok = true;
+    int from_guess = 0;
+    if (guess) {
+      // guarded start: Newton from the guess while every iteration reduces the
+      // FP64 residual; if it does not (or fails otherwise), plain Newton from
+      // the fallback (the caller's inival)
+      const int64_t off = nd.U - ubase, n = (int64_t)nd.t.N * Ph::NS;
+      ok = team_copy(team, nd.U, guess + off, n) &&
+           team_newton<GroupTeam, Ph, KT, PRECON>(team, nd, ctl, time, tstepinv, lambda, res, true);
+      from_guess = 1;
+      if (ok && res.status != VFVM_OK) {
+        const int nn = res.nnewton, nl = res.nlin;
+        from_guess = 0;
+        ok = team_copy(team, nd.U, fallback + off, n) &&
+             team_newton<GroupTeam, Ph, KT, PRECON>(team, nd, ctl, time, tstepinv, lambda, res);
+        res.nnewton += nn;
+        res.nlin += nl;
+      }
+    } else {
+      ok = team_newton<GroupTeam, Ph, KT, PRECON>(team, nd, ctl, time, tstepinv, lambda, res);
+    }
+    res.from_guess = from_guess;
     if (!ok) { if (threadIdx.x == 0) atomicExch(failed, 1); return; }
     if (team.bid == 0 && threadIdx.x == 0) outs[inst] = res;
   }

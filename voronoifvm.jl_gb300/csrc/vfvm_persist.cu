@@ -36,9 +36,16 @@ extern "C" vfvm_batch* vfvm_batch_create(int32_t ninst, const vfvm_grid* grids, 
   b->ninst = ninst;
   b->phys = phys[0].physics_id;
   b->offsets.assign(ninst + 1, 0);
+  // systems that all use the same grid arrays share one set of device tables
+  bool shared = true;
+  for (int i = 1; i < ninst && shared; ++i)
+    shared = grids[i].dim == grids[0].dim && grids[i].nnodes == grids[0].nnodes && grids[i].ncells == grids[0].ncells &&
+             grids[i].nbfaces == grids[0].nbfaces && grids[i].coord == grids[0].coord &&
+             grids[i].cellnodes == grids[0].cellnodes && grids[i].cellregions == grids[0].cellregions &&
+             grids[i].bfacenodes == grids[0].bfacenodes && grids[i].bfaceregions == grids[0].bfaceregions;
   for (int i = 0; i < ninst; ++i) {
     int st = 0;
-    vfvm_ctx* c = vfvm_create(&grids[i], &phys[i], &st);
+    vfvm_ctx* c = (shared && i > 0) ? clone_context(b->ctx[0], &phys[i], &st) : vfvm_create(&grids[i], &phys[i], &st);
     if (!c || c->multireg) {
       if (c) vfvm_destroy(c);
       *status = c ? VFVM_ERR_INPUT : st;
@@ -71,6 +78,17 @@ extern "C" void vfvm_batch_destroy(vfvm_batch* b) {
   delete b;
 }
 
+extern "C" int vfvm_batch_set_instance(vfvm_batch* b, int32_t inst, const double* params, int32_t nparams,
+                                       const double* nodedata, int32_t nnodedata) {
+  if (!b || inst < 0 || inst >= b->ninst) return VFVM_ERR_INPUT;
+  vfvm_ctx* c = b->ctx[inst];
+  int rc = VFVM_OK;
+  if (params && (rc = vfvm_set_params(c, params, nparams))) return rc;
+  if (nodedata && (rc = set_nodedata(c, nodedata, nnodedata))) return rc;
+  b->desc_precision = -1;  // descriptors are rebuilt before the next solve
+  return VFVM_OK;
+}
+
 extern "C" int vfvm_batch_offsets(vfvm_batch* b, int64_t* offsets) {
   if (!b || !offsets) return VFVM_ERR_INPUT;
   std::copy(b->offsets.begin(), b->offsets.end(), offsets);
@@ -79,11 +97,20 @@ extern "C" int vfvm_batch_offsets(vfvm_batch* b, int64_t* offsets) {
 
 namespace {
 
-int batch_run(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, double tstep, double lambda, float* ms) {
+int batch_run(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, double tstep, double lambda, float* ms,
+              const double* guess = nullptr, const double* fallback = nullptr) {
   if (ctl->precon == VFVM_PRECON_BLOCK_ILU0)
     for (auto* c : b->ctx)
       if (c->ncolors > kMaxBlockIluColors) return VFVM_ERR_INPUT;
-  return dispatch_physics(b->phys, [&](auto ph) { return batch_run_t<decltype(ph)>(b, ctl, ctas, time, tstep, lambda, ms); });
+  return dispatch_physics(b->phys, [&](auto ph) { return batch_run_t<decltype(ph)>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms);
+  });
+}
+
+// Device inputs written on the legacy default stream before the call (the
+// default stream of most frameworks) are complete before the batch reads them.
+cudaError_t wait_legacy_stream(vfvm_batch* b) {
+  cudaError_t e = cudaEventRecord(b->e0, cudaStreamLegacy);
+  return e == cudaSuccess ? cudaStreamWaitEvent(b->stream, b->e0, 0) : e;
 }
 
 int batch_ctas(vfvm_batch* b, const vfvm_control* ctl) {
@@ -92,11 +119,12 @@ int batch_ctas(vfvm_batch* b, const vfvm_control* ctl) {
   return 2;
 }
 
-int batch_results(vfvm_batch* b, vfvm_history* hist, float ms) {
+int batch_results(vfvm_batch* b, vfvm_history* hist, float ms, int32_t* from_guess = nullptr) {
   std::vector<NewtonOut> outs(b->ninst);
   VFVM_CUDA(cudaMemcpy(outs.data(), b->outs.p, sizeof(NewtonOut) * b->ninst, cudaMemcpyDeviceToHost));
   int worst = VFVM_OK;
   for (int i = 0; i < b->ninst; ++i) {
+    if (from_guess) from_guess[i] = outs[i].from_guess;
     if (outs[i].status != VFVM_OK && worst == VFVM_OK) worst = outs[i].status;
     if (hist) {
       std::memset(&hist[i], 0, sizeof(vfvm_history));
@@ -117,6 +145,7 @@ extern "C" int vfvm_batch_solve_device(vfvm_batch* b, const vfvm_control* ctl, c
                                        double* U_dev, double time, double tstep, double lambda, vfvm_history* hist) {
   if (!b || !ctl || !inival_dev || !U_dev) return VFVM_ERR_INPUT;
   const size_t n = (size_t)b->offsets[b->ninst];
+  VFVM_CUDA(wait_legacy_stream(b));
   VFVM_CUDA(cudaMemcpyAsync(b->U.p, inival_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
   VFVM_CUDA(cudaMemcpyAsync(b->Uold.p, inival_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
   float ms = 0;
@@ -125,6 +154,25 @@ extern "C" int vfvm_batch_solve_device(vfvm_batch* b, const vfvm_control* ctl, c
   VFVM_CUDA(cudaMemcpyAsync(U_dev, b->U.p, n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
   VFVM_CUDA(cudaStreamSynchronize(b->stream));
   return batch_results(b, hist, ms);
+}
+
+// Guarded start: Newton from guess_dev while every iteration reduces the FP64
+// residual, else plain Newton from inival_dev; from_guess[i] (optional) = 1
+// where the result was reached from the guess.
+extern "C" int vfvm_batch_solve_guarded_device(vfvm_batch* b, const vfvm_control* ctl, const double* guess_dev,
+                                               const double* inival_dev, double* U_dev, double time, double tstep,
+                                               double lambda, vfvm_history* hist, int32_t* from_guess) {
+  if (!b || !ctl || !guess_dev || !inival_dev || !U_dev) return VFVM_ERR_INPUT;
+  const size_t n = (size_t)b->offsets[b->ninst];
+  VFVM_CUDA(wait_legacy_stream(b));
+  VFVM_CUDA(cudaMemcpyAsync(b->U.p, inival_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+  VFVM_CUDA(cudaMemcpyAsync(b->Uold.p, inival_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+  float ms = 0;
+  int rc = batch_run(b, ctl, batch_ctas(b, ctl), time, tstep, lambda, &ms, guess_dev, inival_dev);
+  if (rc) return rc;
+  VFVM_CUDA(cudaMemcpyAsync(U_dev, b->U.p, n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+  VFVM_CUDA(cudaStreamSynchronize(b->stream));
+  return batch_results(b, hist, ms, from_guess);
 }
 
 extern "C" int vfvm_batch_solve(vfvm_batch* b, const vfvm_control* ctl, const double* inival, double* U, double time,
@@ -149,6 +197,7 @@ extern "C" int vfvm_batch_tune(vfvm_batch* b, const vfvm_control* ctl, const dou
   const size_t n = (size_t)b->offsets[b->ninst];
   float best = 1e30f;
   int bestc = candidates[0];
+  VFVM_CUDA(wait_legacy_stream(b));
   for (int k = 0; k < ncand; ++k) {
     VFVM_CUDA(cudaMemcpyAsync(b->U.p, inival_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
     VFVM_CUDA(cudaMemcpyAsync(b->Uold.p, inival_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));

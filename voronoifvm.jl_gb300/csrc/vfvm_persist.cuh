@@ -26,7 +26,8 @@ struct vfvm_batch {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int tuned_ctas = 0;
   ~vfvm_batch() {
-    for (auto* c : ctx) vfvm_destroy(c);
+    // clones hold views of the first context's grid tables: destroy it last
+    for (size_t i = ctx.size(); i-- > 0;) vfvm_destroy(ctx[i]);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     if (stream) cudaStreamDestroy(stream);
@@ -37,5 +38,6 @@ namespace vfvm {
 template <class Ph>
 int persistent_solve_t(vfvm_ctx* c, const vfvm_control* ctl, const PersistRunHost& run, vfvm_history* hist, float* ms);
 template <class Ph>
-int batch_run_t(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, double tstep, double lambda, float* ms);
+int batch_run_t(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, double tstep, double lambda,
+                const double* guess, const double* fallback, float* ms);
 }  // namespace vfvm

@@ -126,7 +126,7 @@ namespace vfvm {
 
 template <class Ph, typename KT, int PRECON>
 int batch_launch(vfvm_batch* b, const vfvm_control* ctl, int ctas_per_system, double time, double tstep,
-                 double lambda, float* ms) {
+                 double lambda, const double* guess, const double* fallback, float* ms) {
   auto kern = newton_batch_kernel<Ph, KT, PRECON>;
   int per_sm = 0;
   VFVM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPersistThreads, 0));
@@ -161,7 +161,9 @@ int batch_launch(vfvm_batch* b, const vfvm_control* ctl, int ctas_per_system, do
   int ninst = b->ninst;
   double tinv = 1.0 / tstep;
   int gsz = G;
-  void* args[] = {&insts, &ninst, &order, &dc, &groups, &gsz, &queue, &time, &tinv, &lambda, &outs, &failed};
+  const double* ubase = b->U.p;
+  void* args[] = {&insts, &ninst, &order, &dc, &groups, &gsz, &queue, &time, &tinv, &lambda, &outs, &failed,
+                  &guess, &fallback, &ubase};
   VFVM_CUDA(cudaEventRecord(b->e0, b->stream));
   VFVM_CUDA(cudaLaunchCooperativeKernel((void*)kern, dim3(grid), dim3(kPersistThreads), args, 0, b->stream));
   VFVM_CUDA(cudaEventRecord(b->e1, b->stream));
@@ -188,7 +190,8 @@ int batch_prepare(vfvm_batch* b, int precision) {
 }
 
 template <class Ph>
-int batch_run_t(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, double tstep, double lambda, float* ms) {
+int batch_run_t(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, double tstep, double lambda,
+                const double* guess, const double* fallback, float* ms) {
   const bool f64 = ctl->precision == VFVM_PRECISION_FP64;
   const bool jac = ctl->precon == VFVM_PRECON_JACOBI;
   int rc = f64 ? batch_prepare<Ph, double>(b, ctl->precision) : batch_prepare<Ph, float>(b, ctl->precision);
@@ -196,14 +199,14 @@ int batch_run_t(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, d
   (void)jac;
   switch (ctl->precon) {
     case VFVM_PRECON_JACOBI:
-      return f64 ? batch_launch<Ph, double, VFVM_PRECON_JACOBI>(b, ctl, ctas, time, tstep, lambda, ms)
-                 : batch_launch<Ph, float, VFVM_PRECON_JACOBI>(b, ctl, ctas, time, tstep, lambda, ms);
+      return f64 ? batch_launch<Ph, double, VFVM_PRECON_JACOBI>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms)
+                 : batch_launch<Ph, float, VFVM_PRECON_JACOBI>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms);
     case VFVM_PRECON_ILU0:
-      return f64 ? batch_launch<Ph, double, VFVM_PRECON_ILU0>(b, ctl, ctas, time, tstep, lambda, ms)
-                 : batch_launch<Ph, float, VFVM_PRECON_ILU0>(b, ctl, ctas, time, tstep, lambda, ms);
+      return f64 ? batch_launch<Ph, double, VFVM_PRECON_ILU0>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms)
+                 : batch_launch<Ph, float, VFVM_PRECON_ILU0>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms);
     default:
-      return f64 ? batch_launch<Ph, double, VFVM_PRECON_BLOCK_ILU0>(b, ctl, ctas, time, tstep, lambda, ms)
-                 : batch_launch<Ph, float, VFVM_PRECON_BLOCK_ILU0>(b, ctl, ctas, time, tstep, lambda, ms);
+      return f64 ? batch_launch<Ph, double, VFVM_PRECON_BLOCK_ILU0>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms)
+                 : batch_launch<Ph, float, VFVM_PRECON_BLOCK_ILU0>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms);
   }
 }
 

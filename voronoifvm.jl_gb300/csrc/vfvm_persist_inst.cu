@@ -10,5 +10,6 @@
 namespace vfvm {
 template int persistent_solve_t<VFVM_INST_PHYS>(vfvm_ctx*, const vfvm_control*, const PersistRunHost&, vfvm_history*,
                                                 float*);
-template int batch_run_t<VFVM_INST_PHYS>(vfvm_batch*, const vfvm_control*, int, double, double, double, float*);
+template int batch_run_t<VFVM_INST_PHYS>(vfvm_batch*, const vfvm_control*, int, double, double, double, const double*,
+                                         const double*, float*);
 }  // namespace vfvm

@@ -24,7 +24,7 @@ struct DevState {
   // Newton
   double damp, oldnorm, tolx, rnorm, norm, resnorm, updnorm, dnorm;
   int niter, nround, finished, status, nlin, nnewton, abort, tot_newton;
-  int tot_lin, nsteps, pad6, pad7;
+  int tot_lin, nsteps, early, pad7;  // early: residual control met before the linear solve
   double maxdiff, pad5;
   // BiCGStab
   double rho, alpha, omega, beta, tol2, rr, bnorm2, pad2;

@@ -79,7 +79,8 @@ class Physics:
 
     ``kind``: one of ``_lib.PHYSICS_IDS``; ``data``: its parameter vector;
     ``nodedata``: optional per-node values (shape ``(nnodes,)`` or
-    ``(nnodedata, nnodes)``)."""
+    ``(nnodedata, nnodes)``); assign a new array to change them between solves
+    (an array changed in place is not seen)."""
     kind: str
     data: Sequence[float] = ()
     nodedata: Optional[np.ndarray] = None
@@ -132,8 +133,9 @@ class SolverControl:
     handle_exceptions: bool = False
     store_all: bool = True
     log: bool = False
-    # device loop driver: "persistent" (one cooperative launch per solve) or "graph"
-    engine: str = "persistent"
+    # device loop driver: "persistent" (one cooperative launch per solve), "graph"
+    # (a CUDA graph of full-occupancy kernels) or "auto" (persistent for small systems)
+    engine: str = "auto"
     # batched solves: CTAs per system (0: library default)
     team_ctas: int = 0
 
@@ -181,10 +183,11 @@ class NewtonSolverHistory:
     updatenorm: float = 0.0
     resnorm: float = 0.0
     time: float = 0.0  # seconds
+    status: int = 0    # 0, or the error code of the solve (batched solves report it per system)
 
     @classmethod
     def from_c(cls, h: L.History_t):
-        return cls(h.nnewton, h.nlin, h.nsteps, h.updatenorm, h.resnorm, h.time_ms * 1e-3)
+        return cls(h.nnewton, h.nlin, h.nsteps, h.updatenorm, h.resnorm, h.time_ms * 1e-3, h.status)
 
 
 class TransientSolution:
@@ -225,6 +228,7 @@ class System:
         self.boundary_values = np.zeros((self.nspec, nb), order="F")
         self._ctx = None
         self._ctx_key = None
+        self._nodedata_id = None
         self._keep = None
 
     # -- context management
@@ -261,8 +265,9 @@ class System:
 
     @property
     def ctx(self):
+        nd = self.physics.nodedata
         key = (self.boundary_factors.tobytes(), self.boundary_values.tobytes(),
-               None if self.physics.nodedata is None else id(self.physics.nodedata))
+               None if nd is None else np.shape(nd))
         if self._ctx is None or key != self._ctx_key:
             lib = L.load()
             self.close()
@@ -273,8 +278,17 @@ class System:
                 _raise(status.value or L.ERR_INPUT, "vfvm_create failed")
             self._ctx, self._ctx_key, self._keep = h, key, keep
             self._params = tuple(self.physics.data)
-        elif tuple(self.physics.data) != self._params:
-            self._set_params(self.physics.data)
+            self._nodedata_id = id(nd)
+        else:
+            if tuple(self.physics.data) != self._params:
+                self._set_params(self.physics.data)
+            if nd is not None and id(nd) != self._nodedata_id:
+                # same shape, new values: upload them into the existing context
+                a = np.asarray(nd, dtype=np.float64)
+                a = a.reshape(-1, self.grid.nnodes) if a.ndim == 1 else a
+                h = np.ascontiguousarray(a.T)
+                _raise(L.load().vfvm_set_nodedata(self._ctx, L.ptr(h), a.shape[0]), "vfvm_set_nodedata")
+                self._nodedata_id = id(nd)
         return self._ctx
 
     def _set_params(self, data):
