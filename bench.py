@@ -1,24 +1,32 @@
 #!/usr/bin/env python
 """Benchmark: Newton solves/s at ||F||_inf <= 1e-10 on one GB300.
 
-Workload (the transient benchmark configuration): porous medium equation
-u_t - div(grad u^2) = 0 on the unit square, 513 x 513 points (524,288
-triangles), one species, storage u, flux u_K^2 - u_L^2, initial value
-1e-3 + exp(-|x - (0.5, 0.5)|^2 / 0.1^2), homogeneous Neumann boundary,
-20 implicit Euler steps of dt = 1e-3, FP64 residual.  One benchmark step is
-the whole 20-step run (20 Newton solves); every Newton solve stops on the
-residual criterion max|F| <= 1e-10 over the rows without a Dirichlet penalty
-(the reference's SolverControl.updatecontrol = false).
+Default workload (``--workload learned``, the learned-vs-plain comparison):
+stationary -div(kappa grad u) + exp(u) = f on the unit square, 257 x 257
+points (triangles), u = 0 on the boundary, kappa = exp(G) with G a Gaussian
+random field (covariance exp(-r^2 / (2 * 0.1^2)), sigma 1) and f uniform in
+[-1, 1], both seeded per instance.  The network is trained on 4096 solves of
+the plain method (seeds 0..4095); the timed set is 512 held-out instances
+(seeds 1000000..1000511).  One benchmark step solves all 512 held-out
+instances; every Newton solve stops on max|F| <= 1e-10 over the rows without a
+Dirichlet penalty.
 
-Forms:
-  mixed (headline): FP64 residual and update, FP32 Jacobian + FP32 BiCGStab/ILU0
-                    (Newton refines in FP64)
-  fp64:             FP64 Jacobian and FP64 BiCGStab/ILU0
+Forms (solves/s of each is reported; `value` is the first):
+  learned+mixed+batched: network prediction -> guarded batched Newton (one
+      persistent launch for all instances), FP32 Jacobian and Krylov (FP64
+      residual and update), ILU0 + Galerkin coarse-grid correction stage
+  plain GPU: one system at a time through solve() (CUDA-graph engine), FP64
+      BiCGStab/ILU0, from inival = 0
+  plus the steps in between (coarse stage, batching, mixed precision, learned
+  start) as an ablation.
+
+``--workload porous``: the transient porous-medium run (513 x 513, 20 implicit
+Euler steps of dt = 1e-3).
 
 `value` is device-timed (inputs resident in HBM, L2 flushed between steps);
-`e2e` goes through the reference-facing C ABI call (vfvm_evolve, host
-buffers, copies inside the timed region).  `--impl reference` times the CPU
-restatement of the reference path (assembly + sparse direct solve) on the host.
+`e2e` goes through the public host API with host buffers (copies inside the
+timed region).  `--impl reference` times the CPU restatement of the reference
+path (assembly + sparse direct solve) on the host.
 """
 from __future__ import annotations
 
@@ -329,6 +337,307 @@ def run_ours(args, rank, world):
     return line
 
 
+# ----------------------------------------------------------------------------- learned workload
+LN = 257               # fine grid points per side
+LNC = 33               # coarse subgrid (every 8th node) seen and predicted by the network
+NTRAIN = 4096
+NEVAL = 512
+EVAL_SEED0 = 1_000_000
+COARSE = 196           # coarse-grid correction unknowns
+# Stopping rule of the learned workload: max|F| <= 1e-12, which implies the
+# metric's 1e-10.  On this grid (h^2 = 1.5e-5) max|F| <= 1e-10 still leaves
+# about 6e-8 relative solution error, above the 1e-8 agreement asked of every
+# form; 1e-12 brings it to about 1e-9.
+FTOL_L = 1.0e-12
+METRIC_L = ("Newton solves/s at ||F||<=1e-10 (stationary -div(kappa grad u) + exp(u) = f, 257x257 triangles, "
+            "512 held-out GRF instances): learned+mixed+batched form")
+
+
+def learned_control(vfvm, form):
+    """Solver settings of the forms compared on the learned workload."""
+    base = dict(updatecontrol=False, abstol=FTOL_L, reltol=0.0, reltol_linear=1e-4, maxiters_linear=3000)
+    if form == "plain":            # the plain GPU form: one system at a time, FP64, ILU0
+        return vfvm.SolverControl(engine="graph", precision="fp64", precon_linear="ilu0", **base)
+    if form == "single_coarse":
+        return vfvm.SolverControl(engine="graph", precision="fp64", precon_linear="ilu0", coarse=COARSE, **base)
+    if form == "batched_fp64":
+        return vfvm.SolverControl(precision="fp64", precon_linear="ilu0", coarse=COARSE, **base)
+    if form in ("batched_mixed", "learned"):
+        return vfvm.SolverControl(precision="mixed", precon_linear="ilu0", coarse=COARSE, **base)
+    raise KeyError(form)
+
+
+def kappa_instances(lk, n, seeds):
+    inst = [lk.kappa_instance(n, int(s)) for s in seeds]
+    return np.array([a for a, _ in inst]), np.array([b for _, b in inst])
+
+
+def batch_bytes(info, hist, ncoarse, jbytes=4, vbytes=4):
+    """Algorithmic bytes of a batched solve: per Newton step one assembly, the
+    ILU0 factorisation and the Galerkin product; per BiCGStab iteration two
+    SpMVs, two ILU0 applications, two coarse corrections and the vector updates
+    (each array touched once per use; index arrays counted, L2 reuse not)."""
+    N, E, nnzb = info["nnodes"], info["nedges"], info["nblocks"]
+    n = N  # one species
+    asm = algorithmic_assembly_bytes(N, E, nnzb, 1, False, jbytes)
+    factor = nnzb * (jbytes + vbytes + 4) + N * vbytes
+    galerkin = nnzb * (jbytes + 8) + ncoarse * ncoarse * 4
+    newton = asm + factor + galerkin + 4 * n * 8  # + F -> b, update of U
+    spmv = nnzb * (vbytes + 4) + (N + 1) * 4 + 2 * n * vbytes
+    ilu = nnzb * (vbytes + 4) + N * 4 + 3 * n * vbytes
+    coarse = n * (4 + vbytes) + n * 2 * vbytes + ncoarse * ncoarse * 4
+    vec = (4 + 3 + 7 + 2 + 2) * n * vbytes
+    it = 2 * spmv + 2 * ilu + 2 * coarse + vec
+    return sum(h.nnewton * newton + h.nlin * it for h in hist)
+
+
+def cpu_leg_learned(vfvm, nsolves, logk, f):
+    """CPU restatement of the reference path (C++ assembly + SuperLU) on the
+    first `nsolves` held-out instances, from inival 0, same stopping rule."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    x = np.linspace(0.0, 1.0, LN)
+    g = vfvm.simplexgrid(x, x)
+    c = O.Control()
+    c.updatecontrol = False
+    c.abstol = FTOL_L
+    c.reltol = 0.0
+    sols, secs = [], 0.0
+    for i in range(nsolves):
+        osys = O.OracleSystem(g, "kappa_exp", [float(f[i])], nodedata=np.exp(logk[i]))
+        t0 = time.perf_counter()
+        u, _ = O.solve_step(osys, np.zeros(g.nnodes), c)
+        secs += time.perf_counter() - t0
+        sols.append(u)
+    return nsolves / secs, secs, sols
+
+
+def run_learned(args, rank, world):
+    import ctypes
+    import torch
+    import __graft_entry__ as ge
+    vfvm = ge.load_package()
+    lk = vfvm.learned
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    cuda = torch.device(f"cuda:{dev}")
+    t_setup = time.perf_counter()
+    # --- training data: plain-method solutions of NTRAIN seeded instances (batched on the GPU)
+    sweep = lk.KappaSweep(LN, NEVAL)
+    N = sweep.nnodes
+    zeros = torch.zeros(NEVAL * N, dtype=torch.float64, device=cuda)
+    U = torch.empty_like(zeros)
+    model = lk.LearnedInitialIterate(LN, LNC, hidden=512, layers=4, max_batch=NEVAL, seed=0)
+    ctl_train = learned_control(vfvm, "batched_mixed")
+    Xtr, Ttr = [], []
+    t_data = time.perf_counter()
+    tuned = None
+    for c0 in range(0, args.ntrain, NEVAL):
+        seeds = np.arange(c0, min(c0 + NEVAL, args.ntrain))
+        logk, f = kappa_instances(lk, LN, seeds)
+        sweep.load(logk, f)
+        if tuned is None:
+            tuned = sweep.solver.tune(zeros.data_ptr(), ctl_train, candidates=(2, 4, 8))
+        hist, _ = sweep.solve_device(zeros.data_ptr(), U.data_ptr(), ctl_train)
+        if any(h.status != 0 for h in hist[:len(seeds)]):
+            raise RuntimeError("a training solve failed")
+        Xtr.append(model.features(logk, f))
+        Ttr.append(model.coarse(U.view(NEVAL, N)[:len(seeds)].cpu().numpy()))
+    t_data = time.perf_counter() - t_data
+    t_train = time.perf_counter()
+    Xtr = np.concatenate(Xtr)
+    losses = model.fit(Xtr, np.concatenate(Ttr), scale=lk.kappa_scale(Xtr[:, -1]), epochs=args.epochs, batch=256,
+                       lr=1e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t_train
+    # --- held-out set
+    logk_e, f_e = kappa_instances(lk, LN, np.arange(EVAL_SEED0, EVAL_SEED0 + NEVAL))
+    sweep.load(logk_e, f_e)
+    Xe = torch.from_numpy(model.features(logk_e, f_e)).to(cuda)
+    Se = torch.from_numpy(lk.kappa_scale(f_e)).to(cuda)
+    guess = torch.empty((NEVAL, N), dtype=torch.float64, device=cuda)
+    flush = torch.empty(int(512 * 2 ** 20 // 4), dtype=torch.float32, device=cuda)  # > L2 (129 MB)
+    t_setup = time.perf_counter() - t_setup
+
+    def timed(fn, steps, warmup):
+        ms, out = [], None
+        for it in range(warmup + steps):
+            flush.fill_(float(it))
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            out = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            if it >= warmup:
+                ms.append(e0.elapsed_time(e1))
+        return float(np.mean(ms)), out
+
+    ctl_l = learned_control(vfvm, "learned")
+
+    def learned_step():
+        model.predict_device(Xe, scale=Se, out=guess)
+        return sweep.solve_device(zeros.data_ptr(), U.data_ptr(), ctl_l, guess_dev=guess.data_ptr())
+
+    def plain_batch(ctl):
+        # a system whose Newton fails is counted, not fatal (its status is in the history)
+        try:
+            sweep.solve_device(zeros.data_ptr(), U.data_ptr(), ctl)
+        except vfvm.ConvergenceError:
+            pass
+        return sweep.solver.history, None
+
+    forms = {}
+    with ClockSampler(dev) as clk:
+        ms_l, (hist_l, from_guess) = timed(learned_step, args.steps, args.warmup)
+    clocks = clk.summary()
+    U_learned = U.view(NEVAL, N).cpu().numpy()
+    forms["learned_mixed_batched"] = dict(
+        solves_per_s=NEVAL / (ms_l * 1e-3), newton_per_solve=float(np.mean([h.nnewton for h in hist_l])),
+        krylov_per_solve=float(np.mean([h.nlin for h in hist_l])), from_guess=int(from_guess.sum()))
+    kernel_ms = float(np.mean([h.time for h in hist_l])) * 1e3  # the batched launch alone (CUDA events)
+    # --- ablation: the same batch without the learned start, in FP64, and without the coarse stage
+    for name in ("batched_mixed", "batched_fp64"):
+        ctl = learned_control(vfvm, name)
+        ms, (h, _) = timed(lambda: plain_batch(ctl), 1, 1)
+        ok = [x for x in h if x.status == 0]
+        forms[name] = dict(solves_per_s=len(ok) / (ms * 1e-3), newton_per_solve=float(np.mean([x.nnewton for x in ok])),
+                           krylov_per_solve=float(np.mean([x.nlin for x in ok])), failed=len(h) - len(ok))
+    # --- one system at a time through solve() (plain GPU form, and with the coarse stage)
+    x = np.linspace(0.0, 1.0, LN)
+    single = vfvm.System(sweep.grid, vfvm.Physics("kappa_exp", [float(f_e[0])], np.exp(logk_e[0])))
+    for name in ("plain", "single_coarse"):
+        ctl = learned_control(vfvm, name)
+        vfvm.solve(single, inival=0.0, control=ctl)  # warm-up: graph build
+        nn, nl, secs = [], [], 0.0
+        for i in range(args.single_sample):
+            single.physics.data = [float(f_e[i])]
+            single.physics.nodedata = np.exp(logk_e[i])
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            vfvm.solve(single, inival=0.0, control=ctl)
+            secs += time.perf_counter() - t0
+            h = vfvm.solve.last_history
+            nn.append(h.nnewton)
+            nl.append(h.nlin)
+        forms[name] = dict(solves_per_s=args.single_sample / secs, newton_per_solve=float(np.mean(nn)),
+                           krylov_per_solve=float(np.mean(nl)), sample=args.single_sample)
+    # --- e2e through the public API with host buffers
+    inival_h = np.zeros(NEVAL * N)
+    e2e = []
+    for it in range(args.warmup + max(1, min(args.steps, 3))):
+        flush.fill_(float(it))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sweep.load(logk_e, f_e)
+        Xh = torch.from_numpy(model.features(logk_e, f_e)).to(cuda)
+        ini = torch.from_numpy(inival_h).to(cuda)
+        g = model.predict_device(Xh, scale=torch.from_numpy(lk.kappa_scale(f_e)).to(cuda))
+        sweep.solve_device(ini.data_ptr(), U.data_ptr(), ctl_l, guess_dev=g.data_ptr())
+        Uh = U.cpu().numpy()
+        t1 = time.perf_counter()
+        if it >= args.warmup:
+            e2e.append(t1 - t0)
+    e2e_value = NEVAL / float(np.mean(e2e))
+    h2d = int(logk_e.nbytes + f_e.nbytes + Xh.numel() * 4 + inival_h.nbytes)
+    d2h = int(Uh.nbytes)
+    # --- roofline of the dominant kernel (the batched Newton launch)
+    peak, peak_kind = peaks()
+    info = sweep.systems[0].info()
+    B = batch_bytes(info, hist_l, COARSE)
+    achieved = B / (kernel_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC_L, "value": forms["learned_mixed_batched"]["solves_per_s"], "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_l, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"kappa-exp {LN}x{LN} triangles, {NEVAL} held-out GRF instances per step "
+                               f"(network trained on {args.ntrain} plain solves), stopping rule max|F|<=1e-12 (implies the metric's 1e-10)",
+                   "form": "network start (guarded) + FP64 residual/update, FP32 Jacobian + FP32 BiCGStab with "
+                           f"multicolour ILU0 and a {COARSE}-unknown Galerkin coarse stage, all instances in one "
+                           "persistent launch",
+                   "l2": "flushed (512 MB write) between timed steps; the per-step working set (~3 GB) exceeds L2",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "forms": forms,
+        "learned_vs_plain": forms["learned_mixed_batched"]["solves_per_s"] / forms["plain"]["solves_per_s"],
+        "training": {"instances": args.ntrain, "epochs": args.epochs, "loss_first": losses[0], "loss_last": losses[-1],
+                     "data_s": t_data, "train_s": t_train, "setup_s": t_setup, "tuned_ctas": tuned[0] if tuned else None},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"kernel": "batched Newton (persistent cooperative launch: assembly, ILU0, coarse stage, BiCGStab)",
+                     "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes": B, "ms_per_launch": kernel_ms},
+        "gpu_launches": int(args.steps * (len(model.sizes) - 1 + 3)),
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu:
+        sps, secs, osols = cpu_leg_learned(vfvm, args.cpu_solves, logk_e, f_e)
+        line["cpu_baseline"] = {"value": sps, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"{args.cpu_solves} held-out instance(s) from inival 0 (C++ assembly "
+                                          f"restatement + SuperLU), {secs:.1f} s"}
+        err = max(float(np.max(np.abs(U_learned[i] - u)) / np.max(np.abs(u))) for i, u in enumerate(osols))
+        line["max_rel_err_vs_oracle"] = err
+    if rank == 0:
+        print(json.dumps(line))
+    return line
+
+
+def _oracle_instance_solve(seed):
+    """Worker of the reference arm: one held-out instance solved by the CPU
+    restatement (C++ assembly + SuperLU) from inival 0; returns seconds."""
+    import __graft_entry__ as ge
+    vfvm = ge.load_package()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    logk, f = vfvm.learned.kappa_instance(LN, seed)
+    x = np.linspace(0.0, 1.0, LN)
+    g = vfvm.simplexgrid(x, x)
+    c = O.Control()
+    c.updatecontrol = False
+    c.abstol = FTOL_L
+    c.reltol = 0.0
+    t0 = time.perf_counter()
+    osys = O.OracleSystem(g, "kappa_exp", [float(f)], nodedata=np.exp(logk))
+    O.solve_step(osys, np.zeros(g.nnodes), c)
+    return time.perf_counter() - t0
+
+
+def run_reference_learned(args, rank, world):
+    """Reference arm: the CPU restatement on all host cores, one instance per
+    process; each step solves `cores` held-out instances side by side."""
+    import multiprocessing as mp
+    if rank != 0:
+        return None
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    seed = EVAL_SEED0
+    with ctx.Pool(cores) as pool:
+        walls = []
+        for it in range(args.warmup + max(args.steps, 1)):
+            seeds = list(range(seed, seed + cores))
+            seed += cores
+            t0 = time.perf_counter()
+            pool.map(_oracle_instance_solve, seeds)
+            if it >= args.warmup:
+                walls.append(time.perf_counter() - t0)
+    secs = float(np.sum(walls))
+    sps = cores * len(walls) / secs
+    line = {
+        "impl": "reference", "metric": METRIC_L, "value": sps, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / len(walls),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"kappa-exp {LN}x{LN} triangles, held-out GRF instances, stopping rule max|F|<=1e-12",
+                   "sample": f"{cores} held-out instances per step, one process per core, one Newton solve each "
+                             "from inival 0"},
+        "cpu_baseline": {"value": sps, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores * len(walls)} held-out instances (C++ assembly restatement + SuperLU)"},
+        "e2e": {"value": sps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return line
+
+
 def run_assembly_only(args):
     """Profiling mode: build the workload and launch the assembly kernel
     `--steps` times (FP32-Jacobian form), nothing else."""
@@ -360,10 +669,14 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--nsteps", type=int, default=NSTEPS)
-    ap.add_argument("--cpu-solves", type=int, default=2)
+    ap.add_argument("--cpu-solves", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--engine", choices=["persistent", "graph"], default="graph")
     ap.add_argument("--precon", choices=["ilu0", "jacobi", "block_ilu0"], default=PRECON)
+    ap.add_argument("--workload", choices=["learned", "porous"], default="learned")
+    ap.add_argument("--ntrain", type=int, default=NTRAIN)
+    ap.add_argument("--epochs", type=int, default=300)
+    ap.add_argument("--single-sample", type=int, default=16)
     args = ap.parse_args()
     globals()["ENGINE"] = args.engine
     globals()["PRECON"] = args.precon
@@ -375,12 +688,12 @@ def main():
     if args.impl == "reference":
         if world > 1 and rank != 0:
             return
-        run_reference(args, rank, world)
+        (run_reference_learned if args.workload == "learned" else run_reference)(args, rank, world)
         return
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
-    run_ours(args, rank, world)
+    (run_learned if args.workload == "learned" else run_ours)(args, rank, world)
     if world > 1:
         import torch
         torch.distributed.destroy_process_group()

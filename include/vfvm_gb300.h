@@ -119,7 +119,11 @@ typedef struct vfvm_control {
   int32_t num_final_steps, force_first_step, handle_exceptions, store_all;
   int32_t engine;              /* VFVM_ENGINE_*: how the device Newton loop is driven */
   int32_t team_ctas;           /* batched solves: CTAs per system (0 = default) */
+  int32_t coarse;              /* coarse-grid correction stage of the preconditioner: about this many
+                                  coarse unknowns (aggregates x nspec, at most VFVM_COARSE_MAX); 0 = off */
 } vfvm_control;
+
+#define VFVM_COARSE_MAX 208
 
 #define VFVM_ENGINE_GRAPH 0      /* CUDA graph of kernels with conditional WHILE nodes */
 #define VFVM_ENGINE_PERSISTENT 1 /* one persistent cooperative launch per solve (or per fixed-step run) */
@@ -291,13 +295,15 @@ int vfvm_mlp_forward(vfvm_mlp* net, int32_t batch, const float* X, float* Y);
 int vfvm_mlp_gradients(vfvm_mlp* net, int32_t batch, const float* X, const float* T, float* grads, float* loss);
 /* one Adam step with learning rate lr; loss (optional) before the step */
 int vfvm_mlp_train_step(vfvm_mlp* net, int32_t batch, const float* X, const float* T, float lr, float* loss);
-/* fine = scale * (bilinear prolongation of coarse) + shift for batch coarse
- * fields (nc x nc nodes, x fastest, FP32) onto nested fine grids
+/* fine = s_b * (scale * (bilinear prolongation of coarse) + shift) for batch
+ * coarse fields (nc x nc nodes, x fastest, FP32) onto nested fine grids
  * ((nc-1)*ratio+1 nodes per side, FP64, the node order of simplexgrid);
- * instance b reads coarse + b*coarse_stride and writes fine + b*fine_stride
- * (device pointers), enqueued on stream (NULL: the legacy default stream). */
+ * instance b reads coarse + b*coarse_stride and writes fine + b*fine_stride;
+ * s_b = inst_scale[b] (device array of batch values; NULL: 1).  Device
+ * pointers, enqueued on stream (NULL: the legacy default stream). */
 int vfvm_prolong_bilinear(int32_t batch, int32_t nc, int32_t ratio, const float* coarse, int64_t coarse_stride,
-                          double scale, double shift, double* fine, int64_t fine_stride, void* stream);
+                          double scale, double shift, const double* inst_scale, double* fine, int64_t fine_stride,
+                          void* stream);
 
 #ifdef __cplusplus
 }

@@ -27,9 +27,10 @@ def test_example440_as_one_batch(vfvm):
     assert total == pytest.approx(testval, rel=RTOL)
 
 
+@pytest.mark.parametrize("coarse", [0, 60])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("precon", ["jacobi", "ilu0", "block_ilu0"])
-def test_rd2_batch_vs_oracle(vfvm, oracle, precision, precon):
+def test_rd2_batch_vs_oracle(vfvm, oracle, precision, precon, coarse):
     rng = np.random.default_rng(7)
     sizes = [9, 25, 13, 17, 21, 11]
     systems, params = [], []
@@ -38,7 +39,7 @@ def test_rd2_batch_vs_oracle(vfvm, oracle, precision, precon):
         params.append(p)
         systems.append(vfvm.System(vfvm.simplexgrid(lin(n - 1), lin(n - 1)), vfvm.Physics("rd2", p), species=[1, 2]))
     batch = vfvm.BatchSolver(systems)
-    control = vfvm.SolverControl(precision=precision, precon_linear=precon, maxiters_linear=500)
+    control = vfvm.SolverControl(precision=precision, precon_linear=precon, maxiters_linear=500, coarse=coarse)
     sols = batch.solve([np.full(s.ndofs, 0.5) for s in systems], control=control)
     for s, p, u in zip(systems, params, sols):
         osys = oracle.OracleSystem(s.grid, "rd2", p)

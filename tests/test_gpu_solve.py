@@ -163,6 +163,25 @@ def test_kappa_exp_vs_oracle(vfvm, oracle):
     assert rel_err(U, oracle_solution(oracle, g, "kappa_exp", [0.7], nodedata=kappa)) <= SOL_TOL
 
 
+@pytest.mark.parametrize("engine,precon", [("graph", "ilu0"), ("graph", "jacobi"), ("persistent", "ilu0"),
+                                           ("persistent", "block_ilu0")])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_coarse_stage_vs_oracle(vfvm, oracle, engine, precon, precision):
+    # the coarse-grid correction changes the Krylov iterations, not the solution
+    g = vfvm.simplexgrid(lin(40), lin(40))
+    kappa = np.exp(np.random.default_rng(6).normal(size=g.nnodes))
+    sys = vfvm.System(g, vfvm.Physics("kappa_exp", [-0.4], kappa))
+    plain = vfvm.SolverControl(engine=engine, precon_linear=precon, precision=precision, maxiters_linear=1000)
+    vfvm.solve(sys, inival=0.0, control=plain)
+    lin_plain = vfvm.solve.last_history.nlin
+    control = vfvm.SolverControl(engine=engine, precon_linear=precon, precision=precision, maxiters_linear=1000,
+                                 coarse=100)
+    U = vfvm.solve(sys, inival=0.0, control=control)
+    lin_coarse = vfvm.solve.last_history.nlin
+    assert rel_err(U, oracle_solution(oracle, g, "kappa_exp", [-0.4], nodedata=kappa)) <= SOL_TOL
+    assert lin_coarse < 0.7 * lin_plain
+
+
 def test_bipolar_embedding_vs_oracle(vfvm, oracle):
     g = vfvm.simplexgrid(lin(6), lin(6), lin(6))
     sys = vfvm.System(g, vfvm.Physics("bipolar", BIPOLAR), species=[1, 2, 3])

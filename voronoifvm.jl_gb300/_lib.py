@@ -17,6 +17,7 @@ c_d, c_i32, c_i64, c_vp = ctypes.c_double, ctypes.c_int32, ctypes.c_int64, ctype
 OK, ERR_CONVERGENCE, ERR_ASSEMBLY, ERR_LINEAR, ERR_TIMEOUT, ERR_INPUT, ERR_CUDA, ERR_EMBEDDING = range(8)
 ERR_NOALLOC_LIMIT = 8
 NOALLOC_MAX_ROWS = 131072  # VFVM_NOALLOC_MAX_ROWS
+COARSE_MAX = 208           # VFVM_COARSE_MAX
 
 PHYSICS_IDS = {
     "ex105": 1, "ex106": 2, "ex110": 3, "ex160": 4, "ex207": 5, "ex301": 6, "ex440": 7,
@@ -52,7 +53,8 @@ class Control_t(ctypes.Structure):
                 ("dp", c_d), ("dp_min", c_d), ("dp_max", c_d), ("dp_grow", c_d), ("dp_decrease", c_d),
                 ("du_opt", c_d), ("du_max_factor", c_d),
                 ("num_final_steps", c_i32), ("force_first_step", c_i32), ("handle_exceptions", c_i32),
-                ("store_all", c_i32), ("engine", c_i32), ("team_ctas", c_i32)]
+                ("store_all", c_i32), ("engine", c_i32), ("team_ctas", c_i32),
+                ("coarse", c_i32)]
 
 
 class History_t(ctypes.Structure):
@@ -100,7 +102,7 @@ SIGNATURES = {
     "vfvm_mlp_forward": (ctypes.c_int, [c_vp, c_i32, c_vp, c_vp]),
     "vfvm_mlp_gradients": (ctypes.c_int, [c_vp, c_i32, c_vp, c_vp, P(ctypes.c_float), P(ctypes.c_float)]),
     "vfvm_mlp_train_step": (ctypes.c_int, [c_vp, c_i32, c_vp, c_vp, ctypes.c_float, P(ctypes.c_float)]),
-    "vfvm_prolong_bilinear": (ctypes.c_int, [c_i32, c_i32, c_i32, c_vp, c_i64, c_d, c_d, c_vp, c_i64, c_vp]),
+    "vfvm_prolong_bilinear": (ctypes.c_int, [c_i32, c_i32, c_i32, c_vp, c_i64, c_d, c_d, c_vp, c_vp, c_i64, c_vp]),
 }
 
 _lib = None

@@ -28,6 +28,7 @@ int set_time(vfvm_ctx* c, double time, double tstep, double lambda) {
 
 int set_control(vfvm_ctx* c, const vfvm_control* ctl) {
   if (ctl->precon == VFVM_PRECON_BLOCK_ILU0 && c->ncolors > kMaxBlockIluColors) return VFVM_ERR_INPUT;
+  if (int rc = ensure_coarse(c, ctl->coarse)) return rc;
   static thread_local DevControl staged;
   staged = make_devcontrol(*ctl);
   VFVM_CUDA(cudaMemcpyAsync(c->ws->ctl, &staged, sizeof(DevControl), cudaMemcpyHostToDevice, c->stream));
@@ -41,6 +42,7 @@ int check_control(const vfvm_control* ctl) {
   if (ctl->precon != VFVM_PRECON_JACOBI && ctl->precon != VFVM_PRECON_ILU0 && ctl->precon != VFVM_PRECON_BLOCK_ILU0)
     return VFVM_ERR_INPUT;
   if (ctl->krylov != VFVM_KRYLOV_BICGSTAB) return VFVM_ERR_INPUT;
+  if (ctl->coarse < 0 || ctl->coarse > VFVM_COARSE_MAX) return VFVM_ERR_INPUT;
   return VFVM_OK;
 }
 

@@ -231,7 +231,7 @@ extern "C" void vfvm_control_default(vfvm_control* c) {
   c->dp = 1.0; c->dp_min = 1.0e-3; c->dp_max = 1.0; c->dp_grow = 1.0; c->dp_decrease = 0.5;
   c->du_opt = 0.1; c->du_max_factor = 1.2;
   c->num_final_steps = 5; c->force_first_step = 0; c->handle_exceptions = 0; c->store_all = 1;
-  c->engine = VFVM_ENGINE_AUTO; c->team_ctas = 0;
+  c->engine = VFVM_ENGINE_AUTO; c->team_ctas = 0; c->coarse = 0;
 }
 
 extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph, int* status) {
@@ -551,6 +551,7 @@ extern "C" void vfvm_destroy(vfvm_ctx* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->ws) destroy_workspace(c->ws);
+  for (auto& kv : c->coarse_spaces) delete kv.second;
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

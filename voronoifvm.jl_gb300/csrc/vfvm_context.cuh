@@ -1,7 +1,9 @@
 // Context: device-resident tables and work buffers of one system.
 #pragma once
+#include <map>
 #include <vector>
 #include <string>
+#include "vfvm_coarse.cuh"
 #include "vfvm_common.cuh"
 
 namespace vfvm {
@@ -55,6 +57,15 @@ struct AsmTables {
 
 struct Workspace;  // Krylov / Newton work buffers (vfvm_solver.cu)
 
+// Aggregation tables of the coarse-grid correction (vfvm_coarse.cuh), built for
+// a target number of coarse unknowns; contexts on a shared grid view the
+// tables of the first one and own only the matrix and vectors.
+struct CoarseSpace {
+  int target = 0, nagg = 0, nc = 0, npairs = 0;
+  DBuf<int> agg_of_node, agg_ptr, agg_nodes, pair_ptr, pair_ij, pair_slot, pair_row;
+  DBuf<float> A, rc, zc;
+};
+
 }  // namespace vfvm
 
 struct vfvm_ctx {
@@ -98,8 +109,13 @@ struct vfvm_ctx {
   vfvm::DBuf<int> errflag;
 
   vfvm::Workspace* ws = nullptr;
+  vfvm::CoarseSpace* coarse = nullptr;     // coarse-grid correction in use (nullptr: none)
+  std::map<int, vfvm::CoarseSpace*> coarse_spaces;  // built on first use, by target size
+  const vfvm_ctx* grid_base = nullptr;     // clones: the context whose grid tables they view
 
   vfvm::AsmTables tables() const;
+  // the coarse stage's device view (nc == 0 when it is off)
+  vfvm::CoarseData coarse_data() const;
 };
 
 namespace vfvm {
@@ -118,4 +134,7 @@ void destroy_workspace(Workspace* w);
 vfvm_ctx* clone_context(const vfvm_ctx* base, const vfvm_physics_desc* ph, int* status);
 // replace the per-node physics data (nnodes x nnodedata values, host)
 int set_nodedata(vfvm_ctx* c, const double* data, int nnd);
+// select the coarse space for about `target` coarse unknowns (0: none), building
+// it on first use.  Clones view the tables of their grid_base (built first).
+int ensure_coarse(vfvm_ctx* c, int target);
 }  // namespace vfvm

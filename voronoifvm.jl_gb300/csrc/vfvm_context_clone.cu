@@ -29,6 +29,7 @@ vfvm_ctx* clone_context(const vfvm_ctx* b, const vfvm_physics_desc* ph, int* sta
   c->nregions = b->nregions; c->nbregions = b->nbregions; c->single_region = b->single_region;
   c->multireg = b->multireg; c->nnd = b->nnd; c->device = b->device;
   c->nnzb = b->nnzb; c->nnz = b->nnz; c->ncolors = b->ncolors; c->h_color_ptr = b->h_color_ptr;
+  c->grid_base = b->grid_base ? b->grid_base : b;
   CLONE_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   // shared grid tables
   c->coord.view(b->coord); c->node_fac.view(b->node_fac); c->slot_fac.view(b->slot_fac);

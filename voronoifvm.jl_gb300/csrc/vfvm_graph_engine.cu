@@ -663,6 +663,8 @@ int ensure_workspace(vfvm_ctx* c, int precision) {
     VFVM_CUDA(w->Uinit.alloc((size_t)c->N * c->ns));
     VFVM_CUDA(cudaEventCreate(&w->ev0));
     VFVM_CUDA(cudaEventCreate(&w->ev1));
+    VFVM_CUDA(cudaFuncSetAttribute(coarse_invert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)coarse_smem_bytes(kCoarseMax)));
     // node colours for the ILU0 ordering
     std::vector<int> col(c->N, 0);
     for (int q = 0; q < c->ncolors; ++q) {
@@ -713,6 +715,17 @@ static void record_ilu_apply(vfvm_ctx* c, KVecs<KT>& k, const KT* y, KT* z, cuda
   }
 }
 
+// z += P A_c^-1 P^T y (coarse-grid correction stage)
+template <int NS, typename KT>
+static void record_coarse_add(vfvm_ctx* c, const KT* y, KT* z, cudaStream_t s) {
+  const CoarseData cd = c->coarse_data();
+  if (!cd.nc) return;
+  const int64_t n = (int64_t)c->N * NS;
+  coarse_restrict_kernel<NS, KT><<<(cd.nagg * 32 + 255) / 256, 256, 0, s>>>(cd, y);
+  coarse_matvec_kernel<<<(cd.nc * 32 + 255) / 256, 256, 0, s>>>(cd);
+  coarse_prolong_kernel<NS, KT><<<red_blocks(n), kThreads, 0, s>>>(cd, z, n);
+}
+
 // z = M^-1 y
 template <int NS, typename KT>
 static void record_precon_apply(vfvm_ctx* c, KVecs<KT>& k, int precon, const KT* y, KT* z, cudaStream_t s) {
@@ -720,6 +733,7 @@ static void record_precon_apply(vfvm_ctx* c, KVecs<KT>& k, int precon, const KT*
     jacobi_apply_kernel<NS, KT><<<(c->N + 127) / 128, 128, 0, s>>>(c->N, k.dinv.p, y, z);
   else
     record_ilu_apply<NS, KT>(c, k, y, z, s);
+  record_coarse_add<NS, KT>(c, y, z, s);
 }
 
 template <int NS, int LPR, typename KT>
@@ -731,7 +745,8 @@ static void record_krylov_iteration(vfvm_ctx* c, KVecs<KT>& k, const KT* A, int 
   const int rpb = kThreads / LPR;
   int sblocks = (N + rpb - 1) / rpb;
   if (sblocks > kMaxRedBlocks) sblocks = kMaxRedBlocks;
-  const bool jac = precon == VFVM_PRECON_JACOBI;
+  // block Jacobi without a coarse stage: SpMV, Jacobi and dot product fused
+  const bool jac = precon == VFVM_PRECON_JACOBI && c->coarse_data().nc == 0;
   const int eb = red_blocks(n);
   bi_p_kernel<KT><<<eb, kThreads, 0, s>>>(n, k.r.p, k.p.p, k.v.p, w->st);
   // v = M^-1 A p,  alpha = rho / (r0 . v)
@@ -741,7 +756,7 @@ static void record_krylov_iteration(vfvm_ctx* c, KVecs<KT>& k, const KT* A, int 
   } else {
     spmv_kernel<NS, LPR, KT, 0><<<sblocks, kThreads, 0, s>>>(N, c->browptr.p, c->bcol.p, A, k.p.p, nullptr, nullptr,
                                                              k.b.p, w->st, w->partials.p);
-    record_ilu_apply<NS, KT>(c, k, k.b.p, k.v.p, s);
+    record_precon_apply<NS, KT>(c, k, precon, k.b.p, k.v.p, s);
     dot_kernel<KT, 1><<<eb, kThreads, 0, s>>>(n, k.v.p, k.r0.p, w->st, w->partials.p);
   }
   bi_s_kernel<KT><<<eb, kThreads, 0, s>>>(n, k.r.p, k.v.p, k.s.p, w->st);
@@ -752,7 +767,7 @@ static void record_krylov_iteration(vfvm_ctx* c, KVecs<KT>& k, const KT* A, int 
   } else {
     spmv_kernel<NS, LPR, KT, 0><<<sblocks, kThreads, 0, s>>>(N, c->browptr.p, c->bcol.p, A, k.s.p, nullptr, nullptr,
                                                              k.b.p, w->st, w->partials.p);
-    record_ilu_apply<NS, KT>(c, k, k.b.p, k.t.p, s);
+    record_precon_apply<NS, KT>(c, k, precon, k.b.p, k.t.p, s);
     dot_kernel<KT, 2><<<eb, kThreads, 0, s>>>(n, k.t.p, k.s.p, w->st, w->partials.p);
   }
   bi_xr_kernel<KT><<<eb, kThreads, 0, s>>>(n, k.x.p, k.r.p, k.s.p, k.t.p, k.p.p, k.r0.p, w->st, w->ctl, w->partials.p,
@@ -775,6 +790,12 @@ static void record_precon_setup(vfvm_ctx* c, KVecs<KT>& k, const MT* J, int prec
         ilu_factor_kernel<NS, KT><<<b, 128, 0, s>>>(c->color_nodes.p, cb, ce, w->node_color.p, c->browptr.p, c->bcol.p,
                                                     c->diag.p, c->lower_ptr.p, c->lower_slots.p, k.ilu.p, k.dinv.p);
     }
+  }
+  const CoarseData cd = c->coarse_data();
+  if (cd.nc) {  // Galerkin coarse matrix and its inverse
+    cudaMemsetAsync(cd.A, 0, (size_t)cd.nc * cd.nc * sizeof(float), s);
+    coarse_galerkin_kernel<NS, MT><<<(cd.npairs * 32 + 255) / 256, 256, 0, s>>>(cd, c->bcol.p, J);
+    coarse_invert_kernel<<<1, 1024, coarse_smem_bytes(cd.nc), s>>>(cd.A, cd.nc);
   }
 }
 
@@ -880,7 +901,7 @@ static int build_graph_t(vfvm_ctx* c, int precision, int precon, int kind, cudaG
 
 int get_graph(vfvm_ctx* c, int precision, int precon, int kind, cudaGraphExec_t* out) {
   Workspace* w = c->ws;
-  GraphKey key{precision, precon, kind};
+  GraphKey key{precision, precon, kind, c->coarse ? c->coarse->target : 0};
   auto it = w->graphs.find(key);
   if (it != w->graphs.end()) { *out = it->second; return VFVM_OK; }
   cudaGraph_t g = nullptr;

@@ -2,6 +2,7 @@
 // NS x NS diagonal blocks) on a block-CSR matrix.  Runs inside one persistent
 // launch: a whole grid (GridTeam) or one CTA (CtaTeam).
 #pragma once
+#include "vfvm_coarse.cuh"
 #include "vfvm_team.cuh"
 
 namespace vfvm {
@@ -17,6 +18,7 @@ struct KrylovData {
   const KT* b;              // N * NS
   KT* x;                    // N * NS (output; initial guess 0)
   KT *r, *r0, *p, *v, *s, *t;
+  CoarseData cd;            // coarse-grid correction stage (cd.nc == 0: none)
 };
 
 struct KrylovCtl {

@@ -445,9 +445,11 @@ extern "C" int vfvm_mlp_train_step(vfvm_mlp* m, int32_t batch, const float* X, c
 
 namespace vfvm {
 
-// fine[b][ix + nf*iy] = scale * (bilinear interpolation of coarse[b][cx + nc*cy]) + shift, nf = (nc-1)*r+1
+// fine[b][ix + nf*iy] = s_b * (scale * (bilinear interpolation of coarse[b][cx + nc*cy]) + shift),
+// nf = (nc-1)*r+1, s_b = inst_scale[b] (1 without inst_scale)
 __global__ void prolong_bilinear_kernel(int batch, int nc, int r, const float* __restrict__ coarse, int64_t cstride,
-                                        double scale, double shift, double* __restrict__ fine, int64_t fstride) {
+                                        double scale, double shift, const double* __restrict__ inst_scale,
+                                        double* __restrict__ fine, int64_t fstride) {
   const int nf = (nc - 1) * r + 1;
   const int64_t per = (int64_t)nf * nf;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -459,24 +461,24 @@ __global__ void prolong_bilinear_kernel(int batch, int nc, int r, const float* _
   const double tx = (double)(ix - cx * r) / r, ty = (double)(iy - cy * r) / r;
   const float* c = coarse + b * cstride + cx + (int64_t)nc * cy;
   const double v = (1.0 - tx) * (1.0 - ty) * c[0] + tx * (1.0 - ty) * c[1] + (1.0 - tx) * ty * c[nc] + tx * ty * c[nc + 1];
-  fine[b * fstride + k] = scale * v + shift;
+  fine[b * fstride + k] = (inst_scale ? inst_scale[b] : 1.0) * (scale * v + shift);
 }
 
 }  // namespace vfvm
 
 // Bilinear prolongation of batch coarse fields (nc x nc nodes, x fastest, FP32),
-// times scale plus shift, onto the nested fine grids ((nc-1)*ratio+1 nodes per side, FP64), e.g. a
+// times scale plus shift, times an optional per-instance factor, onto the nested fine grids ((nc-1)*ratio+1 nodes per side, FP64), e.g. a
 // coarse network prediction to a Newton initial value.  Device pointers; the
 // instance b reads coarse + b*coarse_stride and writes fine + b*fine_stride.
 extern "C" int vfvm_prolong_bilinear(int32_t batch, int32_t nc, int32_t ratio, const float* coarse,
-                                     int64_t coarse_stride, double scale, double shift, double* fine,
-                                     int64_t fine_stride, void* stream) {
+                                     int64_t coarse_stride, double scale, double shift, const double* inst_scale,
+                                     double* fine, int64_t fine_stride, void* stream) {
   if (batch < 1 || nc < 2 || ratio < 1 || !coarse || !fine) return VFVM_ERR_INPUT;
   const int64_t nf = (int64_t)(nc - 1) * ratio + 1;
   if (coarse_stride < (int64_t)nc * nc || fine_stride < nf * nf) return VFVM_ERR_INPUT;
   const int64_t total = nf * nf * batch;
   prolong_bilinear_kernel<<<nb(total), 256, 0, (cudaStream_t)stream>>>(batch, nc, ratio, coarse, coarse_stride, scale,
-                                                                       shift, fine, fine_stride);
+                                                                       shift, inst_scale, fine, fine_stride);
   VFVM_CUDA(cudaGetLastError());
   return VFVM_OK;
 }

@@ -137,7 +137,7 @@ struct PersistRun {
 };
 
 template <class Ph, typename KT, int PRECON>
-__global__ void __launch_bounds__(kPersistThreads) newton_persistent_kernel(NewtonData<Ph, KT> nd, DevControl ctl,
+__global__ void __launch_bounds__(kPersistThreads, 1) newton_persistent_kernel(NewtonData<Ph, KT> nd, DevControl ctl,
                                                                             GridSync gs, PersistRun run,
                                                                             NewtonOut* out) {
   GroupTeam team = grid_team(gs);
@@ -177,7 +177,7 @@ struct BatchSync {
 };
 
 template <class Ph, typename KT, int PRECON>
-__global__ void __launch_bounds__(kPersistThreads) newton_batch_kernel(const NewtonData<Ph, KT>* __restrict__ insts,
+__global__ void __launch_bounds__(kPersistThreads, 1) newton_batch_kernel(const NewtonData<Ph, KT>* __restrict__ insts,
                                                                        int ninst, const int* __restrict__ order,
                                                                        DevControl ctl, const BatchSync* __restrict__ groups,
                                                                        int gsize, unsigned* queue, double time,

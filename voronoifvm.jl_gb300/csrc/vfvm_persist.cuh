@@ -12,8 +12,8 @@ struct vfvm_batch {
   std::vector<vfvm_ctx*> ctx;
   std::vector<int64_t> offsets;  // dof offsets, ninst+1
   vfvm::DBuf<double> U, Uold;
-  vfvm::DBuf<char> desc;               // NewtonData array of the current precision
-  int desc_precision = -1;
+  vfvm::DBuf<char> desc;               // NewtonData array of the current precision and coarse stage
+  int desc_precision = -1, desc_coarse = 0, desc_coarse_nc = 0;
   vfvm::DBuf<int> order;
   vfvm::DBuf<unsigned> bars;
   vfvm::DBuf<double> partials;

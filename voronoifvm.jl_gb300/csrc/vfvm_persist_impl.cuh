@@ -11,8 +11,9 @@
 
 namespace vfvm {
 
+// coarse: include the context's selected coarse stage (not with block Jacobi)
 template <class Ph, typename KT>
-NewtonData<Ph, KT> make_newton_data(vfvm_ctx* c, double* U, double* Uold) {
+NewtonData<Ph, KT> make_newton_data(vfvm_ctx* c, double* U, double* Uold, bool coarse) {
   Workspace* w = c->ws;
   KVecs<KT>& k = *reinterpret_cast<KVecs<KT>*>(std::is_same<KT, double>::value ? (void*)&w->k64 : (void*)&w->k32);
   KT* J = std::is_same<KT, double>::value ? (KT*)c->J.p : (KT*)c->Jf.p;
@@ -42,6 +43,7 @@ NewtonData<Ph, KT> make_newton_data(vfvm_ctx* c, double* U, double* Uold) {
   nd.il.ilu = k.ilu.p;
   nd.il.y = k.sh.p;
   nd.nvals = c->nnzb * (int64_t)c->ns * c->ns;
+  nd.kd.cd = coarse ? c->coarse_data() : CoarseData{};
   return nd;
 }
 
@@ -57,8 +59,11 @@ int persistent_launch(vfvm_ctx* c, const vfvm_control* ctl, const PersistRunHost
                              float* ms) {
   Workspace* w = c->ws;
   auto kern = newton_persistent_kernel<Ph, KT, PRECON>;
+  NewtonData<Ph, KT> nd = make_newton_data<Ph, KT>(c, c->U.p, c->Uold.p, PRECON != VFVM_PRECON_JACOBI);
+  const size_t smem = nd.kd.cd.nc ? coarse_smem_bytes(nd.kd.cd.nc) : 0;
+  VFVM_CUDA(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  VFVM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPersistThreads, 0));
+  VFVM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPersistThreads, smem));
   const int sms = sm_count();
   if (per_sm < 1 || sms < 1) return VFVM_ERR_CUDA;
   int grid = sms * std::min(per_sm, 2);
@@ -69,14 +74,13 @@ int persistent_launch(vfvm_ctx* c, const vfvm_control* ctl, const PersistRunHost
   if (w->ppartials.n < (size_t)2 * grid * 8) VFVM_CUDA(w->ppartials.alloc((size_t)2 * grid * 8));
   if (w->pout.n < sizeof(NewtonOut)) VFVM_CUDA(w->pout.alloc(sizeof(NewtonOut)));
   VFVM_CUDA(cudaMemsetAsync(w->pbar.p, 0, 8 * sizeof(unsigned), c->stream));
-  NewtonData<Ph, KT> nd = make_newton_data<Ph, KT>(c, c->U.p, c->Uold.p);
   DevControl dc = make_devcontrol(*ctl);
   GridSync gs{w->pbar.p, w->ppartials.p};
   PersistRun run{rh.nsteps, rh.time, 1.0 / rh.tstep, rh.lambda, rh.t0, rh.dt};
   NewtonOut* out = reinterpret_cast<NewtonOut*>(w->pout.p);
   void* args[] = {&nd, &dc, &gs, &run, &out};
   VFVM_CUDA(cudaEventRecord(w->ev0, c->stream));
-  VFVM_CUDA(cudaLaunchCooperativeKernel((void*)kern, dim3(grid), dim3(kPersistThreads), args, 0, c->stream));
+  VFVM_CUDA(cudaLaunchCooperativeKernel((void*)kern, dim3(grid), dim3(kPersistThreads), args, smem, c->stream));
   VFVM_CUDA(cudaEventRecord(w->ev1, c->stream));
   NewtonOut h;
   VFVM_CUDA(cudaMemcpyAsync(&h, out, sizeof(NewtonOut), cudaMemcpyDeviceToHost, c->stream));
@@ -128,8 +132,10 @@ template <class Ph, typename KT, int PRECON>
 int batch_launch(vfvm_batch* b, const vfvm_control* ctl, int ctas_per_system, double time, double tstep,
                  double lambda, const double* guess, const double* fallback, float* ms) {
   auto kern = newton_batch_kernel<Ph, KT, PRECON>;
+  const size_t smem = b->desc_coarse_nc ? coarse_smem_bytes(b->desc_coarse_nc) : 0;
+  VFVM_CUDA(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  VFVM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPersistThreads, 0));
+  VFVM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPersistThreads, smem));
   const int sms = sm_count();
   if (per_sm < 1 || sms < 1) return VFVM_ERR_CUDA;
   const int G = std::max(1, ctas_per_system);
@@ -165,7 +171,7 @@ int batch_launch(vfvm_batch* b, const vfvm_control* ctl, int ctas_per_system, do
   void* args[] = {&insts, &ninst, &order, &dc, &groups, &gsz, &queue, &time, &tinv, &lambda, &outs, &failed,
                   &guess, &fallback, &ubase};
   VFVM_CUDA(cudaEventRecord(b->e0, b->stream));
-  VFVM_CUDA(cudaLaunchCooperativeKernel((void*)kern, dim3(grid), dim3(kPersistThreads), args, 0, b->stream));
+  VFVM_CUDA(cudaLaunchCooperativeKernel((void*)kern, dim3(grid), dim3(kPersistThreads), args, smem, b->stream));
   VFVM_CUDA(cudaEventRecord(b->e1, b->stream));
   VFVM_CUDA(cudaStreamSynchronize(b->stream));
   if (ms) VFVM_CUDA(cudaEventElapsedTime(ms, b->e0, b->e1));
@@ -174,18 +180,24 @@ int batch_launch(vfvm_batch* b, const vfvm_control* ctl, int ctas_per_system, do
   return hfailed ? VFVM_ERR_TIMEOUT : VFVM_OK;
 }
 
+// instance descriptors for a precision and coarse-stage size (0: none)
 template <class Ph, typename KT>
-int batch_prepare(vfvm_batch* b, int precision) {
-  if (b->desc_precision == precision) return VFVM_OK;
+int batch_prepare(vfvm_batch* b, int precision, int coarse) {
+  if (b->desc_precision == precision && b->desc_coarse == coarse) return VFVM_OK;
   std::vector<NewtonData<Ph, KT>> d(b->ninst);
+  int maxnc = 0;
   for (int i = 0; i < b->ninst; ++i) {
     int rc = ensure_workspace(b->ctx[i], precision);
     if (rc) return rc;
-    d[i] = make_newton_data<Ph, KT>(b->ctx[i], b->U.p + b->offsets[i], b->Uold.p + b->offsets[i]);
+    if ((rc = ensure_coarse(b->ctx[i], coarse))) return rc;
+    d[i] = make_newton_data<Ph, KT>(b->ctx[i], b->U.p + b->offsets[i], b->Uold.p + b->offsets[i], coarse > 0);
+    maxnc = std::max(maxnc, d[i].kd.cd.nc);
   }
   VFVM_CUDA(b->desc.alloc(sizeof(NewtonData<Ph, KT>) * b->ninst));
   VFVM_CUDA(cudaMemcpy(b->desc.p, d.data(), sizeof(NewtonData<Ph, KT>) * b->ninst, cudaMemcpyHostToDevice));
   b->desc_precision = precision;
+  b->desc_coarse = coarse;
+  b->desc_coarse_nc = maxnc;
   return VFVM_OK;
 }
 
@@ -194,7 +206,9 @@ int batch_run_t(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, d
                 const double* guess, const double* fallback, float* ms) {
   const bool f64 = ctl->precision == VFVM_PRECISION_FP64;
   const bool jac = ctl->precon == VFVM_PRECON_JACOBI;
-  int rc = f64 ? batch_prepare<Ph, double>(b, ctl->precision) : batch_prepare<Ph, float>(b, ctl->precision);
+  const int coarse = ctl->precon == VFVM_PRECON_JACOBI ? 0 : ctl->coarse;
+  int rc = f64 ? batch_prepare<Ph, double>(b, ctl->precision, coarse)
+               : batch_prepare<Ph, float>(b, ctl->precision, coarse);
   if (rc) return rc;
   (void)jac;
   switch (ctl->precon) {

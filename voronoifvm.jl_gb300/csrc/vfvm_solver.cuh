@@ -34,11 +34,12 @@ struct DevState {
 };
 
 struct GraphKey {
-  int precision, precon, kind;
+  int precision, precon, kind, coarse;
   bool operator<(const GraphKey& o) const {
     if (precision != o.precision) return precision < o.precision;
     if (precon != o.precon) return precon < o.precon;
-    return kind < o.kind;
+    if (kind != o.kind) return kind < o.kind;
+    return coarse < o.coarse;
   }
 };
 

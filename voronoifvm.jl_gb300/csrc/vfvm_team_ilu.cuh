@@ -210,7 +210,9 @@ __device__ bool team_bicgstab_ilu(Team& team, const KrylovData<NS, KT>& d, const
   const int64_t n = (int64_t)d.N * NS;
   iters = 0;
   if (!team_ilu_factor<Team, NS, KT>(team, d, il, nvals)) return false;
+  if (d.cd.nc && !team_coarse_setup<Team, NS, KT>(team, d.cd, d.col, d.A)) return false;
   if (!team_ilu_apply<Team, NS, KT>(team, d, il, d.b, d.r)) return false;  // r = M^-1 b
+  if (d.cd.nc && !team_coarse_add<Team, NS, KT>(team, d.cd, d.b, d.r, n)) return false;
   double acc1[1] = {0.0};
   for (int64_t q = team.rank(); q < n; q += team.size()) {
     const KT rq = d.r[q];
@@ -231,6 +233,7 @@ __device__ bool team_bicgstab_ilu(Team& team, const KrylovData<NS, KT>& d, const
     team_spmv<Team, NS, LPR, KT>(team, d, d.p, il.y);
     if (!team.sync()) return false;
     if (!team_ilu_apply<Team, NS, KT>(team, d, il, il.y, d.v)) return false;
+    if (d.cd.nc && !team_coarse_add<Team, NS, KT>(team, d.cd, il.y, d.v, n)) return false;
     double acc[2] = {0.0, 0.0}, red[2];
     team_dots<Team, KT>(team, n, d.r0, d.v, acc);
     if (!team.template reduce<2>(acc, 0u, red)) return false;
@@ -241,6 +244,7 @@ __device__ bool team_bicgstab_ilu(Team& team, const KrylovData<NS, KT>& d, const
     team_spmv<Team, NS, LPR, KT>(team, d, d.s, il.y);
     if (!team.sync()) return false;
     if (!team_ilu_apply<Team, NS, KT>(team, d, il, il.y, d.t)) return false;
+    if (d.cd.nc && !team_coarse_add<Team, NS, KT>(team, d.cd, il.y, d.t, n)) return false;
     acc[0] = acc[1] = 0.0;
     team_dots<Team, KT>(team, n, d.s, d.t, acc);
     if (!team.template reduce<2>(acc, 0u, red)) return false;
@@ -483,7 +487,9 @@ __device__ bool team_bicgstab_bilu(Team& team, const KrylovData<NS, KT>& d, cons
   __syncthreads();
   const int64_t q0 = (int64_t)sd.K0 * NS, q1 = (int64_t)sd.K1 * NS;
   bilu_factor<NS, KT>(sd, d, il);
+  if (d.cd.nc && !team_coarse_setup<Team, NS, KT>(team, d.cd, d.col, d.A)) return false;
   bilu_apply<NS, KT>(sd, d, il, d.b, d.r);  // r = M^-1 b (subdomain-local)
+  if (d.cd.nc && !team_coarse_add_range<Team, NS, KT>(team, d.cd, d.b, d.r, q0, q1)) return false;
   double acc1[1] = {0.0};
   for (int64_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
     const KT rq = d.r[q];
@@ -504,6 +510,7 @@ __device__ bool team_bicgstab_bilu(Team& team, const KrylovData<NS, KT>& d, cons
     cta_spmv<NS, LPR, KT>(sd, d, d.p, il.y);
     __syncthreads();
     bilu_apply<NS, KT>(sd, d, il, il.y, d.v);
+    if (d.cd.nc && !team_coarse_add_range<Team, NS, KT>(team, d.cd, il.y, d.v, q0, q1)) return false;
     double acc[2] = {0.0, 0.0}, red[2];
     for (int64_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) acc[0] += double(d.r0[q]) * double(d.v[q]);
     if (!team.template reduce<2>(acc, 0u, red)) return false;
@@ -514,6 +521,7 @@ __device__ bool team_bicgstab_bilu(Team& team, const KrylovData<NS, KT>& d, cons
     cta_spmv<NS, LPR, KT>(sd, d, d.s, il.y);
     __syncthreads();
     bilu_apply<NS, KT>(sd, d, il, il.y, d.t);
+    if (d.cd.nc && !team_coarse_add_range<Team, NS, KT>(team, d.cd, il.y, d.t, q0, q1)) return false;
     acc[0] = acc[1] = 0.0;
     for (int64_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
       const double tt = double(d.t[q]);

@@ -34,7 +34,7 @@ from .batch import BatchSolver
 from .grid import simplexgrid
 from .system import NewtonSolverHistory, Physics, SolverControl, System, _raise
 
-__all__ = ["grf_logkappa", "kappa_instance", "Network", "KappaSweep", "LearnedInitialIterate"]
+__all__ = ["grf_logkappa", "kappa_instance", "kappa_scale", "Network", "KappaSweep", "LearnedInitialIterate"]
 
 
 def grf_logkappa(n: int, seed: int, ell: float = 0.1, sigma: float = 1.0, modes: int = 20,
@@ -61,6 +61,15 @@ def grf_logkappa(n: int, seed: int, ell: float = 0.1, sigma: float = 1.0, modes:
     # G[ix, iy] = sum_m amp (a cos(kx x + ky y) + b sin(kx x + ky y))
     G = C @ A @ C.T - Sn @ A @ Sn.T + Sn @ B @ C.T + C @ B @ Sn.T
     return np.ascontiguousarray(G.T).ravel()
+
+
+def kappa_scale(f) -> np.ndarray:
+    """Per-instance output factor of the kappa_exp surrogate: f - 1.  Linearised
+    at u = 0 the problem reads -div(kappa grad u) + u = f - 1, so u / (f - 1) is
+    nearly independent of f and the network learns that ratio (kept away from
+    0 by 1e-3 for f close to 1)."""
+    s = np.asarray(f, dtype=np.float64) - 1.0
+    return np.where(np.abs(s) < 1e-3, np.copysign(1e-3, s), s)
 
 
 def kappa_instance(n: int, seed: int, ell: float = 0.1, sigma: float = 1.0):
@@ -210,12 +219,18 @@ class LearnedInitialIterate:
     def features(self, logk: np.ndarray, f: np.ndarray) -> np.ndarray:
         return np.concatenate([self.coarse(logk), np.asarray(f).reshape(-1, 1)], axis=1).astype(np.float32)
 
-    def fit(self, X: np.ndarray, Ufine: np.ndarray, epochs: int = 200, batch: int = 256, lr: float = 1e-3,
+    def fit(self, X: np.ndarray, U: np.ndarray, scale=None, epochs: int = 200, batch: int = 256, lr: float = 1e-3,
             lr_final: float = 1e-5, seed: int = 0, log_every: int = 0):
-        """Train on features X (S, nin) and fine solutions (S, n*n); Adam with a
-        cosine learning-rate decay.  Returns the per-epoch training losses."""
+        """Train on features X (S, nin) and solutions U: fine (S, n*n) or already
+        restricted to the coarse subgrid (S, nc*nc).  With `scale` (S,), the
+        network learns U / scale (see kappa_scale) and predict_device multiplies
+        back.  Adam with a cosine learning-rate decay.  Returns the per-epoch
+        training losses."""
         import torch
-        T = self.coarse(Ufine)
+        U = np.asarray(U)
+        T = U if U.shape[1] == self.nc * self.nc else self.coarse(U)
+        if scale is not None:
+            T = T / np.asarray(scale, dtype=np.float64)[:, None]
         self.mean, self.std = float(T.mean()), float(T.std() + 1e-30)
         dev = torch.device("cuda")
         Xd = torch.from_numpy(np.ascontiguousarray(X, dtype=np.float32)).to(dev)
@@ -244,15 +259,22 @@ class LearnedInitialIterate:
         """Standardised coarse solution prediction (CUDA float32, S x nc*nc)."""
         return self.net.forward(Xd)
 
-    def predict_device(self, Xd, out=None):
-        """Fine initial values (CUDA float64, S x n*n) for features Xd on the device."""
+    def predict_device(self, Xd, scale=None, out=None):
+        """Fine initial values (CUDA float64, S x n*n) for features Xd on the
+        device; `scale`: the per-instance factors used in fit (CUDA float64
+        tensor of S values), or None."""
         import torch
         Yc = self.predict_coarse(Xd).contiguous()
         S = Yc.shape[0]
         if out is None:
             out = torch.empty((S, self.n * self.n), dtype=torch.float64, device=Xd.device)
+        sp = None
+        if scale is not None:
+            if not (scale.is_cuda and scale.dtype == torch.float64 and scale.numel() == S and scale.is_contiguous()):
+                raise ValueError("scale must be a contiguous CUDA float64 tensor with one value per instance")
+            sp = scale.data_ptr()
         _raise(L.load().vfvm_prolong_bilinear(S, self.nc, self.r, Yc.data_ptr(), self.nc * self.nc, self.std,
-                                              self.mean, out.data_ptr(), self.n * self.n, None),
+                                              self.mean, sp, out.data_ptr(), self.n * self.n, None),
                "vfvm_prolong_bilinear")
         return out
 

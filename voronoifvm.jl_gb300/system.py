@@ -138,6 +138,9 @@ class SolverControl:
     engine: str = "auto"
     # batched solves: CTAs per system (0: library default)
     team_ctas: int = 0
+    # coarse-grid correction stage of the preconditioner: about this many coarse
+    # unknowns (aggregates of nodes x species, at most 208); 0 = one-level only
+    coarse: int = 0
 
     def to_c(self, is_linear: bool = False) -> L.Control_t:
         c = L.Control_t()
@@ -161,6 +164,7 @@ class SolverControl:
         c.store_all = int(bool(self.store_all))
         c.engine = L.ENGINE[self.engine]
         c.team_ctas = int(self.team_ctas)
+        c.coarse = int(self.coarse)
         return c
 
 
