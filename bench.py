@@ -638,6 +638,31 @@ def run_reference_learned(args, rank, world):
     return line
 
 
+def run_batch_only(args):
+    """Profiling mode: `--batch-n` kappa-exp instances on the 257 x 257 grid,
+    batched mixed-precision solves with the coarse stage from inival 0,
+    `--warmup` + `--steps` launches, nothing else."""
+    import torch
+    import __graft_entry__ as ge
+    vfvm = ge.load_package()
+    lk = vfvm.learned
+    n = args.batch_n
+    logk, f = kappa_instances(lk, LN, np.arange(EVAL_SEED0, EVAL_SEED0 + n))
+    sweep = lk.KappaSweep(LN, n)
+    sweep.load(logk, f)
+    z = torch.zeros(n * sweep.nnodes, dtype=torch.float64, device="cuda")
+    U = torch.empty_like(z)
+    ctl = learned_control(vfvm, "batched_mixed")
+    ctl.team_ctas = 8
+    ms = []
+    for _ in range(args.warmup + args.steps):
+        hist, _ = sweep.solve_device(z.data_ptr(), U.data_ptr(), ctl)
+        ms.append(hist[0].time * 1e3)
+    print(json.dumps({"mode": "batch", "instances": n, "launches": args.warmup + args.steps, "ms": ms,
+                      "graphed": sweep.solver.graphed, "newton": float(np.mean([h.nnewton for h in hist])),
+                      "krylov": float(np.mean([h.nlin for h in hist]))}))
+
+
 def run_assembly_only(args):
     """Profiling mode: build the workload and launch the assembly kernel
     `--steps` times (FP32-Jacobian form), nothing else."""
@@ -662,7 +687,8 @@ def run_assembly_only(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--mode", choices=["bench", "assembly"], default="bench")
+    ap.add_argument("--mode", choices=["bench", "assembly", "batch"], default="bench")
+    ap.add_argument("--batch-n", type=int, default=16)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -684,6 +710,9 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.mode == "assembly":
         run_assembly_only(args)
+        return
+    if args.mode == "batch":
+        run_batch_only(args)
         return
     if args.impl == "reference":
         if world > 1 and rank != 0:

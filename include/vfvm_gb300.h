@@ -217,6 +217,10 @@ int vfvm_batch_offsets(vfvm_batch* batch, int64_t* offsets);
  * one set of device grid tables. */
 int vfvm_batch_set_instance(vfvm_batch* batch, int32_t inst, const double* params, int32_t nparams,
                             const double* nodedata, int32_t nnodedata);
+/* out[0] = systems, out[1] = packed unknowns, out[2] = CTAs per system chosen
+ * by vfvm_batch_tune (0: not tuned), out[3] = 1 if the last solve ran as a
+ * captured CUDA graph (scheduler resets + the persistent cooperative launch) */
+int vfvm_batch_info(vfvm_batch* batch, int64_t out[4]);
 /* One stationary solve (tstep = INFINITY) or implicit Euler step of every
  * system from inival; hist (optional) receives one record per system. */
 int vfvm_batch_solve(vfvm_batch* batch, const vfvm_control* control, const double* inival, double* U, double time,

@@ -23,6 +23,7 @@ def test_example440_as_one_batch(vfvm):
     batch = vfvm.BatchSolver(systems)
     control = vfvm.SolverControl(abstol=1e-15, reltol=1e-20, reltol_linear=1e-12, maxiters_linear=1000)
     sols = batch.solve([np.full(321, 0.1)] * 100, control=control)
+    assert batch.graphed  # one captured graph: scheduler resets + the persistent launch
     total = sum(float(vfvm.integrate(s, u)[0]) for s, u in zip(systems, sols))
     assert total == pytest.approx(testval, rel=RTOL)
 

@@ -49,6 +49,13 @@ class BatchSolver:
         self.best_ctas: Optional[int] = None
 
     @property
+    def graphed(self) -> bool:
+        """True if the last solve ran as a captured CUDA graph."""
+        out = np.zeros(4, dtype=np.int64)
+        _raise(L.load().vfvm_batch_info(self.h, L.ptr(out, L.c_i64)), "vfvm_batch_info")
+        return bool(out[3])
+
+    @property
     def ninst(self) -> int:
         return len(self.systems)
 

@@ -89,6 +89,15 @@ extern "C" int vfvm_batch_set_instance(vfvm_batch* b, int32_t inst, const double
   return VFVM_OK;
 }
 
+extern "C" int vfvm_batch_info(vfvm_batch* b, int64_t out[4]) {
+  if (!b || !out) return VFVM_ERR_INPUT;
+  out[0] = b->ninst;
+  out[1] = b->offsets[b->ninst];
+  out[2] = b->tuned_ctas;
+  out[3] = b->last_graphed ? 1 : 0;
+  return VFVM_OK;
+}
+
 extern "C" int vfvm_batch_offsets(vfvm_batch* b, int64_t* offsets) {
   if (!b || !offsets) return VFVM_ERR_INPUT;
   std::copy(b->offsets.begin(), b->offsets.end(), offsets);

@@ -25,7 +25,10 @@ struct vfvm_batch {
   cudaStream_t stream = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int tuned_ctas = 0;
+  cudaGraphExec_t exec = nullptr;  // the captured solve (resets + persistent launch)
+  bool use_graph = true, last_graphed = false;
   ~vfvm_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
     // clones hold views of the first context's grid tables: destroy it last
     for (size_t i = ctx.size(); i-- > 0;) vfvm_destroy(ctx[i]);
     if (e0) cudaEventDestroy(e0);

@@ -152,11 +152,7 @@ int batch_launch(vfvm_batch* b, const vfvm_control* ctl, int ctas_per_system, do
   for (int g = 0; g < ngroups; ++g)
     hs[g] = BatchSync{GridSync{b->bars.p + 8 * (size_t)g, b->partials.p + (size_t)2 * G * 8 * g}, b->slots.p + g};
   if (b->syncs.n < sizeof(BatchSync) * ngroups) VFVM_CUDA(b->syncs.alloc(sizeof(BatchSync) * ngroups));
-  VFVM_CUDA(cudaMemcpyAsync(b->syncs.p, hs.data(), sizeof(BatchSync) * ngroups, cudaMemcpyHostToDevice, b->stream));
-  VFVM_CUDA(cudaMemsetAsync(b->bars.p, 0, 8 * sizeof(unsigned) * ngroups, b->stream));
-  VFVM_CUDA(cudaMemsetAsync(b->queue.p, 0, sizeof(unsigned), b->stream));
-  VFVM_CUDA(cudaMemsetAsync(b->failed.p, 0, sizeof(int), b->stream));
-  VFVM_CUDA(cudaMemsetAsync(b->outs.p, 0, sizeof(NewtonOut) * b->ninst, b->stream));
+  VFVM_CUDA(cudaMemcpy(b->syncs.p, hs.data(), sizeof(BatchSync) * ngroups, cudaMemcpyHostToDevice));
   const NewtonData<Ph, KT>* insts = reinterpret_cast<const NewtonData<Ph, KT>*>(b->desc.p);
   const int* order = b->order.p;
   DevControl dc = make_devcontrol(*ctl);
@@ -170,10 +166,51 @@ int batch_launch(vfvm_batch* b, const vfvm_control* ctl, int ctas_per_system, do
   const double* ubase = b->U.p;
   void* args[] = {&insts, &ninst, &order, &dc, &groups, &gsz, &queue, &time, &tinv, &lambda, &outs, &failed,
                   &guess, &fallback, &ubase};
+  // The solve is one captured graph: scheduler resets + the persistent
+  // cooperative launch.  Each call captures it again and updates the cached
+  // executable graph in place (kernel arguments change between calls).
+  auto enqueue = [&]() -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(b->bars.p, 0, 8 * sizeof(unsigned) * ngroups, b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->queue.p, 0, sizeof(unsigned), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->failed.p, 0, sizeof(int), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->outs.p, 0, sizeof(NewtonOut) * b->ninst, b->stream);
+    if (e == cudaSuccess)
+      e = cudaLaunchCooperativeKernel((void*)kern, dim3(grid), dim3(kPersistThreads), args, smem, b->stream);
+    return e;
+  };
+  bool graphed = false;
+  if (b->use_graph) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      const cudaError_t e1 = enqueue();
+      e = cudaStreamEndCapture(b->stream, &g);
+      if (e1 != cudaSuccess) e = e1;
+    }
+    if (e == cudaSuccess && g) {
+      if (b->exec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(b->exec, g, &info) != cudaSuccess) {
+          cudaGetLastError();
+          cudaGraphExecDestroy(b->exec);
+          b->exec = nullptr;
+        }
+      }
+      if (!b->exec && cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) b->exec = nullptr;
+      graphed = b->exec != nullptr;
+    }
+    if (g) cudaGraphDestroy(g);
+    if (!graphed) {  // capture of the cooperative launch refused: launch directly from now on
+      cudaGetLastError();
+      b->use_graph = false;
+    }
+  }
   VFVM_CUDA(cudaEventRecord(b->e0, b->stream));
-  VFVM_CUDA(cudaLaunchCooperativeKernel((void*)kern, dim3(grid), dim3(kPersistThreads), args, smem, b->stream));
+  if (graphed) VFVM_CUDA(cudaGraphLaunch(b->exec, b->stream));
+  else VFVM_CUDA(enqueue());
   VFVM_CUDA(cudaEventRecord(b->e1, b->stream));
   VFVM_CUDA(cudaStreamSynchronize(b->stream));
+  b->last_graphed = graphed;
   if (ms) VFVM_CUDA(cudaEventElapsedTime(ms, b->e0, b->e1));
   int hfailed = 0;
   VFVM_CUDA(cudaMemcpy(&hfailed, failed, sizeof(int), cudaMemcpyDeviceToHost));
