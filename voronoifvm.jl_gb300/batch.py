@@ -48,12 +48,20 @@ class BatchSolver:
         self.history: List[NewtonSolverHistory] = []
         self.best_ctas: Optional[int] = None
 
+    def _info(self):
+        out = np.zeros(6, dtype=np.int64)
+        _raise(L.load().vfvm_batch_info(self.h, L.ptr(out, L.c_i64)), "vfvm_batch_info")
+        return out
+
     @property
     def graphed(self) -> bool:
         """True if the last solve ran as a captured CUDA graph."""
-        out = np.zeros(4, dtype=np.int64)
-        _raise(L.load().vfvm_batch_info(self.h, L.ptr(out, L.c_i64)), "vfvm_batch_info")
-        return bool(out[3])
+        return bool(self._info()[3])
+
+    @property
+    def engine(self) -> str:
+        """Engine of the last solve: "persistent" (CTA teams) or "sweep" (whole-GPU kernels)."""
+        return "sweep" if self._info()[4] == 1 else "persistent"
 
     @property
     def ninst(self) -> int:

@@ -506,6 +506,49 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
     }
     SETUP_CUDA(c->lower_ptr.upload(lptr));
     SETUP_CUDA(c->lower_slots.upload(lslots));
+    // ELL copies for the Krylov solve (fixed width, entry w of row r at w*N + r,
+    // padding -1): the matrix by node, and the ILU0 lower/upper couplings by
+    // position in colour order.  One thread per row then issues all of a row's
+    // loads at once instead of walking pointer chains.
+    int W = 0, LW = 0, UW = 0;
+    for (int k = 0; k < N; ++k) {
+      W = std::max(W, c->h_browptr[k + 1] - c->h_browptr[k]);
+      LW = std::max(LW, lptr[k + 1] - lptr[k]);
+    }
+    std::vector<int> upcount(N, 0);
+    for (int k = 0; k < N; ++k)
+      for (int s = c->h_browptr[k]; s < c->h_browptr[k + 1]; ++s)
+        if (color[c->h_bcol[s]] > color[k]) ++upcount[k];
+    for (int k = 0; k < N; ++k) UW = std::max(UW, upcount[k]);
+    c->ell_w = W; c->lo_w = LW; c->up_w = UW;
+    std::vector<int> ecol((size_t)W * N, -1), eslot((size_t)W * N, -1);
+    for (int k = 0; k < N; ++k)
+      for (int s = c->h_browptr[k], w = 0; s < c->h_browptr[k + 1]; ++s, ++w) {
+        ecol[(size_t)w * N + k] = c->h_bcol[s];
+        eslot[(size_t)w * N + k] = s;
+      }
+    std::vector<int> lnode((size_t)std::max(LW, 1) * N, -1), lslot((size_t)std::max(LW, 1) * N, -1);
+    std::vector<int> unode((size_t)std::max(UW, 1) * N, -1), uslot((size_t)std::max(UW, 1) * N, -1);
+    for (int pos = 0; pos < N; ++pos) {
+      const int k = cn[pos];
+      for (int q = lptr[k], w = 0; q < lptr[k + 1]; ++q, ++w) {
+        lslot[(size_t)w * N + pos] = lslots[q];
+        lnode[(size_t)w * N + pos] = c->h_bcol[lslots[q]];
+      }
+      int w = 0;
+      for (int s = c->h_browptr[k]; s < c->h_browptr[k + 1]; ++s)
+        if (color[c->h_bcol[s]] > color[k]) {
+          uslot[(size_t)w * N + pos] = s;
+          unode[(size_t)w * N + pos] = c->h_bcol[s];
+          ++w;
+        }
+    }
+    SETUP_CUDA(c->ell_col.upload(ecol));
+    SETUP_CUDA(c->ell_slot.upload(eslot));
+    SETUP_CUDA(c->lo_node.upload(lnode));
+    SETUP_CUDA(c->lo_slot.upload(lslot));
+    SETUP_CUDA(c->up_node.upload(unode));
+    SETUP_CUDA(c->up_slot.upload(uslot));
   }
 
   // --- upload

@@ -102,6 +102,11 @@ struct vfvm_ctx {
   vfvm::DBuf<int> color_nodes;              // nodes sorted by (colour, index)
   vfvm::DBuf<int> color_ptr;                // device copy of h_color_ptr
   vfvm::DBuf<int> lower_ptr, lower_slots;   // per node: lower-colour slots in factorization order
+  // ELL (fixed-width, column-major, -1 padded) copies for the Krylov solve:
+  // matrix rows by node (ell_*: node index, block slot), ILU0 lower/upper
+  // couplings by position in colour order (lo_*/up_*: neighbour node, block slot)
+  int ell_w = 0, lo_w = 0, up_w = 0;
+  vfvm::DBuf<int> ell_col, ell_slot, lo_node, lo_slot, up_node, up_slot;
 
   // assembly buffers
   vfvm::DBuf<double> U, Uold, F, J;         // J: nnzb*ns*ns

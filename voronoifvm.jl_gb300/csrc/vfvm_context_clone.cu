@@ -40,6 +40,9 @@ vfvm_ctx* clone_context(const vfvm_ctx* b, const vfvm_physics_desc* ph, int* sta
   c->dirichlet_dof.view(b->dirichlet_dof); c->pmap.view(b->pmap);
   c->color_nodes.view(b->color_nodes); c->color_ptr.view(b->color_ptr);
   c->lower_ptr.view(b->lower_ptr); c->lower_slots.view(b->lower_slots);
+  c->ell_w = b->ell_w; c->lo_w = b->lo_w; c->up_w = b->up_w;
+  c->ell_col.view(b->ell_col); c->ell_slot.view(b->ell_slot); c->lo_node.view(b->lo_node);
+  c->lo_slot.view(b->lo_slot); c->up_node.view(b->up_node); c->up_slot.view(b->up_slot);
   // own physics data; the legacy boundary data must match the base's structure
   c->h_params.assign(ph->params, ph->params + ph->nparams);
   c->nparams = ph->nparams;

@@ -639,15 +639,21 @@ void destroy_workspace(Workspace* w) {
 }
 
 template <typename KT>
-static cudaError_t alloc_kvecs(KVecs<KT>& k, size_t n, size_t nblk, int ns) {
+static cudaError_t alloc_kvecs(KVecs<KT>& k, const vfvm_ctx* c) {
   cudaError_t e;
+  const size_t n = (size_t)c->N * c->ns, nblk = (size_t)c->nnzb, b2 = (size_t)c->ns * c->ns;
   DBuf<KT>* v[] = {&k.b, &k.x, &k.r, &k.r0, &k.p, &k.ph, &k.v, &k.s, &k.sh, &k.t};
   for (auto* b : v) {
     if (b->n == n) continue;
     if ((e = b->alloc(n)) != cudaSuccess) return e;
     if ((e = cudaMemset(b->p, 0, n * sizeof(KT))) != cudaSuccess) return e;
   }
-  if (k.ilu.n != nblk * ns * ns && (e = k.ilu.alloc(nblk * ns * ns)) != cudaSuccess) return e;
+  if (k.ilu.n != nblk * b2 && (e = k.ilu.alloc(nblk * b2)) != cudaSuccess) return e;
+  const size_t ne = (size_t)c->ell_w * c->N * b2, nl = (size_t)std::max(c->lo_w, 1) * c->N * b2,
+               nu = (size_t)std::max(c->up_w, 1) * c->N * b2;
+  if (k.ell_val.n != ne && (e = k.ell_val.alloc(ne)) != cudaSuccess) return e;
+  if (k.lo_val.n != nl && (e = k.lo_val.alloc(nl)) != cudaSuccess) return e;
+  if (k.up_val.n != nu && (e = k.up_val.alloc(nu)) != cudaSuccess) return e;
   return cudaSuccess;
 }
 
@@ -677,10 +683,10 @@ int ensure_workspace(vfvm_ctx* c, int precision) {
   Workspace* w = c->ws;
   const size_t n = (size_t)c->N * c->ns;
   if (precision == VFVM_PRECISION_FP64) {
-    VFVM_CUDA(alloc_kvecs(w->k64, n, c->nnzb, c->ns));
+    VFVM_CUDA(alloc_kvecs(w->k64, c));
     if (w->k64.dinv.n != (size_t)c->N * c->ns * c->ns) VFVM_CUDA(w->k64.dinv.alloc((size_t)c->N * c->ns * c->ns));
   } else {
-    VFVM_CUDA(alloc_kvecs(w->k32, n, c->nnzb, c->ns));
+    VFVM_CUDA(alloc_kvecs(w->k32, c));
     if (w->k32.dinv.n != (size_t)c->N * c->ns * c->ns) VFVM_CUDA(w->k32.dinv.alloc((size_t)c->N * c->ns * c->ns));
     if (c->Jf.n != (size_t)c->nnzb * c->ns * c->ns) VFVM_CUDA(c->Jf.alloc((size_t)c->nnzb * c->ns * c->ns));
   }

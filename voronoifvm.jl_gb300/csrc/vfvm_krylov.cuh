@@ -19,6 +19,11 @@ struct KrylovData {
   KT* x;                    // N * NS (output; initial guess 0)
   KT *r, *r0, *p, *v, *s, *t;
   CoarseData cd;            // coarse-grid correction stage (cd.nc == 0: none)
+  // ELL copy of the matrix (entry w of row K at w*N + K; column -1 = padding)
+  int ew;
+  const int* ell_col;
+  const int* ell_slot;      // block slot of each ELL entry
+  KT* ell_val;              // packed from A after each assembly
 };
 
 struct KrylovCtl {

@@ -45,6 +45,7 @@ extern "C" vfvm_batch* vfvm_batch_create(int32_t ninst, const vfvm_grid* grids, 
              grids[i].bfacenodes == grids[0].bfacenodes && grids[i].bfaceregions == grids[0].bfaceregions;
   for (int i = 0; i < ninst; ++i) {
     int st = 0;
+    b->shared_grid = shared;
     vfvm_ctx* c = (shared && i > 0) ? clone_context(b->ctx[0], &phys[i], &st) : vfvm_create(&grids[i], &phys[i], &st);
     if (!c || c->multireg) {
       if (c) vfvm_destroy(c);
@@ -86,15 +87,18 @@ extern "C" int vfvm_batch_set_instance(vfvm_batch* b, int32_t inst, const double
   if (params && (rc = vfvm_set_params(c, params, nparams))) return rc;
   if (nodedata && (rc = set_nodedata(c, nodedata, nnodedata))) return rc;
   b->desc_precision = -1;  // descriptors are rebuilt before the next solve
+  if (b->sweep) b->sweep->valid = false;
   return VFVM_OK;
 }
 
-extern "C" int vfvm_batch_info(vfvm_batch* b, int64_t out[4]) {
+extern "C" int vfvm_batch_info(vfvm_batch* b, int64_t out[6]) {
   if (!b || !out) return VFVM_ERR_INPUT;
   out[0] = b->ninst;
   out[1] = b->offsets[b->ninst];
   out[2] = b->tuned_ctas;
   out[3] = b->last_graphed ? 1 : 0;
+  out[4] = b->last_engine;
+  out[5] = b->shared_grid ? 1 : 0;
   return VFVM_OK;
 }
 

@@ -6,6 +6,22 @@
 #include <vector>
 #include "vfvm_solver.cuh"
 
+namespace vfvm {
+// device memory and the captured graph of the sweep engine (vfvm_sweep.cuh)
+struct SweepHost {
+  int precision = -1, coarse = -1;
+  bool valid = false;                 // false after vfvm_batch_set_instance: parameters are re-gathered
+  DBuf<char> F, J, ilu, dinv, ell, lo, up, vecs, params, nodedata, cA, crc, czc, st, partials, tickets, call, klist;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<char> args;             // the kernel arguments the graph was built with
+  ~SweepHost() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+};
+}  // namespace vfvm
+
 struct vfvm_batch {
   // systems of one physics, packed unknowns, instance descriptors, scheduling state
   int ninst = 0, phys = 0, ns = 1;
@@ -27,7 +43,11 @@ struct vfvm_batch {
   int tuned_ctas = 0;
   cudaGraphExec_t exec = nullptr;  // the captured solve (resets + persistent launch)
   bool use_graph = true, last_graphed = false;
+  bool shared_grid = false;          // all systems are clones of ctx[0] (one grid)
+  vfvm::SweepHost* sweep = nullptr;  // sweep engine state (shared-grid batches)
+  int last_engine = 0;               // 0 persistent teams, 1 sweep
   ~vfvm_batch() {
+    delete sweep;
     if (exec) cudaGraphExecDestroy(exec);
     // clones hold views of the first context's grid tables: destroy it last
     for (size_t i = ctx.size(); i-- > 0;) vfvm_destroy(ctx[i]);

@@ -46,6 +46,7 @@ struct GraphKey {
 template <typename KT>
 struct KVecs {
   DBuf<KT> b, x, r, r0, p, ph, v, s, sh, t, dinv, ilu;
+  DBuf<KT> ell_val, lo_val, up_val;  // ELL values (matrix, ILU0 L and U couplings), packed per Newton step
 };
 
 struct Workspace {

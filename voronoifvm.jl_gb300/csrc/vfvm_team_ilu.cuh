@@ -22,7 +22,210 @@ struct IluData {
   const int* lower_slots;
   KT* ilu;                 // nnzb * NS * NS factor values
   KT* y;                   // temporary vector (N * NS)
+  // ELL copies of the factor's couplings by colour position (entry w of
+  // position p at w*N + p; node -1 = padding): lower (elimination) and upper
+  int lw, uw;
+  const int* lo_node;
+  const int* lo_slot;
+  const int* up_node;
+  const int* up_slot;
+  KT* lo_val;
+  KT* up_val;
 };
+
+// ---------------------------------------------------------------------------
+// ELL kernels of the Krylov solve.  One thread per row: the row's index and
+// value loads are independent of each other (fixed width, column-major), so a
+// thread has all of them in flight at once; the vector gathers follow.
+// ---------------------------------------------------------------------------
+
+// ell_val <- A (rows [r0, r1), thread tid of nt)
+template <int NS, typename KT>
+__device__ __forceinline__ void pack_ell_rows(const KrylovData<NS, KT>& d, int r0, int r1, int tid, int nt) {
+  constexpr int B = NS * NS;
+  for (int w = 0; w < d.ew; ++w)
+    for (int K = r0 + tid; K < r1; K += nt) {
+      const int64_t e = (int64_t)w * d.N + K;
+      const int s = d.ell_slot[e];
+#pragma unroll
+      for (int i = 0; i < B; ++i) d.ell_val[e * B + i] = s >= 0 ? __ldcg(&d.A[(int64_t)s * B + i]) : KT(0);
+    }
+}
+
+// out = A x on rows [r0, r1); two rows per thread and pass
+template <int NS, typename KT>
+__device__ __forceinline__ void spmv_ell_rows(const KrylovData<NS, KT>& d, const KT* __restrict__ x,
+                                              KT* __restrict__ out, int r0, int r1, int tid, int nt) {
+  constexpr int B = NS * NS;
+  constexpr int R = 2;
+  const int N = d.N;
+  const int* __restrict__ col = d.ell_col;
+  const KT* __restrict__ val = d.ell_val;
+  for (int K0 = r0 + tid; K0 < r1; K0 += R * nt) {
+    KT y[R][NS];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+      for (int i = 0; i < NS; ++i) y[r][i] = KT(0);
+#pragma unroll 4
+    for (int w = 0; w < d.ew; ++w) {
+      int m[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int K = K0 + r * nt;
+        m[r] = K < r1 ? col[(int64_t)w * N + K] : -1;
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (m[r] < 0) continue;
+        const KT* Ab = val + ((int64_t)w * N + K0 + r * nt) * B;
+#pragma unroll
+        for (int j = 0; j < NS; ++j) {
+          const KT xm = x[(size_t)m[r] * NS + j];
+#pragma unroll
+          for (int i = 0; i < NS; ++i) y[r][i] += Ab[i * NS + j] * xm;
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int K = K0 + r * nt;
+      if (K < r1) {
+#pragma unroll
+        for (int i = 0; i < NS; ++i) out[(size_t)K * NS + i] = y[r][i];
+      }
+    }
+  }
+}
+
+// lo_val/up_val <- the factor's couplings for colour positions [p0, p1);
+// couplings to nodes outside [K0, K1) become 0 (subdomain ILU0)
+template <int NS, typename KT>
+__device__ __forceinline__ void pack_ilu_positions(const IluData<KT>& il, int N, int p0, int p1, int tid, int nt,
+                                                   int K0, int K1) {
+  constexpr int B = NS * NS;
+  for (int w = 0; w < il.lw; ++w)
+    for (int p = p0 + tid; p < p1; p += nt) {
+      const int64_t e = (int64_t)w * N + p;
+      const int sl = il.lo_slot[e], k = il.lo_node[e];
+      const bool keep = sl >= 0 && k >= K0 && k < K1;
+#pragma unroll
+      for (int i = 0; i < B; ++i) il.lo_val[e * B + i] = keep ? __ldcg(&il.ilu[(int64_t)sl * B + i]) : KT(0);
+    }
+  for (int w = 0; w < il.uw; ++w)
+    for (int p = p0 + tid; p < p1; p += nt) {
+      const int64_t e = (int64_t)w * N + p;
+      const int sl = il.up_slot[e], k = il.up_node[e];
+      const bool keep = sl >= 0 && k >= K0 && k < K1;
+#pragma unroll
+      for (int i = 0; i < B; ++i) il.up_val[e * B + i] = keep ? __ldcg(&il.ilu[(int64_t)sl * B + i]) : KT(0);
+    }
+}
+
+// forward sweep of one colour: z_K = y_K - sum L_Kk z_k over positions [p0, p1);
+// two positions per thread and pass
+template <int NS, typename KT>
+__device__ __forceinline__ void ilu_fwd_positions(const IluData<KT>& il, int N, const KT* __restrict__ y,
+                                                  KT* __restrict__ z, int p0, int p1, int tid, int nt) {
+  constexpr int B = NS * NS;
+  constexpr int R = 2;
+  const int* __restrict__ lnode = il.lo_node;
+  const KT* __restrict__ lval = il.lo_val;
+  for (int pb = p0 + tid; pb < p1; pb += R * nt) {
+    int K[R];
+    KT w[R][NS];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int p = pb + r * nt;
+      K[r] = p < p1 ? il.color_nodes[p] : -1;
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+      for (int i = 0; i < NS; ++i) w[r][i] = K[r] >= 0 ? y[(size_t)K[r] * NS + i] : KT(0);
+#pragma unroll 4
+    for (int l = 0; l < il.lw; ++l) {
+      int k[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int p = pb + r * nt;
+        k[r] = p < p1 ? lnode[(int64_t)l * N + p] : -1;
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (k[r] < 0) continue;
+        const KT* Lb = lval + ((int64_t)l * N + pb + r * nt) * B;
+#pragma unroll
+        for (int j = 0; j < NS; ++j) {
+          const KT zk = z[(size_t)k[r] * NS + j];
+#pragma unroll
+          for (int i = 0; i < NS; ++i) w[r][i] -= Lb[i * NS + j] * zk;
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+      if (K[r] >= 0) {
+#pragma unroll
+        for (int i = 0; i < NS; ++i) z[(size_t)K[r] * NS + i] = w[r][i];
+      }
+  }
+}
+
+// backward sweep of one colour: z_K = D_K^-1 (z_K - sum U_Kj z_j); two positions per pass
+template <int NS, typename KT>
+__device__ __forceinline__ void ilu_bwd_positions(const IluData<KT>& il, const KT* __restrict__ dinv, int N,
+                                                  KT* __restrict__ z, int p0, int p1, int tid, int nt) {
+  constexpr int B = NS * NS;
+  constexpr int R = 2;
+  const int* __restrict__ unode = il.up_node;
+  const KT* __restrict__ uval = il.up_val;
+  for (int pb = p0 + tid; pb < p1; pb += R * nt) {
+    int K[R];
+    KT w[R][NS];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int p = pb + r * nt;
+      K[r] = p < p1 ? il.color_nodes[p] : -1;
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+      for (int i = 0; i < NS; ++i) w[r][i] = K[r] >= 0 ? z[(size_t)K[r] * NS + i] : KT(0);
+#pragma unroll 4
+    for (int l = 0; l < il.uw; ++l) {
+      int j[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int p = pb + r * nt;
+        j[r] = p < p1 ? unode[(int64_t)l * N + p] : -1;
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (j[r] < 0) continue;
+        const KT* Ub = uval + ((int64_t)l * N + pb + r * nt) * B;
+#pragma unroll
+        for (int jj = 0; jj < NS; ++jj) {
+          const KT zj = z[(size_t)j[r] * NS + jj];
+#pragma unroll
+          for (int i = 0; i < NS; ++i) w[r][i] -= Ub[i * NS + jj] * zj;
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+      if (K[r] >= 0) {
+        const KT* D = dinv + (size_t)K[r] * B;
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+          KT acc = KT(0);
+#pragma unroll
+          for (int jj = 0; jj < NS; ++jj) acc += D[i * NS + jj] * w[r][jj];
+          z[(size_t)K[r] * NS + i] = acc;
+        }
+      }
+  }
+}
 
 __device__ __forceinline__ int slot_of(const int* __restrict__ col, int beg, int end, int c) {
   while (beg < end) {
@@ -154,6 +357,115 @@ __device__ bool team_ilu_apply(Team& team, const KrylovData<NS, KT>& d, const Il
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// BiCGStab vector updates, four elements per thread per pass (q, q+st, q+2st,
+// q+3st: each load instruction stays coalesced across the threads, and a
+// thread issues all loads of a pass before its first store).  Element q is
+// always handled by the same thread (q = start mod st), the ownership that
+// lets the coarse prolongation skip a barrier.
+// ---------------------------------------------------------------------------
+constexpr int kVecU = 4;
+
+// p = r + beta (p - omega v)
+template <typename KT>
+__device__ __forceinline__ void vec_p_update(KT* __restrict__ p, const KT* __restrict__ r, const KT* __restrict__ v,
+                                             KT beta, KT omega, int64_t q0, int64_t q1, int64_t st) {
+  for (int64_t q = q0; q < q1; q += kVecU * st) {
+    KT rr[kVecU], pp[kVecU], vv[kVecU];
+#pragma unroll
+    for (int u = 0; u < kVecU; ++u) {
+      const int64_t e = q + u * st;
+      if (e < q1) { rr[u] = r[e]; pp[u] = p[e]; vv[u] = v[e]; }
+    }
+#pragma unroll
+    for (int u = 0; u < kVecU; ++u) {
+      const int64_t e = q + u * st;
+      if (e < q1) p[e] = rr[u] + beta * (pp[u] - omega * vv[u]);
+    }
+  }
+}
+
+// s = r - alpha v
+template <typename KT>
+__device__ __forceinline__ void vec_s_update(KT* __restrict__ s, const KT* __restrict__ r, const KT* __restrict__ v,
+                                             KT alpha, int64_t q0, int64_t q1, int64_t st) {
+  for (int64_t q = q0; q < q1; q += kVecU * st) {
+    KT rr[kVecU], vv[kVecU];
+#pragma unroll
+    for (int u = 0; u < kVecU; ++u) {
+      const int64_t e = q + u * st;
+      if (e < q1) { rr[u] = r[e]; vv[u] = v[e]; }
+    }
+#pragma unroll
+    for (int u = 0; u < kVecU; ++u) {
+      const int64_t e = q + u * st;
+      if (e < q1) s[e] = rr[u] - alpha * vv[u];
+    }
+  }
+}
+
+// acc[0] += w.z, acc[1] += z.z
+template <typename KT>
+__device__ __forceinline__ void vec_dots(const KT* __restrict__ w, const KT* __restrict__ z, int64_t q0, int64_t q1,
+                                         int64_t st, double (&acc)[2]) {
+  for (int64_t q = q0; q < q1; q += kVecU * st) {
+    KT ww[kVecU], zz[kVecU];
+#pragma unroll
+    for (int u = 0; u < kVecU; ++u) {
+      const int64_t e = q + u * st;
+      ww[u] = e < q1 ? w[e] : KT(0);
+      zz[u] = e < q1 ? z[e] : KT(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kVecU; ++u) {
+      acc[0] += double(ww[u]) * double(zz[u]);
+      acc[1] += double(zz[u]) * double(zz[u]);
+    }
+  }
+}
+
+// x += alpha p + omega s;  r = s - omega t;  acc += (r0.r, r.r)
+template <typename KT>
+__device__ __forceinline__ void vec_xr_update(KT* __restrict__ x, KT* __restrict__ r, const KT* __restrict__ p,
+                                              const KT* __restrict__ s, const KT* __restrict__ t,
+                                              const KT* __restrict__ r0, KT alpha, KT omega, int64_t q0, int64_t q1,
+                                              int64_t st, double (&acc)[2]) {
+  for (int64_t q = q0; q < q1; q += kVecU * st) {
+    KT xx[kVecU], pp[kVecU], ss[kVecU], tt[kVecU], r0r[kVecU];
+#pragma unroll
+    for (int u = 0; u < kVecU; ++u) {
+      const int64_t e = q + u * st;
+      if (e < q1) { xx[u] = x[e]; pp[u] = p[e]; ss[u] = s[e]; tt[u] = t[e]; r0r[u] = r0[e]; }
+    }
+#pragma unroll
+    for (int u = 0; u < kVecU; ++u) {
+      const int64_t e = q + u * st;
+      if (e < q1) {
+        x[e] = xx[u] + alpha * pp[u] + omega * ss[u];
+        const KT rn = ss[u] - omega * tt[u];
+        r[e] = rn;
+        acc[0] += double(r0r[u]) * double(rn);
+        acc[1] += double(rn) * double(rn);
+      }
+    }
+  }
+}
+
+// z = (LU)^-1 y with the ELL couplings; ends with a team barrier
+template <class Team, int NS, typename KT>
+__device__ bool team_ilu_apply_ell(Team& team, const KrylovData<NS, KT>& d, const IluData<KT>& il,
+                                   const KT* __restrict__ y, KT* __restrict__ z) {
+  for (int c = 0; c < il.ncolors; ++c) {
+    ilu_fwd_positions<NS, KT>(il, d.N, y, z, il.color_ptr[c], il.color_ptr[c + 1], team.rank(), team.size());
+    if (!team.sync()) return false;
+  }
+  for (int c = il.ncolors - 1; c >= 0; --c) {
+    ilu_bwd_positions<NS, KT>(il, d.dinv, d.N, z, il.color_ptr[c], il.color_ptr[c + 1], team.rank(), team.size());
+    if (!team.sync()) return false;
+  }
+  return true;
+}
+
 // out = A x (plain), LPR lanes per block row
 template <class Team, int NS, int LPR, typename KT>
 __device__ __forceinline__ void team_spmv(Team& team, const KrylovData<NS, KT>& d, const KT* __restrict__ xin,
@@ -210,8 +522,11 @@ __device__ bool team_bicgstab_ilu(Team& team, const KrylovData<NS, KT>& d, const
   const int64_t n = (int64_t)d.N * NS;
   iters = 0;
   if (!team_ilu_factor<Team, NS, KT>(team, d, il, nvals)) return false;
-  if (d.cd.nc && !team_coarse_setup<Team, NS, KT>(team, d.cd, d.col, d.A)) return false;
-  if (!team_ilu_apply<Team, NS, KT>(team, d, il, d.b, d.r)) return false;  // r = M^-1 b
+  pack_ell_rows<NS, KT>(d, 0, d.N, team.rank(), team.size());
+  pack_ilu_positions<NS, KT>(il, d.N, 0, d.N, team.rank(), team.size(), 0, d.N);
+  if (d.cd.nc && !team_coarse_setup<Team, NS, KT>(team, d.cd, d.col, d.A)) return false;  // (ends with a barrier)
+  if (!d.cd.nc && !team.sync()) return false;
+  if (!team_ilu_apply_ell<Team, NS, KT>(team, d, il, d.b, d.r)) return false;  // r = M^-1 b
   if (d.cd.nc && !team_coarse_add<Team, NS, KT>(team, d.cd, d.b, d.r, n)) return false;
   double acc1[1] = {0.0};
   for (int64_t q = team.rank(); q < n; q += team.size()) {
@@ -227,36 +542,31 @@ __device__ bool team_bicgstab_ilu(Team& team, const KrylovData<NS, KT>& d, const
   double rr = red1[0], alpha = 1.0, omega = 1.0, beta = 0.0;
   if (!(rr > tol2) || c.maxiters <= 0 || isnan(rr)) return true;
   int it = 0, brk = 0;
+  const int64_t q0 = team.rank(), qs = team.size();
   while (true) {
-    for (int64_t q = team.rank(); q < n; q += team.size()) d.p[q] = d.r[q] + KT(beta) * (d.p[q] - KT(omega) * d.v[q]);
+    vec_p_update<KT>(d.p, d.r, d.v, KT(beta), KT(omega), q0, n, qs);
     if (!team.sync()) return false;
-    team_spmv<Team, NS, LPR, KT>(team, d, d.p, il.y);
+    spmv_ell_rows<NS, KT>(d, d.p, il.y, 0, d.N, team.rank(), team.size());
     if (!team.sync()) return false;
-    if (!team_ilu_apply<Team, NS, KT>(team, d, il, il.y, d.v)) return false;
+    if (!team_ilu_apply_ell<Team, NS, KT>(team, d, il, il.y, d.v)) return false;
     if (d.cd.nc && !team_coarse_add<Team, NS, KT>(team, d.cd, il.y, d.v, n)) return false;
     double acc[2] = {0.0, 0.0}, red[2];
-    team_dots<Team, KT>(team, n, d.r0, d.v, acc);
+    vec_dots<KT>(d.r0, d.v, q0, n, qs, acc);
     if (!team.template reduce<2>(acc, 0u, red)) return false;
     if (red[0] == 0.0 || isnan(red[0])) { brk = 1; alpha = 0.0; }
     else alpha = rho / red[0];
-    for (int64_t q = team.rank(); q < n; q += team.size()) d.s[q] = d.r[q] - KT(alpha) * d.v[q];
+    vec_s_update<KT>(d.s, d.r, d.v, KT(alpha), q0, n, qs);
     if (!team.sync()) return false;
-    team_spmv<Team, NS, LPR, KT>(team, d, d.s, il.y);
+    spmv_ell_rows<NS, KT>(d, d.s, il.y, 0, d.N, team.rank(), team.size());
     if (!team.sync()) return false;
-    if (!team_ilu_apply<Team, NS, KT>(team, d, il, il.y, d.t)) return false;
+    if (!team_ilu_apply_ell<Team, NS, KT>(team, d, il, il.y, d.t)) return false;
     if (d.cd.nc && !team_coarse_add<Team, NS, KT>(team, d.cd, il.y, d.t, n)) return false;
     acc[0] = acc[1] = 0.0;
-    team_dots<Team, KT>(team, n, d.s, d.t, acc);
+    vec_dots<KT>(d.s, d.t, q0, n, qs, acc);
     if (!team.template reduce<2>(acc, 0u, red)) return false;
     omega = red[1] > 0.0 ? red[0] / red[1] : 0.0;
     acc[0] = acc[1] = 0.0;
-    for (int64_t q = team.rank(); q < n; q += team.size()) {
-      d.x[q] += KT(alpha) * d.p[q] + KT(omega) * d.s[q];
-      const KT rn = d.s[q] - KT(omega) * d.t[q];
-      d.r[q] = rn;
-      acc[0] += double(d.r0[q]) * double(rn);
-      acc[1] += double(rn) * double(rn);
-    }
+    vec_xr_update<KT>(d.x, d.r, d.p, d.s, d.t, d.r0, KT(alpha), KT(omega), q0, n, qs, acc);
     if (!team.template reduce<2>(acc, 0u, red)) return false;
     ++it;
     rr = red[1];
@@ -426,6 +736,21 @@ __device__ void bilu_apply(const Subdomain& sd, const KrylovData<NS, KT>& d, con
   }
 }
 
+// CTA-local z = (LU)^-1 y on the subdomain's positions with the ELL couplings
+// (couplings that leave the subdomain were packed as 0); ends with __syncthreads
+template <int NS, typename KT>
+__device__ void bilu_apply_ell(const Subdomain& sd, const KrylovData<NS, KT>& d, const IluData<KT>& il,
+                               const KT* __restrict__ y, KT* __restrict__ z) {
+  for (int c = 0; c < il.ncolors; ++c) {
+    ilu_fwd_positions<NS, KT>(il, d.N, y, z, sd.cb[c], sd.ce[c], threadIdx.x, blockDim.x);
+    __syncthreads();
+  }
+  for (int c = il.ncolors - 1; c >= 0; --c) {
+    ilu_bwd_positions<NS, KT>(il, d.dinv, d.N, z, sd.cb[c], sd.ce[c], threadIdx.x, blockDim.x);
+    __syncthreads();
+  }
+}
+
 // y = A x on the subdomain's rows, LPR lanes per block row, CTA threads only
 template <int NS, int LPR, typename KT>
 __device__ __forceinline__ void cta_spmv(const Subdomain& sd, const KrylovData<NS, KT>& d, const KT* __restrict__ xin,
@@ -487,8 +812,12 @@ __device__ bool team_bicgstab_bilu(Team& team, const KrylovData<NS, KT>& d, cons
   __syncthreads();
   const int64_t q0 = (int64_t)sd.K0 * NS, q1 = (int64_t)sd.K1 * NS;
   bilu_factor<NS, KT>(sd, d, il);
+  pack_ell_rows<NS, KT>(d, sd.K0, sd.K1, threadIdx.x, blockDim.x);
+  for (int c = 0; c < il.ncolors && c < kMaxColors; ++c)
+    pack_ilu_positions<NS, KT>(il, d.N, sd.cb[c], sd.ce[c], threadIdx.x, blockDim.x, sd.K0, sd.K1);
+  __syncthreads();
   if (d.cd.nc && !team_coarse_setup<Team, NS, KT>(team, d.cd, d.col, d.A)) return false;
-  bilu_apply<NS, KT>(sd, d, il, d.b, d.r);  // r = M^-1 b (subdomain-local)
+  bilu_apply_ell<NS, KT>(sd, d, il, d.b, d.r);  // r = M^-1 b (subdomain-local)
   if (d.cd.nc && !team_coarse_add_range<Team, NS, KT>(team, d.cd, d.b, d.r, q0, q1)) return false;
   double acc1[1] = {0.0};
   for (int64_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
@@ -505,39 +834,30 @@ __device__ bool team_bicgstab_bilu(Team& team, const KrylovData<NS, KT>& d, cons
   if (!(rr > tol2) || c.maxiters <= 0 || isnan(rr)) return true;
   int it = 0, brk = 0;
   while (true) {
-    for (int64_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) d.p[q] = d.r[q] + KT(beta) * (d.p[q] - KT(omega) * d.v[q]);
+    vec_p_update<KT>(d.p, d.r, d.v, KT(beta), KT(omega), q0 + threadIdx.x, q1, blockDim.x);
     if (!team.sync()) return false;  // SpMV reads neighbouring subdomains' p
-    cta_spmv<NS, LPR, KT>(sd, d, d.p, il.y);
+    spmv_ell_rows<NS, KT>(d, d.p, il.y, sd.K0, sd.K1, threadIdx.x, blockDim.x);
     __syncthreads();
-    bilu_apply<NS, KT>(sd, d, il, il.y, d.v);
+    bilu_apply_ell<NS, KT>(sd, d, il, il.y, d.v);
     if (d.cd.nc && !team_coarse_add_range<Team, NS, KT>(team, d.cd, il.y, d.v, q0, q1)) return false;
     double acc[2] = {0.0, 0.0}, red[2];
-    for (int64_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) acc[0] += double(d.r0[q]) * double(d.v[q]);
+    vec_dots<KT>(d.r0, d.v, q0 + threadIdx.x, q1, blockDim.x, acc);
+    acc[1] = 0.0;
     if (!team.template reduce<2>(acc, 0u, red)) return false;
     if (red[0] == 0.0 || isnan(red[0])) { brk = 1; alpha = 0.0; }
     else alpha = rho / red[0];
-    for (int64_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) d.s[q] = d.r[q] - KT(alpha) * d.v[q];
+    vec_s_update<KT>(d.s, d.r, d.v, KT(alpha), q0 + threadIdx.x, q1, blockDim.x);
     if (!team.sync()) return false;  // SpMV reads neighbouring subdomains' s
-    cta_spmv<NS, LPR, KT>(sd, d, d.s, il.y);
+    spmv_ell_rows<NS, KT>(d, d.s, il.y, sd.K0, sd.K1, threadIdx.x, blockDim.x);
     __syncthreads();
-    bilu_apply<NS, KT>(sd, d, il, il.y, d.t);
+    bilu_apply_ell<NS, KT>(sd, d, il, il.y, d.t);
     if (d.cd.nc && !team_coarse_add_range<Team, NS, KT>(team, d.cd, il.y, d.t, q0, q1)) return false;
     acc[0] = acc[1] = 0.0;
-    for (int64_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
-      const double tt = double(d.t[q]);
-      acc[0] += tt * double(d.s[q]);
-      acc[1] += tt * tt;
-    }
+    vec_dots<KT>(d.s, d.t, q0 + threadIdx.x, q1, blockDim.x, acc);
     if (!team.template reduce<2>(acc, 0u, red)) return false;
     omega = red[1] > 0.0 ? red[0] / red[1] : 0.0;
     acc[0] = acc[1] = 0.0;
-    for (int64_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
-      d.x[q] += KT(alpha) * d.p[q] + KT(omega) * d.s[q];
-      const KT rn = d.s[q] - KT(omega) * d.t[q];
-      d.r[q] = rn;
-      acc[0] += double(d.r0[q]) * double(rn);
-      acc[1] += double(rn) * double(rn);
-    }
+    vec_xr_update<KT>(d.x, d.r, d.p, d.s, d.t, d.r0, KT(alpha), KT(omega), q0 + threadIdx.x, q1, blockDim.x, acc);
     if (!team.template reduce<2>(acc, 0u, red)) return false;
     ++it;
     rr = red[1];
