@@ -490,6 +490,7 @@ def run_learned(args, rank, world):
     forms = {}
     with ClockSampler(dev) as clk:
         ms_l, (hist_l, from_guess) = timed(learned_step, args.steps, args.warmup)
+    launches_per_step = sweep.solver.launches + (len(model.sizes) - 1 + 3)  # solve graph + network + prolongation
     clocks = clk.summary()
     U_learned = U.view(NEVAL, N).cpu().numpy()
     ok_l = [h for h in hist_l if h.status == 0]
@@ -569,7 +570,7 @@ def run_learned(args, rank, world):
                                "instances: assembly, ILU0, coarse stage, BiCGStab)",
                      "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes": B, "ms_per_launch": kernel_ms},
-        "gpu_launches": int(args.steps * (len(model.sizes) - 1 + 3)),
+        "gpu_launches": int(args.steps * launches_per_step),
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu:

@@ -221,10 +221,11 @@ int vfvm_batch_set_instance(vfvm_batch* batch, int32_t inst, const double* param
  * by vfvm_batch_tune (0: not tuned), out[3] = 1 if the last solve ran as a
  * captured CUDA graph, out[4] = engine of the last solve (0: persistent CTA
  * teams, one cooperative launch; 1: sweep engine, whole-GPU kernels over all
- * systems), out[5] = 1 if all systems share one grid.  Shared-grid batches
- * with ILU0 (and no legacy boundary data) use the sweep engine unless
+ * systems), out[5] = 1 if all systems share one grid, out[6] = kernels the
+ * last solve launched (counted from the graph's loop iterations).  Shared-grid
+ * batches with ILU0 (and no legacy boundary data) use the sweep engine unless
  * control->engine is VFVM_ENGINE_PERSISTENT. */
-int vfvm_batch_info(vfvm_batch* batch, int64_t out[6]);
+int vfvm_batch_info(vfvm_batch* batch, int64_t out[7]);
 /* One stationary solve (tstep = INFINITY) or implicit Euler step of every
  * system from inival; hist (optional) receives one record per system. */
 int vfvm_batch_solve(vfvm_batch* batch, const vfvm_control* control, const double* inival, double* U, double time,

@@ -49,7 +49,7 @@ class BatchSolver:
         self.best_ctas: Optional[int] = None
 
     def _info(self):
-        out = np.zeros(6, dtype=np.int64)
+        out = np.zeros(7, dtype=np.int64)
         _raise(L.load().vfvm_batch_info(self.h, L.ptr(out, L.c_i64)), "vfvm_batch_info")
         return out
 
@@ -57,6 +57,11 @@ class BatchSolver:
     def graphed(self) -> bool:
         """True if the last solve ran as a captured CUDA graph."""
         return bool(self._info()[3])
+
+    @property
+    def launches(self) -> int:
+        """Kernels launched by the last solve."""
+        return int(self._info()[6])
 
     @property
     def engine(self) -> str:

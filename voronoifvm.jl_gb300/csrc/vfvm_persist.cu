@@ -91,7 +91,7 @@ extern "C" int vfvm_batch_set_instance(vfvm_batch* b, int32_t inst, const double
   return VFVM_OK;
 }
 
-extern "C" int vfvm_batch_info(vfvm_batch* b, int64_t out[6]) {
+extern "C" int vfvm_batch_info(vfvm_batch* b, int64_t out[7]) {
   if (!b || !out) return VFVM_ERR_INPUT;
   out[0] = b->ninst;
   out[1] = b->offsets[b->ninst];
@@ -99,6 +99,7 @@ extern "C" int vfvm_batch_info(vfvm_batch* b, int64_t out[6]) {
   out[3] = b->last_graphed ? 1 : 0;
   out[4] = b->last_engine;
   out[5] = b->shared_grid ? 1 : 0;
+  out[6] = b->last_launches;
   return VFVM_OK;
 }
 

@@ -11,7 +11,8 @@ namespace vfvm {
 struct SweepHost {
   int precision = -1, coarse = -1;
   bool valid = false;                 // false after vfvm_batch_set_instance: parameters are re-gathered
-  DBuf<char> F, J, ilu, dinv, ell, lo, up, vecs, params, nodedata, cA, crc, czc, st, partials, tickets, call, klist;
+  DBuf<char> F, J, ilu, dinv, ell, lo, up, vecs, params, nodedata, cA, crc, czc, st, partials, tickets, call, klist,
+      runs;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<char> args;             // the kernel arguments the graph was built with
@@ -46,6 +47,7 @@ struct vfvm_batch {
   bool shared_grid = false;          // all systems are clones of ctx[0] (one grid)
   vfvm::SweepHost* sweep = nullptr;  // sweep engine state (shared-grid batches)
   int last_engine = 0;               // 0 persistent teams, 1 sweep
+  int64_t last_launches = 0;         // kernels launched by the last solve
   ~vfvm_batch() {
     delete sweep;
     if (exec) cudaGraphExecDestroy(exec);

@@ -357,7 +357,7 @@ int sweep_build_graph(SweepHost& h, const SweepArgs<Ph, KT>& a, cudaStream_t s) 
   // prologue: start values, Dirichlet values, state; Newton condition
   VFVM_CUDA(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   sw_init_kernel<Ph, KT><<<grid, kSweepThreads, 0, s>>>(a);
-  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 1, ncond, a.klist, a.kcount);
+  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 1, ncond, a.klist, a.kcount, a.runs);
   VFVM_CUDA(cudaStreamEndCapture(s, &cap));
   cudaGraphNode_t wnode, knode;
   cudaGraph_t body, kbody;
@@ -365,18 +365,18 @@ int sweep_build_graph(SweepHost& h, const SweepArgs<Ph, KT>& a, cudaStream_t s) 
   // Newton body up to the Krylov loop
   VFVM_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   sweep_newton_head<Ph, KT>(a, s);
-  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 0, kcond, a.klist, a.kcount);
+  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 0, kcond, a.klist, a.kcount, a.runs);
   VFVM_CUDA(cudaStreamEndCapture(s, &cap));
   VFVM_CUDA(add_while(body, kcond, &knode, &kbody));
   // one BiCGStab iteration of every active system
   VFVM_CUDA(cudaStreamBeginCaptureToGraph(s, kbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   sweep_krylov_iteration<Ph, KT>(a, s);
-  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 0, kcond, a.klist, a.kcount);
+  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 0, kcond, a.klist, a.kcount, a.runs);
   VFVM_CUDA(cudaStreamEndCapture(s, &cap));
   // Newton update after the Krylov loop, next Newton condition
   VFVM_CUDA(cudaStreamBeginCaptureToGraph(s, body, &knode, nullptr, 1, cudaStreamCaptureModeThreadLocal));
   sw_update_kernel<Ph, KT><<<grid, kSweepThreads, 0, s>>>(a);
-  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 1, ncond, a.klist, a.kcount);
+  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 1, ncond, a.klist, a.kcount, a.runs);
   VFVM_CUDA(cudaStreamEndCapture(s, &cap));
   VFVM_CUDA(cudaGetLastError());
   VFVM_CUDA(cudaGraphInstantiate(&h.exec, g, 0));
@@ -461,6 +461,7 @@ int sweep_run(vfvm_batch* b, const vfvm_control* ctl, double time, double tstep,
     VFVM_CUDA(take(h.tickets, (size_t)S * 4));
     VFVM_CUDA(take(h.call, sizeof(SweepCall)));
     VFVM_CUDA(take(h.klist, (size_t)(S + 1) * 4));
+    VFVM_CUDA(take(h.runs, 2 * sizeof(unsigned)));
     VFVM_CUDA(cudaMemset(h.tickets.p, 0, (size_t)S * 4));
     VFVM_CUDA(cudaMemset(h.st.p, 0, (size_t)S * sizeof(SweepState)));
     VFVM_CUDA(cudaMemset(h.vecs.p, 0, (size_t)9 * S * n * kt));
@@ -494,6 +495,7 @@ int sweep_run(vfvm_batch* b, const vfvm_control* ctl, double time, double tstep,
     a.ncolors = c0->ncolors;
     a.klist = reinterpret_cast<int*>(h.klist.p);
     a.kcount = reinterpret_cast<int*>(h.klist.p) + S;
+    a.runs = reinterpret_cast<unsigned*>(h.runs.p);
     if ((rc = sweep_build_graph<Ph, KT>(h, a, b->stream))) return rc;
     h.precision = ctl->precision;
     h.coarse = ctl->coarse;
@@ -519,6 +521,7 @@ int sweep_run(vfvm_batch* b, const vfvm_control* ctl, double time, double tstep,
   call.fallback = guess ? fallback : nullptr;
   call.guard = guess ? 1 : 0;
   VFVM_CUDA(cudaMemcpyAsync(h.call.p, &call, sizeof(call), cudaMemcpyHostToDevice, b->stream));
+  VFVM_CUDA(cudaMemsetAsync(h.runs.p, 0, 2 * sizeof(unsigned), b->stream));
   VFVM_CUDA(cudaEventRecord(b->e0, b->stream));
   const char* eager = std::getenv("VFVM_SWEEP_EAGER");
   if (eager && eager[0] == '1') {
@@ -533,6 +536,15 @@ int sweep_run(vfvm_batch* b, const vfvm_control* ctl, double time, double tstep,
   VFVM_CUDA(cudaMemcpyAsync(st.data(), h.st.p, (size_t)S * sizeof(SweepState), cudaMemcpyDeviceToHost, b->stream));
   VFVM_CUDA(cudaStreamSynchronize(b->stream));
   if (ms) VFVM_CUDA(cudaEventElapsedTime(ms, b->e0, b->e1));
+  {  // kernels launched by the graph: prologue 2, per Newton body head + 3, per BiCGStab body iteration
+    unsigned runs[2] = {0, 0};
+    VFVM_CUDA(cudaMemcpy(runs, h.runs.p, sizeof(runs), cudaMemcpyDeviceToHost));
+    const int64_t C = c0->ncolors, co = nc > 0 ? 1 : 0;
+    const int64_t NB = runs[1] > 0 ? (int64_t)runs[1] - 1 : 0, KB = (int64_t)runs[0] - NB;
+    const int64_t head = 3 + 1 + C + 1 + 3 * co + 2 * C + 2 * co + 1;   // restart .. kstart
+    const int64_t iter = 2 + 2 * (2 * C + 2 * co) + 1 + 1 + 1 + 1 + 1;  // p, spmv x2, applies, alpha, s, omega, xr, cond
+    b->last_launches = 2 + NB * (head + 3) + KB * iter;
+  }
   std::vector<NewtonOut> outs(S);
   for (int i = 0; i < S; ++i) {
     outs[i] = NewtonOut{st[i].status, st[i].nnewton, st[i].nlin, 0, st[i].updnorm, st[i].resnorm,
@@ -556,6 +568,7 @@ int batch_run_t(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, d
                : sweep_run<Ph, float>(b, ctl, time, tstep, lambda, guess, fallback, ms);
   }
   b->last_engine = 0;
+  b->last_launches = 1;
   const bool f64 = ctl->precision == VFVM_PRECISION_FP64;
   const bool jac = ctl->precon == VFVM_PRECON_JACOBI;
   const int coarse = ctl->precon == VFVM_PRECON_JACOBI ? 0 : ctl->coarse;

@@ -58,6 +58,7 @@ struct SweepArgs {
   int ncolors;
   int* klist;                  // systems still in BiCGStab (built before each iteration)
   int* kcount;
+  unsigned* runs;              // loop-condition evaluations [BiCGStab, Newton] (launch accounting)
 };
 
 // Runs body(i) for the systems this block serves.  use_list = 0: the 2D grid
@@ -599,7 +600,9 @@ __global__ void __launch_bounds__(kSweepThreads) sw_update_kernel(SweepArgs<Ph, 
 // (which 1).  For which 0 also the compact list of systems still in BiCGStab,
 // in system order (one block; each thread takes a contiguous chunk).
 static __global__ void __launch_bounds__(1024) sw_cond_kernel(const SweepState* st, int S, int which,
-                                                             cudaGraphConditionalHandle h, int* klist, int* kcount) {
+                                                             cudaGraphConditionalHandle h, int* klist, int* kcount,
+                                                             unsigned* runs) {
+  if (threadIdx.x == 0) atomicAdd(&runs[which], 1u);  // loop bodies executed (launch accounting)
   __shared__ int wsum[32];
   __shared__ int total;
   const int t = threadIdx.x, nt = blockDim.x;
