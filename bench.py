@@ -643,6 +643,97 @@ def run_reference_learned(args, rank, world):
     return line
 
 
+# ----------------------------------------------------------------------------- other benchmark configurations
+def run_bipolar(args):
+    """3D bipolar drift-diffusion (psi, n, p) on the tetrahedral grid of 64^3 points,
+    doping +-1e3 on the two halves, ohmic contacts at x = 0 and x = 1, bias
+    0.5 * lambda over the embedding lambda = 0, 0.1, ..., 1 (11 Newton solves)."""
+    import torch
+    import __graft_entry__ as ge
+    vfvm = ge.load_package()
+    n = args.nx if args.nx != NX else 64
+    X = np.linspace(0.0, 1.0, n)
+    g = vfvm.simplexgrid(X, X, X)
+    params = [1.0, 1.0, 1.0, 1.0, 1.0, 1.0e3, 0.5]  # lambda^2, mu_n, mu_p, tau_n, tau_p, doping, V
+    sysm = vfvm.System(g, vfvm.Physics("bipolar", params), species=[1, 2, 3])
+    C = np.where(g.coord[0] < 0.5, params[5], -params[5])
+    nn = 0.5 * C + np.sqrt(0.25 * C * C + 1.0)
+    inival = np.asfortranarray(np.stack([np.arcsinh(0.5 * C), nn, 1.0 / nn]))
+    embed = np.linspace(0.0, 1.0, 11)
+    out = {}
+    forms = (("mixed_block_jacobi", "mixed", "jacobi", 0), ("fp64_block_jacobi", "fp64", "jacobi", 0),
+             ("mixed_ilu0_coarse", "mixed", "ilu0", 150))
+    for form, prec, precon, coarse in forms:
+        # fixed embedding steps of 0.1 (the 10-step bias ramp; no step-size control by the change
+        # of the solution, whose densities span 1e-3..1e3), residual control max|F| <= 1e-10
+        c = vfvm.SolverControl(precision=prec, precon_linear=precon, coarse=coarse, engine="graph",
+                               maxiters_linear=2000, reltol_linear=1e-6, updatecontrol=False, abstol=FTOL,
+                               reltol=0.0)
+        c.Δp = c.Δp_max = c.Δp_min = 0.1
+        c.Δu_opt = np.finfo(np.float64).max
+        try:
+            vfvm.solve(sysm, inival=inival, embed=embed[:2], control=c)  # warm-up (graph build)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sol = vfvm.solve(sysm, inival=inival, embed=embed, control=c)
+            ok = len(sol) >= len(embed)
+        except Exception as e:
+            out[form] = {"failed": str(e)}
+            continue
+        secs = time.perf_counter() - t0
+        h = sol.history
+        out[form] = {"solves_per_s": (len(embed) - 1) / secs, "seconds": secs, "completed": bool(ok),
+                     "newton": getattr(h, "nnewton", None), "krylov": getattr(h, "nlin", None)}
+    info = sysm.info()
+    line = {"metric": "Newton solves/s at ||F||<=1e-10 (3D bipolar drift-diffusion, 64^3 points, 10 embedding steps)",
+            "value": next((v["solves_per_s"] for v in out.values() if "solves_per_s" in v), None), "unit": UNIT,
+            "config": {"workload": f"bipolar DD {n}^3 points tetrahedra, 3 species, SG fluxes, SRH, doping +-1e3, "
+                                   "ohmic contacts, bias 0.5 lambda over lambda = 0..1 (11 values)",
+                       "nodes": info["nnodes"], "edges": info["nedges"], "unknowns": 3 * info["nnodes"]},
+            "forms": out, "e2e_api": "vfvm.solve(sys; inival, embed, control) with host buffers"}
+    print(json.dumps(line))
+
+
+def run_rd2_batch(args):
+    """256 two-species reaction-diffusion instances on uneven square grids
+    (33..257 points per side) with D1, D2, k log-uniform in [1e-2, 1e2]
+    (PCG64 seed 0), solved together by the batched solver."""
+    import torch
+    import __graft_entry__ as ge
+    vfvm = ge.load_package()
+    rng = np.random.default_rng(0)
+    S = 256
+    sides = rng.integers(33, 258, size=S)
+    prm = 10.0 ** rng.uniform(-2, 2, size=(S, 3))
+    systems = [vfvm.System(vfvm.simplexgrid(np.linspace(0, 1, m), np.linspace(0, 1, m)), vfvm.Physics("rd2", list(p)),
+                           species=[1, 2]) for m, p in zip(sides, prm)]
+    batch = vfvm.BatchSolver(systems)
+    U0 = torch.full((batch.ndofs,), 0.5, dtype=torch.float64, device="cuda")
+    U = torch.empty_like(U0)
+    out = {}
+    for form, prec, coarse in (("mixed_coarse", "mixed", 100), ("mixed", "mixed", 0), ("fp64_coarse", "fp64", 100)):
+        c = vfvm.SolverControl(precision=prec, precon_linear="ilu0", coarse=coarse, maxiters_linear=1000,
+                               updatecontrol=False, abstol=FTOL, reltol=0.0)
+        try:
+            best, times = batch.tune(U0.data_ptr(), c, candidates=(1, 2, 4, 8))
+            batch.solve_device(U0.data_ptr(), U.data_ptr(), c)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            h = batch.solve_device(U0.data_ptr(), U.data_ptr(), c)
+            secs = time.perf_counter() - t0
+        except Exception as e:
+            out[form] = {"failed": str(e)}
+            continue
+        out[form] = {"solves_per_s": S / secs, "seconds": secs, "ctas_per_system": best, "engine": batch.engine,
+                     "graphed": batch.graphed, "newton_per_solve": float(np.mean([x.nnewton for x in h])),
+                     "krylov_per_solve": float(np.mean([x.nlin for x in h]))}
+    line = {"metric": "Newton solves/s at ||F||<=1e-10 (256 two-species reaction-diffusion instances, uneven grids)",
+            "value": out.get("mixed_coarse", {}).get("solves_per_s"), "unit": UNIT,
+            "config": {"workload": "rd2, 256 instances, sides U{33..257}, D1, D2, k log-uniform [1e-2, 1e2], seed 0",
+                       "unknowns": int(batch.ndofs)}, "forms": out}
+    print(json.dumps(line))
+
+
 def run_batch_only(args):
     """Profiling mode: `--batch-n` kappa-exp instances on the 257 x 257 grid,
     batched mixed-precision solves with the coarse stage from inival 0,
@@ -704,7 +795,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--engine", choices=["persistent", "graph"], default="graph")
     ap.add_argument("--precon", choices=["ilu0", "jacobi", "block_ilu0"], default=PRECON)
-    ap.add_argument("--workload", choices=["learned", "porous"], default="learned")
+    ap.add_argument("--workload", choices=["learned", "porous", "bipolar", "rd2batch"], default="learned")
     ap.add_argument("--ntrain", type=int, default=NTRAIN)
     ap.add_argument("--epochs", type=int, default=300)
     ap.add_argument("--single-sample", type=int, default=16)
@@ -723,6 +814,12 @@ def main():
         if world > 1 and rank != 0:
             return
         (run_reference_learned if args.workload == "learned" else run_reference)(args, rank, world)
+        return
+    if args.workload == "bipolar":
+        run_bipolar(args)
+        return
+    if args.workload == "rd2batch":
+        run_rd2_batch(args)
         return
     if world > 1:
         import torch
