@@ -60,3 +60,32 @@ def test_batch_tune(vfvm):
     sols = batch.solve([np.zeros(s.ndofs) for s in systems])
     ref = vfvm.solve(systems[-1], inival=0.0)
     assert np.max(np.abs(sols[-1] - ref)) <= 1e-8 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_sweep_engine_matches_cta_teams(vfvm, oracle, precision):
+    # a shared-grid batch runs on the sweep engine (whole-GPU kernels over all
+    # systems); the same batch on the CTA-team engine and the oracle agree with it
+    import torch
+    g = vfvm.simplexgrid(lin(24), lin(24))
+    rng = np.random.default_rng(11)
+    kappas = [np.exp(rng.normal(size=g.nnodes)) for _ in range(5)]
+    fs = [-0.9, -0.2, 0.3, 0.8, 0.0]
+    systems = [vfvm.System(g, vfvm.Physics("kappa_exp", [f], k)) for f, k in zip(fs, kappas)]
+    batch = vfvm.BatchSolver(systems)
+    U0 = torch.zeros(batch.ndofs, dtype=torch.float64, device="cuda")
+    out = {}
+    for engine in ("auto", "persistent"):
+        c = vfvm.SolverControl(precision=precision, coarse=50, engine=engine, updatecontrol=False, abstol=1e-12,
+                               reltol=0.0, maxiters_linear=500)
+        U = torch.empty_like(U0)
+        hist = batch.solve_device(U0.data_ptr(), U.data_ptr(), c)
+        assert all(h.status == 0 for h in hist)
+        out[batch.engine] = U.cpu().numpy()
+    assert set(out) == {"sweep", "persistent"}
+    assert np.max(np.abs(out["sweep"] - out["persistent"])) <= 1e-9 * np.max(np.abs(out["persistent"]))
+    for i, (f, k) in enumerate(zip(fs, kappas)):
+        osys = oracle.OracleSystem(g, "kappa_exp", [f], nodedata=k)
+        uo, _ = oracle.solve_step(osys, np.zeros(g.nnodes), oracle.Control(abstol=1e-12, reltol=1e-20))
+        u = out["sweep"][batch.offsets[i]:batch.offsets[i + 1]]
+        assert np.max(np.abs(u - uo)) <= 1e-8 * np.max(np.abs(uo))

@@ -18,8 +18,9 @@ __device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, 
                                               double lambda, double* __restrict__ F, P* __restrict__ J) {
   constexpr int NS = Ph::NS;
   double uK[NS];
+  P uKs[NS];  // the values in the partials' precision, converted once per node
 #pragma unroll
-  for (int i = 0; i < NS; ++i) uK[i] = U[(size_t)K * NS + i];
+  for (int i = 0; i < NS; ++i) { uK[i] = U[(size_t)K * NS + i]; uKs[i] = P(uK[i]); }
   double fK[NS];
   P jd[NS * NS];
 #pragma unroll
@@ -37,7 +38,7 @@ __device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, 
     NodeItem ni{K, reg, xK, time, lambda, dK};
     Dual<NS, P> u[NS], r[NS], s[NS];
 #pragma unroll
-    for (int i = 0; i < NS; ++i) { u[i] = dseed<NS, P>(uK[i], i); r[i] = dconst<NS, P>(0.0); s[i] = dconst<NS, P>(0.0); }
+    for (int i = 0; i < NS; ++i) { u[i] = dseed<NS, P>(uK[i], uKs[i], i); r[i] = dconst<NS, P>(0.0); s[i] = dconst<NS, P>(0.0); }
     double src[NS], ostor[NS];
 #pragma unroll
     for (int i = 0; i < NS; ++i) { src[i] = 0.0; ostor[i] = 0.0; }
@@ -65,8 +66,9 @@ __device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, 
     const int M = t.bcol[s];
     if (M == K) continue;
     double uM[NS];
+    P uMs[NS];
 #pragma unroll
-    for (int i = 0; i < NS; ++i) uM[i] = U[(size_t)M * NS + i];
+    for (int i = 0; i < NS; ++i) { uM[i] = U[(size_t)M * NS + i]; uMs[i] = P(uM[i]); }
     const bool kfirst = K < M;
     const int A = kfirst ? K : M, B = kfirst ? M : K;
     P jo[NS * NS];
@@ -82,12 +84,14 @@ __device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, 
       Dual<2 * NS, P> ua[NS], ub[NS], f[NS];
 #pragma unroll
       for (int i = 0; i < NS; ++i) {
-        ua[i] = dseed<2 * NS, P>(kfirst ? uK[i] : uM[i], i);
-        ub[i] = dseed<2 * NS, P>(kfirst ? uM[i] : uK[i], NS + i);
+        ua[i] = dseed<2 * NS, P>(kfirst ? uK[i] : uM[i], kfirst ? uKs[i] : uMs[i], i);
+        ub[i] = dseed<2 * NS, P>(kfirst ? uM[i] : uK[i], kfirst ? uMs[i] : uKs[i], NS + i);
         f[i] = dconst<2 * NS, P>(0.0);
       }
       ph.flux(f, ua, ub, ei);
-      const P facp = P(fac);
+      P facp;
+      if constexpr (kShadow<P>) facp = MR ? P(fac) : t.slot_facf[s];  // no conversion on the edge path
+      else facp = fac;
       if (kfirst) {
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
@@ -141,7 +145,7 @@ __device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, 
       BNodeItem bi{K, reg, xK, time, lambda, fac, Dir, nullptr};
       Dual<NS, P> u[NS], y[NS];
 #pragma unroll
-      for (int i = 0; i < NS; ++i) { u[i] = dseed<NS, P>(uK[i], i); y[i] = dconst<NS, P>(0.0); }
+      for (int i = 0; i < NS; ++i) { u[i] = dseed<NS, P>(uK[i], uKs[i], i); y[i] = dconst<NS, P>(0.0); }
       ph.breaction(y, u, bi);
       const P facp = P(fac);
 #pragma unroll

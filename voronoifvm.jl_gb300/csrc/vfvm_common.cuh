@@ -4,6 +4,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cmath>
+#include <type_traits>
 
 #include "../../include/vfvm_gb300.h"
 
@@ -31,72 +32,98 @@ constexpr int kMaxBlockIluColors = 32; // colour limit of the subdomain ILU0 pre
 // for the mixed mode, where the Jacobian feeds an FP32 Krylov solve and only the
 // residual (the value path) must be FP64.  GB300 runs FP64 at 1/57 of the FP32
 // rate, so keeping derivative arithmetic in FP32 removes most FP64 instructions
-// from the assembly.
+// from the assembly.  In the mixed mode the partials are formed from `s`, the
+// value carried in FP32 arithmetic of its own (computed alongside v, never
+// converted from it), so no FP64 -> FP32 conversion sits on the derivative
+// path.  In the FP64 mode s is v and every operation is the plain FP64 one.
 // -----------------------------------------------------------------------------
 template <int N, typename P = double>
 struct Dual {
   double v;
+  P s;
   P d[N];
 };
 
+template <typename P> constexpr bool kShadow = !std::is_same<P, double>::value;
+
 template <int N, typename P> VFVM_HD Dual<N, P> dconst(double v) {
-  Dual<N, P> r; r.v = v;
+  Dual<N, P> r; r.v = v; r.s = P(v);
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = P(0);
   return r;
 }
-template <int N, typename P> VFVM_HD Dual<N, P> dseed(double v, int k) {
-  Dual<N, P> r; r.v = v;
+// seed with the value in both precisions (vs: the caller's P(v), converted once)
+template <int N, typename P> VFVM_HD Dual<N, P> dseed(double v, P vs, int k) {
+  Dual<N, P> r; r.v = v; r.s = vs;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = (i == k) ? P(1) : P(0);
   return r;
 }
+template <int N, typename P> VFVM_HD Dual<N, P> dseed(double v, int k) { return dseed<N, P>(v, P(v), k); }
 template <int N, typename P> VFVM_HD double val(const Dual<N, P>& a) { return a.v; }
 VFVM_HD double val(double a) { return a; }
 
 template <int N, typename P> VFVM_HD Dual<N, P> operator+(const Dual<N, P>& a, const Dual<N, P>& b) {
   Dual<N, P> r; r.v = a.v + b.v;
+  if constexpr (kShadow<P>) r.s = a.s + b.s; else r.s = r.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = a.d[i] + b.d[i];
   return r;
 }
 template <int N, typename P> VFVM_HD Dual<N, P> operator-(const Dual<N, P>& a, const Dual<N, P>& b) {
   Dual<N, P> r; r.v = a.v - b.v;
+  if constexpr (kShadow<P>) r.s = a.s - b.s; else r.s = r.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = a.d[i] - b.d[i];
   return r;
 }
 template <int N, typename P> VFVM_HD Dual<N, P> operator-(const Dual<N, P>& a) {
-  Dual<N, P> r; r.v = -a.v;
+  Dual<N, P> r; r.v = -a.v; r.s = -a.s;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = -a.d[i];
   return r;
 }
 template <int N, typename P> VFVM_HD Dual<N, P> operator*(const Dual<N, P>& a, const Dual<N, P>& b) {
   Dual<N, P> r; r.v = a.v * b.v;
-  const P av = P(a.v), bv = P(b.v);
+  if constexpr (kShadow<P>) r.s = a.s * b.s; else r.s = r.v;
 #pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * bv + av * b.d[i];
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b.s + a.s * b.d[i];
   return r;
 }
 template <int N, typename P> VFVM_HD Dual<N, P> operator/(const Dual<N, P>& a, const Dual<N, P>& b) {
   Dual<N, P> r; r.v = a.v / b.v;
-  const P ib = P(1.0 / b.v), q = P(r.v);
+  P ib, q;
+  if constexpr (kShadow<P>) { ib = P(1) / b.s; q = a.s * ib; r.s = q; }
+  else { ib = 1.0 / b.v; q = r.v; r.s = r.v; }
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - q * b.d[i]) * ib;
   return r;
 }
-template <int N, typename P> VFVM_HD Dual<N, P> operator+(const Dual<N, P>& a, double b) { Dual<N, P> r = a; r.v = a.v + b; return r; }
-template <int N, typename P> VFVM_HD Dual<N, P> operator+(double b, const Dual<N, P>& a) { Dual<N, P> r = a; r.v = b + a.v; return r; }
-template <int N, typename P> VFVM_HD Dual<N, P> operator-(const Dual<N, P>& a, double b) { Dual<N, P> r = a; r.v = a.v - b; return r; }
+template <int N, typename P> VFVM_HD Dual<N, P> operator+(const Dual<N, P>& a, double b) {
+  Dual<N, P> r = a; r.v = a.v + b;
+  if constexpr (kShadow<P>) r.s = a.s + P(b); else r.s = r.v;
+  return r;
+}
+template <int N, typename P> VFVM_HD Dual<N, P> operator+(double b, const Dual<N, P>& a) {
+  Dual<N, P> r = a; r.v = b + a.v;
+  if constexpr (kShadow<P>) r.s = P(b) + a.s; else r.s = r.v;
+  return r;
+}
+template <int N, typename P> VFVM_HD Dual<N, P> operator-(const Dual<N, P>& a, double b) {
+  Dual<N, P> r = a; r.v = a.v - b;
+  if constexpr (kShadow<P>) r.s = a.s - P(b); else r.s = r.v;
+  return r;
+}
 template <int N, typename P> VFVM_HD Dual<N, P> operator-(double b, const Dual<N, P>& a) {
   Dual<N, P> r; r.v = b - a.v;
+  if constexpr (kShadow<P>) r.s = P(b) - a.s; else r.s = r.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = -a.d[i];
   return r;
 }
 template <int N, typename P> VFVM_HD Dual<N, P> operator*(const Dual<N, P>& a, double b) {
   Dual<N, P> r; r.v = a.v * b; const P bp = P(b);
+  if constexpr (kShadow<P>) r.s = a.s * bp; else r.s = r.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * bp;
   return r;
@@ -104,24 +131,50 @@ template <int N, typename P> VFVM_HD Dual<N, P> operator*(const Dual<N, P>& a, d
 template <int N, typename P> VFVM_HD Dual<N, P> operator*(double b, const Dual<N, P>& a) { return a * b; }
 template <int N, typename P> VFVM_HD Dual<N, P> operator/(const Dual<N, P>& a, double b) {
   Dual<N, P> r; r.v = a.v / b; const P ib = P(1.0 / b);
+  if constexpr (kShadow<P>) r.s = a.s * ib; else r.s = r.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * ib;
   return r;
 }
-// chain rule helper: r = f(a) with f'(a) = df
-template <int N, typename P> VFVM_HD Dual<N, P> chain(const Dual<N, P>& a, double fv, double df) {
-  Dual<N, P> r; r.v = fv; const P dp = P(df);
+// chain rule helper: r = f(a) with FP64 value fv and, in the partials'
+// precision, value fs and derivative dfs
+template <int N, typename P> VFVM_HD Dual<N, P> chain(const Dual<N, P>& a, double fv, P fs, P dfs) {
+  Dual<N, P> r; r.v = fv; r.s = fs;
 #pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = dp * a.d[i];
+  for (int i = 0; i < N; ++i) r.d[i] = dfs * a.d[i];
   return r;
 }
-template <int N, typename P> VFVM_HD Dual<N, P> exp(const Dual<N, P>& a) { double e = ::exp(a.v); return chain(a, e, e); }
-template <int N, typename P> VFVM_HD Dual<N, P> expm1(const Dual<N, P>& a) { return chain(a, ::expm1(a.v), ::exp(a.v)); }
-template <int N, typename P> VFVM_HD Dual<N, P> log(const Dual<N, P>& a) { return chain(a, ::log(a.v), 1.0 / a.v); }
-template <int N, typename P> VFVM_HD Dual<N, P> log1p(const Dual<N, P>& a) { return chain(a, ::log1p(a.v), 1.0 / (1.0 + a.v)); }
-template <int N, typename P> VFVM_HD Dual<N, P> pow(const Dual<N, P>& a, double p) { return chain(a, ::pow(a.v, p), p * ::pow(a.v, p - 1.0)); }
+template <int N, typename P> VFVM_HD Dual<N, P> exp(const Dual<N, P>& a) {
+  const double e = ::exp(a.v);
+  if constexpr (kShadow<P>) { const P es = ::expf(a.s); return chain(a, e, es, es); }
+  else return chain(a, e, e, e);
+}
+template <int N, typename P> VFVM_HD Dual<N, P> expm1(const Dual<N, P>& a) {
+  const double e = ::expm1(a.v);
+  if constexpr (kShadow<P>) return chain(a, e, ::expm1f(a.s), ::expf(a.s));
+  else return chain(a, e, e, ::exp(a.v));
+}
+template <int N, typename P> VFVM_HD Dual<N, P> log(const Dual<N, P>& a) {
+  const double l = ::log(a.v);
+  if constexpr (kShadow<P>) return chain(a, l, ::logf(a.s), P(1) / a.s);
+  else return chain(a, l, l, 1.0 / a.v);
+}
+template <int N, typename P> VFVM_HD Dual<N, P> log1p(const Dual<N, P>& a) {
+  const double l = ::log1p(a.v);
+  if constexpr (kShadow<P>) return chain(a, l, ::log1pf(a.s), P(1) / (P(1) + a.s));
+  else return chain(a, l, l, 1.0 / (1.0 + a.v));
+}
+template <int N, typename P> VFVM_HD Dual<N, P> pow(const Dual<N, P>& a, double p) {
+  const double w = ::pow(a.v, p);
+  if constexpr (kShadow<P>) { const P pp = P(p); return chain(a, w, ::powf(a.s, pp), pp * ::powf(a.s, pp - P(1))); }
+  else return chain(a, w, w, p * ::pow(a.v, p - 1.0));
+}
 template <int N, typename P> VFVM_HD Dual<N, P> sq(const Dual<N, P>& a) { return a * a; }
-template <int N, typename P> VFVM_HD Dual<N, P> cube(const Dual<N, P>& a) { return chain(a, a.v * a.v * a.v, 3.0 * a.v * a.v); }
+template <int N, typename P> VFVM_HD Dual<N, P> cube(const Dual<N, P>& a) {
+  const double c = a.v * a.v * a.v;
+  if constexpr (kShadow<P>) return chain(a, c, a.s * a.s * a.s, P(3) * a.s * a.s);
+  else return chain(a, c, c, 3.0 * a.v * a.v);
+}
 template <int N, typename P> VFVM_HD Dual<N, P> dmax(const Dual<N, P>& a, double b) { return a.v >= b ? a : dconst<N, P>(b); }
 
 VFVM_HD double sq(double a) { return a * a; }

@@ -188,7 +188,7 @@ AsmTables vfvm_ctx::tables() const {
   t.N = N; t.ns = ns; t.dim = dim;
   t.coord = coord.p; t.browptr = browptr.p; t.bcol = bcol.p; t.diag = diag.p;
   t.region = single_region;
-  t.node_fac = node_fac.p; t.slot_fac = slot_fac.p;
+  t.node_fac = node_fac.p; t.slot_fac = slot_fac.p; t.slot_facf = slot_facf.p;
   t.nitem_ptr = multireg ? nitem_ptr.p : nullptr; t.nitem_reg = nitem_reg.p; t.nitem_fac = nitem_fac.p;
   t.sitem_ptr = multireg ? sitem_ptr.p : nullptr; t.sitem_reg = sitem_reg.p; t.sitem_fac = sitem_fac.p;
   t.bn_ptr = bn_ptr.p; t.bn_reg = bn_reg.p; t.bn_fac = bn_fac.p;
@@ -563,6 +563,10 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
   SETUP_CUDA(c->diag.upload(c->h_diag));
   SETUP_CUDA(c->node_fac.upload(node_fac));
   SETUP_CUDA(c->slot_fac.upload(slot_fac));
+  {
+    std::vector<float> sf(slot_fac.begin(), slot_fac.end());
+    SETUP_CUDA(c->slot_facf.upload(sf));
+  }
   if (c->multireg) {
     SETUP_CUDA(c->nitem_ptr.upload(nitem_ptr));
     SETUP_CUDA(c->nitem_reg.upload(nitem_reg));

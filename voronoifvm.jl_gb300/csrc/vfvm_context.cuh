@@ -44,6 +44,7 @@ struct AsmTables {
   int region;                 // the single cell region
   const double* node_fac;     // N
   const double* slot_fac;     // per slot: edge factor (0 at the diagonal)
+  const float* slot_facf;     // the same in FP32 (mixed-form Jacobian)
   // multi-region path (nullptr otherwise)
   const int* nitem_ptr; const int* nitem_reg; const double* nitem_fac;
   const int* sitem_ptr; const int* sitem_reg; const double* sitem_fac;
@@ -87,6 +88,7 @@ struct vfvm_ctx {
 
   // device tables
   vfvm::DBuf<double> coord, node_fac, slot_fac, nitem_fac, sitem_fac, bn_fac, params, nodedata, bfactors, bvalues;
+  vfvm::DBuf<float> slot_facf;
   vfvm::DBuf<int> browptr, bcol, diag, nitem_ptr, nitem_reg, sitem_ptr, sitem_reg, bn_ptr, bn_reg;
   vfvm::DBuf<uint8_t> dirichlet_dof;       // 1 where a Dirichlet penalty acts on the dof
 

@@ -32,7 +32,7 @@ vfvm_ctx* clone_context(const vfvm_ctx* b, const vfvm_physics_desc* ph, int* sta
   c->grid_base = b->grid_base ? b->grid_base : b;
   CLONE_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   // shared grid tables
-  c->coord.view(b->coord); c->node_fac.view(b->node_fac); c->slot_fac.view(b->slot_fac);
+  c->coord.view(b->coord); c->node_fac.view(b->node_fac); c->slot_fac.view(b->slot_fac); c->slot_facf.view(b->slot_facf);
   c->nitem_fac.view(b->nitem_fac); c->sitem_fac.view(b->sitem_fac); c->bn_fac.view(b->bn_fac);
   c->browptr.view(b->browptr); c->bcol.view(b->bcol); c->diag.view(b->diag);
   c->nitem_ptr.view(b->nitem_ptr); c->nitem_reg.view(b->nitem_reg); c->sitem_ptr.view(b->sitem_ptr);
