@@ -292,9 +292,8 @@ inline cudaError_t add_while(cudaGraph_t g, cudaGraphConditionalHandle h, cudaGr
 // grid of the BiCGStab iteration kernels: bpi blocks per system, striding over
 // the list of systems still iterating (about four waves of blocks when full)
 template <class Ph, typename KT>
-dim3 sweep_list_grid(const SweepArgs<Ph, KT>& a) {
-  const int sg = std::max(1, std::min(a.S, (4 * 152 * 8) / std::max(1, a.bpi)));
-  return dim3(a.bpi, sg);
+dim3 sweep_list_grid(const SweepArgs<Ph, KT>&) {
+  return dim3(4 * 152 * 8);  // 1D: the kernels spread these blocks over the systems still iterating
 }
 
 template <class Ph, typename KT>
@@ -457,7 +456,7 @@ int sweep_run(vfvm_batch* b, const vfvm_control* ctl, double time, double tstep,
     VFVM_CUDA(take(h.crc, (size_t)S * std::max(1, nc) * 4));
     VFVM_CUDA(take(h.czc, (size_t)S * std::max(1, nc) * 4));
     VFVM_CUDA(take(h.st, (size_t)S * sizeof(SweepState)));
-    VFVM_CUDA(take(h.partials, (size_t)S * bpi * 8 * 8));
+    VFVM_CUDA(take(h.partials, (size_t)S * kSweepMaxBpi * 8 * 8));
     VFVM_CUDA(take(h.tickets, (size_t)S * 4));
     VFVM_CUDA(take(h.call, sizeof(SweepCall)));
     VFVM_CUDA(take(h.klist, (size_t)(S + 1) * 4));

@@ -19,6 +19,7 @@
 namespace vfvm {
 
 constexpr int kSweepThreads = 256;
+constexpr int kSweepMaxBpi = 1024;  // blocks per system at most (reduction slots per system)
 
 struct SweepState {
   double damp, oldnorm, tolx, rnorm, norm, resnorm, updnorm, prev_resnorm;
@@ -61,21 +62,33 @@ struct SweepArgs {
   unsigned* runs;              // loop-condition evaluations [BiCGStab, Newton] (launch accounting)
 };
 
-// Runs body(i) for the systems this block serves.  use_list = 0: the 2D grid
-// (bpi x S) covers every system, blocks of finished systems return at once.
-// use_list = 1 (BiCGStab iterations): a smaller grid strides over the compact
-// list of systems still iterating, so iterations late in a solve, when few
-// systems remain, cost little more than their launches.
+// The work unit of a block: system i, block lb of the nb blocks serving it.
+struct SwUnit {
+  int i, lb, nb;
+  __device__ __forceinline__ int tid() const { return lb * blockDim.x + threadIdx.x; }
+  __device__ __forceinline__ int nt() const { return nb * blockDim.x; }
+};
+// 2D grid (blocks per system x systems): one unit per block
+__device__ __forceinline__ SwUnit sw_unit2d() { return SwUnit{(int)blockIdx.y, (int)blockIdx.x, (int)gridDim.x}; }
+
+// Runs body(unit) for the work units this block serves.  use_list = 0: the 2D
+// grid (bpi x S) covers every system, blocks of finished systems return at
+// once.  use_list = 1 (BiCGStab iterations): a 1D grid strides over the units
+// (bpi per system) of the compact list of systems still iterating, so late
+// iterations, when few systems are left, launch few busy blocks.  (Spreading
+// the last systems over more blocks per system was measured slower.)
 template <class Ph, typename KT, class Body>
 __device__ __forceinline__ void sw_for_active(const SweepArgs<Ph, KT>& a, int use_list, Body&& body) {
   if (!use_list) {
-    const int i = blockIdx.y;
-    if (a.st[i].kactive) body(i);
+    const SwUnit u = sw_unit2d();
+    if (a.st[u.i].kactive) body(u);
     return;
   }
   const int cnt = *a.kcount;
-  for (int y = blockIdx.y; y < cnt; y += gridDim.y) {
-    body(a.klist[y]);
+  if (cnt <= 0) return;
+  const int nb = a.bpi;
+  for (int64_t w = blockIdx.x; w < (int64_t)cnt * nb; w += gridDim.x) {
+    body(SwUnit{a.klist[w / nb], (int)(w % nb), nb});
     __syncthreads();
   }
 }
@@ -118,19 +131,18 @@ __device__ __forceinline__ AsmTables sw_tables(const SweepArgs<Ph, KT>& a, int i
   return t;
 }
 
-__device__ __forceinline__ int sw_gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
-__device__ __forceinline__ int sw_gnt() { return gridDim.x * blockDim.x; }
+
 
 // Block reduction of NV values into the system's partial slot; returns true in
 // thread 0 of the system's last block, with out[] = the totals in block order.
 template <int NV>
 __device__ __forceinline__ bool sw_reduce(double (&v)[NV], unsigned maxmask, double* partials, unsigned* tickets,
-                                          int i, int bpi, double (&out)[NV]) {
+                                          int i, int lb, int bpi, double (&out)[NV]) {
   __shared__ double sh[NV][kTeamMaxWarps];
   __shared__ int last;
   block_allreduce<NV>(v, maxmask, sh);
   if (threadIdx.x == 0) {
-    double* slot = partials + ((int64_t)i * bpi + blockIdx.x) * 8;
+    double* slot = partials + ((int64_t)i * kSweepMaxBpi + lb) * 8;
 #pragma unroll
     for (int k = 0; k < NV; ++k) slot[k] = v[k];
     __threadfence();
@@ -147,7 +159,7 @@ __device__ __forceinline__ bool sw_reduce(double (&v)[NV], unsigned maxmask, dou
     const bool mx = (maxmask >> k) & 1;
     double acc = 0.0;
     for (int bx = lane; bx < bpi; bx += 32) {
-      const double pv = __ldcg(&partials[((int64_t)i * bpi + bx) * 8 + k]);
+      const double pv = __ldcg(&partials[((int64_t)i * kSweepMaxBpi + bx) * 8 + k]);
       acc = mx ? fmax(acc, pv) : acc + pv;
     }
 #pragma unroll
@@ -168,7 +180,8 @@ __device__ __forceinline__ bool sw_reduce(double (&v)[NV], unsigned maxmask, dou
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_init_kernel(SweepArgs<Ph, KT> a) {
   constexpr int NS = Ph::NS;
-  const int i = blockIdx.y;
+  const SwUnit u = sw_unit2d();
+  const int i = u.i;
   const SweepCall& c = *a.call;
   const AsmTables t = sw_tables(a, i);
   Ph ph;
@@ -178,14 +191,14 @@ __global__ void __launch_bounds__(kSweepThreads) sw_init_kernel(SweepArgs<Ph, KT
   const double* src = c.start + i * a.n;
   const double* old = (c.fallback ? c.fallback : c.start) + i * a.n;
   double acc[1] = {0.0}, out[1];
-  for (int K = sw_gtid(); K < a.N; K += sw_gnt()) {
+  for (int K = u.tid(); K < a.N; K += u.nt()) {
 #pragma unroll
     for (int k = 0; k < NS; ++k) { U[(int64_t)K * NS + k] = src[(int64_t)K * NS + k]; Uold[(int64_t)K * NS + k] = old[(int64_t)K * NS + k]; }
     init_dirichlet_node<Ph>(t, ph, K, U, c.time, c.lambda);
 #pragma unroll
     for (int k = 0; k < NS; ++k) acc[0] += fabs(U[(int64_t)K * NS + k]);
   }
-  if (sw_reduce<1>(acc, 0u, a.partials, a.tickets, i, a.bpi, out)) {
+  if (sw_reduce<1>(acc, 0u, a.partials, a.tickets, i, u.lb, u.nb, out)) {
     SweepState& s = a.st[i];
     s.rnorm = out[0];
     s.damp = c.ctl.is_linear ? 1.0 : c.ctl.damp_initial;
@@ -202,7 +215,8 @@ __global__ void __launch_bounds__(kSweepThreads) sw_init_kernel(SweepArgs<Ph, KT
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_restart_kernel(SweepArgs<Ph, KT> a) {
   constexpr int NS = Ph::NS;
-  const int i = blockIdx.y;
+  const SwUnit u = sw_unit2d();
+  const int i = u.i;
   if (!a.st[i].restart) return;
   const SweepCall& c = *a.call;
   const AsmTables t = sw_tables(a, i);
@@ -211,14 +225,14 @@ __global__ void __launch_bounds__(kSweepThreads) sw_restart_kernel(SweepArgs<Ph,
   double* U = a.U + i * a.n;
   const double* fb = c.fallback + i * a.n;
   double acc[1] = {0.0}, out[1];
-  for (int K = sw_gtid(); K < a.N; K += sw_gnt()) {
+  for (int K = u.tid(); K < a.N; K += u.nt()) {
 #pragma unroll
     for (int k = 0; k < NS; ++k) U[(int64_t)K * NS + k] = fb[(int64_t)K * NS + k];
     init_dirichlet_node<Ph>(t, ph, K, U, c.time, c.lambda);
 #pragma unroll
     for (int k = 0; k < NS; ++k) acc[0] += fabs(U[(int64_t)K * NS + k]);
   }
-  if (sw_reduce<1>(acc, 0u, a.partials, a.tickets, i, a.bpi, out)) {
+  if (sw_reduce<1>(acc, 0u, a.partials, a.tickets, i, u.lb, u.nb, out)) {
     SweepState& s = a.st[i];
     s.rnorm = out[0];
     s.damp = c.ctl.is_linear ? 1.0 : c.ctl.damp_initial;
@@ -232,7 +246,8 @@ __global__ void __launch_bounds__(kSweepThreads) sw_restart_kernel(SweepArgs<Ph,
 // residual-control exit and the guard test (in the system's last block)
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_assemble_kernel(SweepArgs<Ph, KT> a) {
-  const int i = blockIdx.y;
+  const SwUnit u = sw_unit2d();
+  const int i = u.i;
   if (!a.st[i].nactive) return;
   constexpr int NS = Ph::NS;
   const SweepCall& c = *a.call;
@@ -240,19 +255,20 @@ __global__ void __launch_bounds__(kSweepThreads) sw_assemble_kernel(SweepArgs<Ph
   Ph ph;
   ph.load(t.params);
   int bad = 0;
-  for (int K = sw_gtid(); K < a.N; K += sw_gnt())
+  for (int K = u.tid(); K < a.N; K += u.nt())
     if (assemble_node<Ph, KT, false>(t, ph, K, a.U + i * a.n, a.Uold + i * a.n, c.time, c.tstepinv, c.lambda,
                                      a.F + i * a.n, a.J + (int64_t)i * a.nb * NS * NS))
       bad = 1;
   double acc[1] = {double(bad)}, out[1];
-  if (sw_reduce<1>(acc, 1u, a.partials, a.tickets, i, a.bpi, out) && out[0] != 0.0) {
+  if (sw_reduce<1>(acc, 1u, a.partials, a.tickets, i, u.lb, u.nb, out) && out[0] != 0.0) {
     a.st[i].status = VFVM_ERR_ASSEMBLY;
   }
 }
 
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_prep_kernel(SweepArgs<Ph, KT> a) {
-  const int i = blockIdx.y;
+  const SwUnit u = sw_unit2d();
+  const int i = u.i;
   SweepState& s = a.st[i];
   if (!s.nactive) return;
   const SweepCall& c = *a.call;
@@ -261,14 +277,14 @@ __global__ void __launch_bounds__(kSweepThreads) sw_prep_kernel(SweepArgs<Ph, KT
   KT* x = a.x + i * a.n;
   const uint8_t* dd = a.dirdof;
   double acc[2] = {0.0, 0.0}, out[2];
-  for (int64_t q = sw_gtid(); q < a.n; q += sw_gnt()) {
+  for (int64_t q = u.tid(); q < a.n; q += u.nt()) {
     const double f = F[q];
     b[q] = KT(f);
     x[q] = KT(0);
     acc[0] += f * f;
     if (!dd[q]) acc[1] = fmax(acc[1], fabs(f));
   }
-  if (sw_reduce<2>(acc, 2u, a.partials, a.tickets, i, a.bpi, out)) {
+  if (sw_reduce<2>(acc, 2u, a.partials, a.tickets, i, u.lb, u.nb, out)) {
     s.resnorm = out[1];
     s.kactive = 0;
     if (s.status != VFVM_OK || isnan(out[0])) {
@@ -294,49 +310,54 @@ __global__ void __launch_bounds__(kSweepThreads) sw_prep_kernel(SweepArgs<Ph, KT
 
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_ilu_copy_kernel(SweepArgs<Ph, KT> a) {
-  const int i = blockIdx.y;
+  const SwUnit u = sw_unit2d();
+  const int i = u.i;
   if (!a.st[i].kactive) return;
   constexpr int B = Ph::NS * Ph::NS;
   const int64_t m = (int64_t)a.nb * B;
   const KT* J = a.J + i * m;
   KT* L = a.ilu + i * m;
-  for (int64_t q = sw_gtid(); q < m; q += sw_gnt()) L[q] = J[q];
+  for (int64_t q = u.tid(); q < m; q += u.nt()) L[q] = J[q];
 }
 
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_ilu_factor_kernel(SweepArgs<Ph, KT> a, int c) {
-  const int i = blockIdx.y;
+  const SwUnit u = sw_unit2d();
+  const int i = u.i;
   if (!a.st[i].kactive) return;
   const KrylovData<Ph::NS, KT> d = sw_kd(a, i);
   const IluData<KT> il = sw_il(a, i);
-  for (int p = il.color_ptr[c] + sw_gtid(); p < il.color_ptr[c + 1]; p += sw_gnt())
+  for (int p = il.color_ptr[c] + u.tid(); p < il.color_ptr[c + 1]; p += u.nt())
     ilu_factor_row<Ph::NS, KT>(il.color_nodes[p], d, il);
 }
 
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_pack_kernel(SweepArgs<Ph, KT> a) {
-  const int i = blockIdx.y;
+  const SwUnit u = sw_unit2d();
+  const int i = u.i;
   if (!a.st[i].kactive) return;
   const KrylovData<Ph::NS, KT> d = sw_kd(a, i);
   const IluData<KT> il = sw_il(a, i);
-  pack_ell_rows<Ph::NS, KT>(d, 0, a.N, sw_gtid(), sw_gnt());
-  pack_ilu_positions<Ph::NS, KT>(il, a.N, 0, a.N, sw_gtid(), sw_gnt(), 0, a.N);
+  pack_ell_rows<Ph::NS, KT>(d, 0, a.N, u.tid(), u.nt());
+  pack_ilu_positions<Ph::NS, KT>(il, a.N, 0, a.N, u.tid(), u.nt(), 0, a.N);
 }
 
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_galerkin_kernel(SweepArgs<Ph, KT> a) {
-  const int i = blockIdx.y;
+  const SwUnit u = sw_unit2d();
+  const int i = u.i;
   if (!a.st[i].kactive) return;
   const KrylovData<Ph::NS, KT> d = sw_kd(a, i);
-  for (int64_t e = sw_gtid(); e < (int64_t)d.cd.nc * d.cd.nc; e += sw_gnt()) d.cd.A[e] = 0.f;
+  for (int64_t e = u.tid(); e < (int64_t)d.cd.nc * d.cd.nc; e += u.nt()) d.cd.A[e] = 0.f;
 }
 
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_galerkin2_kernel(SweepArgs<Ph, KT> a) {
-  const int i = blockIdx.y;
+  const SwUnit u = sw_unit2d();
+  const int i = u.i;
   if (!a.st[i].kactive) return;
   const KrylovData<Ph::NS, KT> d = sw_kd(a, i);
-  coarse_galerkin_warps<Ph::NS, KT>(d.cd, d.col, d.A, sw_gtid() >> 5, sw_gnt() >> 5);
+  coarse_galerkin_warps<Ph::NS, KT>(d.cd, d.col, d.A, u.tid() >> 5, u.nt() >> 5);
 }
 
 // one CTA per system: the dense inverse of its coarse matrix in shared memory
@@ -368,49 +389,54 @@ __device__ __forceinline__ void sw_vectors(const SweepArgs<Ph, KT>& a, int i, in
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_ilu_fwd_kernel(SweepArgs<Ph, KT> a, int c, int which,
                                                                    int use_list) {
-  sw_for_active(a, use_list, [&](int i) {
+  sw_for_active(a, use_list, [&](const SwUnit& u) {
+    const int i = u.i;
     const IluData<KT> il = sw_il(a, i);
     const KT* in; KT* out;
     sw_vectors(a, i, which, in, out);
-    ilu_fwd_positions<Ph::NS, KT>(il, a.N, in, out, il.color_ptr[c], il.color_ptr[c + 1], sw_gtid(), sw_gnt());
+    ilu_fwd_positions<Ph::NS, KT>(il, a.N, in, out, il.color_ptr[c], il.color_ptr[c + 1], u.tid(), u.nt());
   });
 }
 
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_ilu_bwd_kernel(SweepArgs<Ph, KT> a, int c, int which,
                                                                    int use_list) {
-  sw_for_active(a, use_list, [&](int i) {
+  sw_for_active(a, use_list, [&](const SwUnit& u) {
+    const int i = u.i;
     const IluData<KT> il = sw_il(a, i);
     const KT* in; KT* out;
     sw_vectors(a, i, which, in, out);
     ilu_bwd_positions<Ph::NS, KT>(il, a.dinv + (int64_t)i * a.N * Ph::NS * Ph::NS, a.N, out, il.color_ptr[c],
-                                  il.color_ptr[c + 1], sw_gtid(), sw_gnt());
+                                  il.color_ptr[c + 1], u.tid(), u.nt());
   });
 }
 
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_coarse_restrict_kernel(SweepArgs<Ph, KT> a, int which,
                                                                            int use_list) {
-  sw_for_active(a, use_list, [&](int i) {
+  sw_for_active(a, use_list, [&](const SwUnit& u) {
+    const int i = u.i;
     const KrylovData<Ph::NS, KT> d = sw_kd(a, i);
     const KT* in; KT* out;
     sw_vectors(a, i, which, in, out);
-    coarse_restrict_warps<Ph::NS, KT>(d.cd, in, sw_gtid() >> 5, sw_gnt() >> 5);
+    coarse_restrict_warps<Ph::NS, KT>(d.cd, in, u.tid() >> 5, u.nt() >> 5);
   });
 }
 
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_coarse_matvec_kernel(SweepArgs<Ph, KT> a, int use_list) {
-  sw_for_active(a, use_list, [&](int i) {
+  sw_for_active(a, use_list, [&](const SwUnit& u) {
+    const int i = u.i;
     const KrylovData<Ph::NS, KT> d = sw_kd(a, i);
-    coarse_matvec_warps(d.cd, sw_gtid() >> 5, sw_gnt() >> 5);
+    coarse_matvec_warps(d.cd, u.tid() >> 5, u.nt() >> 5);
   });
 }
 
 // r0 = r, rho = r.r: start of BiCGStab on the preconditioned right hand side
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_kstart_kernel(SweepArgs<Ph, KT> a) {
-  const int i = blockIdx.y;
+  const SwUnit u = sw_unit2d();
+  const int i = u.i;
   SweepState& s = a.st[i];
   if (!s.kactive) return;
   const int64_t o = i * a.n;
@@ -420,7 +446,7 @@ __global__ void __launch_bounds__(kSweepThreads) sw_kstart_kernel(SweepArgs<Ph, 
   KT* v = a.v + o;
   double acc[1] = {0.0}, out[1];
   const float* zc = a.cd0.nc ? a.cd0.zc + (int64_t)i * a.cd0.nc : nullptr;
-  for (int64_t q = sw_gtid(); q < a.n; q += sw_gnt()) {
+  for (int64_t q = u.tid(); q < a.n; q += u.nt()) {
     KT rq = r[q];
     if (zc && !a.dirdof[q]) {  // r += P zc (coarse prolongation of M^-1 b)
       const int64_t K = q / Ph::NS;
@@ -430,7 +456,7 @@ __global__ void __launch_bounds__(kSweepThreads) sw_kstart_kernel(SweepArgs<Ph, 
     r0[q] = rq; p[q] = KT(0); v[q] = KT(0);
     acc[0] += double(rq) * double(rq);
   }
-  if (sw_reduce<1>(acc, 0u, a.partials, a.tickets, i, a.bpi, out)) {
+  if (sw_reduce<1>(acc, 0u, a.partials, a.tickets, i, u.lb, u.nb, out)) {
     const DevControl& ctl = a.call->ctl;
     s.rho = out[0]; s.rr = out[0]; s.alpha = 1.0; s.omega = 1.0; s.beta = 0.0; s.kit = 0; s.kbreak = 0;
     const double tol = fmax(ctl.abstol_linear, ctl.reltol_linear * sqrt(out[0]));
@@ -441,32 +467,35 @@ __global__ void __launch_bounds__(kSweepThreads) sw_kstart_kernel(SweepArgs<Ph, 
 
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_p_kernel(SweepArgs<Ph, KT> a) {
-  sw_for_active(a, 1, [&](int i) {
+  sw_for_active(a, 1, [&](const SwUnit& u) {
+    const int i = u.i;
     const SweepState& s = a.st[i];
     const int64_t o = i * a.n;
-    vec_p_update<KT>(a.p + o, a.r + o, a.v + o, KT(s.beta), KT(s.omega), sw_gtid(), a.n, sw_gnt());
+    vec_p_update<KT>(a.p + o, a.r + o, a.v + o, KT(s.beta), KT(s.omega), u.tid(), a.n, u.nt());
   });
 }
 
 // y = A p (which 1) or y = A s (which 2)
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_spmv_kernel(SweepArgs<Ph, KT> a, int which) {
-  sw_for_active(a, 1, [&](int i) {
+  sw_for_active(a, 1, [&](const SwUnit& u) {
+    const int i = u.i;
     const KrylovData<Ph::NS, KT> d = sw_kd(a, i);
     const int64_t o = i * a.n;
-    spmv_ell_rows<Ph::NS, KT>(d, which == 1 ? a.p + o : a.s + o, a.y + o, 0, a.N, sw_gtid(), sw_gnt());
+    spmv_ell_rows<Ph::NS, KT>(d, which == 1 ? a.p + o : a.s + o, a.y + o, 0, a.N, u.tid(), u.nt());
   });
 }
 
 // z += P zc (coarse prolongation) fused with acc += (w.z, z.z)
 template <class Ph, typename KT>
-__device__ __forceinline__ void sw_prolong_dot(const SweepArgs<Ph, KT>& a, int i, const KT* __restrict__ w,
+__device__ __forceinline__ void sw_prolong_dot(const SweepArgs<Ph, KT>& a, const SwUnit& u, const KT* __restrict__ w,
                                                KT* __restrict__ z, double (&acc)[2]) {
+  const int i = u.i;
   constexpr int NS = Ph::NS;
   const float* __restrict__ zc = a.cd0.zc + (int64_t)i * a.cd0.nc;
   const int* __restrict__ agg = a.cd0.agg_of_node;
   const uint8_t* __restrict__ dd = a.dirdof;
-  for (int64_t q = sw_gtid(); q < a.n; q += sw_gnt()) {
+  for (int64_t q = u.tid(); q < a.n; q += u.nt()) {
     KT zq = z[q];
     const KT wq = w[q];
     if (!dd[q]) {
@@ -482,14 +511,15 @@ __device__ __forceinline__ void sw_prolong_dot(const SweepArgs<Ph, KT>& a, int i
 // alpha = rho / (r0 . v); s = r - alpha v happens in the next kernel
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_alpha_kernel(SweepArgs<Ph, KT> a) {
-  sw_for_active(a, 1, [&](int i) {
+  sw_for_active(a, 1, [&](const SwUnit& u) {
+    const int i = u.i;
     SweepState& s = a.st[i];
     const int64_t o = i * a.n;
     double acc[2] = {0.0, 0.0}, out[2];
-    if (a.cd0.nc) sw_prolong_dot<Ph, KT>(a, i, a.r0 + o, a.v + o, acc);  // v += P zc, then r0.v
-    else vec_dots<KT>(a.r0 + o, a.v + o, sw_gtid(), a.n, sw_gnt(), acc);
+    if (a.cd0.nc) sw_prolong_dot<Ph, KT>(a, u, a.r0 + o, a.v + o, acc);  // v += P zc, then r0.v
+    else vec_dots<KT>(a.r0 + o, a.v + o, u.tid(), a.n, u.nt(), acc);
     acc[1] = 0.0;
-    if (sw_reduce<2>(acc, 0u, a.partials, a.tickets, i, a.bpi, out)) {
+    if (sw_reduce<2>(acc, 0u, a.partials, a.tickets, i, u.lb, u.nb, out)) {
       if (out[0] == 0.0 || isnan(out[0])) { s.kbreak = 1; s.alpha = 0.0; }
       else s.alpha = s.rho / out[0];
     }
@@ -498,36 +528,39 @@ __global__ void __launch_bounds__(kSweepThreads) sw_alpha_kernel(SweepArgs<Ph, K
 
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_s_kernel(SweepArgs<Ph, KT> a) {
-  sw_for_active(a, 1, [&](int i) {
+  sw_for_active(a, 1, [&](const SwUnit& u) {
+    const int i = u.i;
     const SweepState& s = a.st[i];
     const int64_t o = i * a.n;
-    vec_s_update<KT>(a.s + o, a.r + o, a.v + o, KT(s.alpha), sw_gtid(), a.n, sw_gnt());
+    vec_s_update<KT>(a.s + o, a.r + o, a.v + o, KT(s.alpha), u.tid(), a.n, u.nt());
   });
 }
 
 // omega = (s . t) / (t . t)
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_omega_kernel(SweepArgs<Ph, KT> a) {
-  sw_for_active(a, 1, [&](int i) {
+  sw_for_active(a, 1, [&](const SwUnit& u) {
+    const int i = u.i;
     SweepState& s = a.st[i];
     const int64_t o = i * a.n;
     double acc[2] = {0.0, 0.0}, out[2];
-    if (a.cd0.nc) sw_prolong_dot<Ph, KT>(a, i, a.s + o, a.t2 + o, acc);  // t += P zc, then s.t, t.t
-    else vec_dots<KT>(a.s + o, a.t2 + o, sw_gtid(), a.n, sw_gnt(), acc);
-    if (sw_reduce<2>(acc, 0u, a.partials, a.tickets, i, a.bpi, out)) s.omega = out[1] > 0.0 ? out[0] / out[1] : 0.0;
+    if (a.cd0.nc) sw_prolong_dot<Ph, KT>(a, u, a.s + o, a.t2 + o, acc);  // t += P zc, then s.t, t.t
+    else vec_dots<KT>(a.s + o, a.t2 + o, u.tid(), a.n, u.nt(), acc);
+    if (sw_reduce<2>(acc, 0u, a.partials, a.tickets, i, u.lb, u.nb, out)) s.omega = out[1] > 0.0 ? out[0] / out[1] : 0.0;
   });
 }
 
 // x += alpha p + omega s, r = s - omega t, convergence and the next beta
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_xr_kernel(SweepArgs<Ph, KT> a) {
-  sw_for_active(a, 1, [&](int i) {
+  sw_for_active(a, 1, [&](const SwUnit& u) {
+    const int i = u.i;
     SweepState& s = a.st[i];
     const int64_t o = i * a.n;
     double acc[2] = {0.0, 0.0}, out[2];
-    vec_xr_update<KT>(a.x + o, a.r + o, a.p + o, a.s + o, a.t2 + o, a.r0 + o, KT(s.alpha), KT(s.omega), sw_gtid(),
-                      a.n, sw_gnt(), acc);
-    if (sw_reduce<2>(acc, 0u, a.partials, a.tickets, i, a.bpi, out)) {
+    vec_xr_update<KT>(a.x + o, a.r + o, a.p + o, a.s + o, a.t2 + o, a.r0 + o, KT(s.alpha), KT(s.omega), u.tid(),
+                      a.n, u.nt(), acc);
+    if (sw_reduce<2>(acc, 0u, a.partials, a.tickets, i, u.lb, u.nb, out)) {
       s.kit += 1;
       s.rr = out[1];
       const int brk = s.kbreak || out[0] == 0.0 || s.omega == 0.0 || isnan(out[1]);
@@ -544,7 +577,8 @@ __global__ void __launch_bounds__(kSweepThreads) sw_xr_kernel(SweepArgs<Ph, KT> 
 // Newton update U -= damp x and the solve_step! logic per system
 template <class Ph, typename KT>
 __global__ void __launch_bounds__(kSweepThreads) sw_update_kernel(SweepArgs<Ph, KT> a) {
-  const int i = blockIdx.y;
+  const SwUnit u = sw_unit2d();
+  const int i = u.i;
   SweepState& s = a.st[i];
   if (!s.nactive || s.restart) return;
   const int64_t o = i * a.n;
@@ -553,7 +587,7 @@ __global__ void __launch_bounds__(kSweepThreads) sw_update_kernel(SweepArgs<Ph, 
   double* U = a.U + o;
   const KT* x = a.x + o;
   double acc[2] = {0.0, 0.0}, out[2];
-  for (int64_t q = sw_gtid(); q < a.n; q += sw_gnt()) {
+  for (int64_t q = u.tid(); q < a.n; q += u.nt()) {
     double u = U[q];
     if (apply) {
       const double dx = double(x[q]);
@@ -563,7 +597,7 @@ __global__ void __launch_bounds__(kSweepThreads) sw_update_kernel(SweepArgs<Ph, 
     }
     acc[1] += fabs(u);
   }
-  if (sw_reduce<2>(acc, 1u, a.partials, a.tickets, i, a.bpi, out)) {
+  if (sw_reduce<2>(acc, 1u, a.partials, a.tickets, i, u.lb, u.nb, out)) {
     const DevControl& ctl = a.call->ctl;
     s.nlin += s.kit;
     s.kit = 0;
