@@ -797,7 +797,7 @@ def main():
     ap.add_argument("--precon", choices=["ilu0", "jacobi", "block_ilu0"], default=PRECON)
     ap.add_argument("--workload", choices=["learned", "porous", "bipolar", "rd2batch"], default="learned")
     ap.add_argument("--ntrain", type=int, default=NTRAIN)
-    ap.add_argument("--epochs", type=int, default=300)
+    ap.add_argument("--epochs", type=int, default=600)
     ap.add_argument("--single-sample", type=int, default=16)
     args = ap.parse_args()
     globals()["ENGINE"] = args.engine
