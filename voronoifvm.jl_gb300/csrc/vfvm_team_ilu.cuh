@@ -300,63 +300,6 @@ __device__ bool team_ilu_factor(Team& team, const KrylovData<NS, KT>& d, const I
   return true;
 }
 
-// z = (LU)^-1 y; ends with a team barrier
-template <class Team, int NS, typename KT>
-__device__ bool team_ilu_apply(Team& team, const KrylovData<NS, KT>& d, const IluData<KT>& il, const KT* __restrict__ y,
-                               KT* __restrict__ z) {
-  for (int c = 0; c < il.ncolors; ++c) {
-    for (int idx = il.color_ptr[c] + team.rank(); idx < il.color_ptr[c + 1]; idx += team.size()) {
-      const int K = il.color_nodes[idx];
-      KT w[NS];
-#pragma unroll
-      for (int i = 0; i < NS; ++i) w[i] = y[(size_t)K * NS + i];
-      for (int q = il.lower_ptr[K]; q < il.lower_ptr[K + 1]; ++q) {
-        const int s = il.lower_slots[q];
-        const int k = d.col[s];
-        const KT* Lb = il.ilu + (size_t)s * NS * NS;
-#pragma unroll
-        for (int j = 0; j < NS; ++j) {
-          const KT wk = z[(size_t)k * NS + j];
-#pragma unroll
-          for (int i = 0; i < NS; ++i) w[i] -= Lb[i * NS + j] * wk;
-        }
-      }
-#pragma unroll
-      for (int i = 0; i < NS; ++i) z[(size_t)K * NS + i] = w[i];
-    }
-    if (!team.sync()) return false;
-  }
-  for (int c = il.ncolors - 1; c >= 0; --c) {
-    for (int idx = il.color_ptr[c] + team.rank(); idx < il.color_ptr[c + 1]; idx += team.size()) {
-      const int K = il.color_nodes[idx];
-      KT w[NS];
-#pragma unroll
-      for (int i = 0; i < NS; ++i) w[i] = z[(size_t)K * NS + i];
-      for (int s = d.rowptr[K]; s < d.rowptr[K + 1]; ++s) {
-        const int j = d.col[s];
-        if (il.node_color[j] <= c) continue;
-        const KT* Ub = il.ilu + (size_t)s * NS * NS;
-#pragma unroll
-        for (int jj = 0; jj < NS; ++jj) {
-          const KT zj = z[(size_t)j * NS + jj];
-#pragma unroll
-          for (int i = 0; i < NS; ++i) w[i] -= Ub[i * NS + jj] * zj;
-        }
-      }
-      const KT* D = d.dinv + (size_t)K * NS * NS;
-#pragma unroll
-      for (int i = 0; i < NS; ++i) {
-        KT acc = KT(0);
-#pragma unroll
-        for (int j = 0; j < NS; ++j) acc += D[i * NS + j] * w[j];
-        z[(size_t)K * NS + i] = acc;
-      }
-    }
-    if (!team.sync()) return false;
-  }
-  return true;
-}
-
 // ---------------------------------------------------------------------------
 // BiCGStab vector updates, four elements per thread per pass (q, q+st, q+2st,
 // q+3st: each load instruction stays coalesced across the threads, and a
@@ -466,56 +409,8 @@ __device__ bool team_ilu_apply_ell(Team& team, const KrylovData<NS, KT>& d, cons
   return true;
 }
 
-// out = A x (plain), LPR lanes per block row
-template <class Team, int NS, int LPR, typename KT>
-__device__ __forceinline__ void team_spmv(Team& team, const KrylovData<NS, KT>& d, const KT* __restrict__ xin,
-                                          KT* __restrict__ out) {
-  const int sub = team.rank() % LPR;
-  const int group = team.rank() / LPR;
-  const int ngroups = team.size() / LPR;
-  const int warp_first_group = (team.rank() & ~31) / LPR;
-  for (int base = warp_first_group; base < d.N; base += ngroups) {
-    const int K = base + (group - warp_first_group);
-    KT y[NS];
-#pragma unroll
-    for (int i = 0; i < NS; ++i) y[i] = KT(0);
-    if (K < d.N) {
-      const int beg = d.rowptr[K], end = d.rowptr[K + 1];
-      for (int s = beg + sub; s < end; s += LPR) {
-        const int m = d.col[s];
-        const KT* Ab = d.A + (size_t)s * NS * NS;
-#pragma unroll
-        for (int j = 0; j < NS; ++j) {
-          const KT xm = xin[(size_t)m * NS + j];
-#pragma unroll
-          for (int i = 0; i < NS; ++i) y[i] += Ab[i * NS + j] * xm;
-        }
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < NS; ++i)
-#pragma unroll
-      for (int o = LPR / 2; o > 0; o >>= 1) y[i] += __shfl_down_sync(0xffffffffu, y[i], o, LPR);
-    if (K < d.N && sub == 0) {
-#pragma unroll
-      for (int i = 0; i < NS; ++i) out[(size_t)K * NS + i] = y[i];
-    }
-  }
-}
-
-// dot products w.z and z.z over the team's dofs
-template <class Team, typename KT>
-__device__ __forceinline__ void team_dots(Team& team, int64_t n, const KT* __restrict__ w, const KT* __restrict__ z,
-                                          double (&acc)[2]) {
-  for (int64_t q = team.rank(); q < n; q += team.size()) {
-    const double zz = double(z[q]);
-    acc[0] += double(w[q]) * zz;
-    acc[1] += zz * zz;
-  }
-}
-
-// Left-ILU0-preconditioned BiCGStab: solves A x = b (x starts at 0).  `iters`
-// receives the iteration count on every thread.  Returns false if a barrier expired.
+// Left multicolour-ILU0 BiCGStab (ELL SpMV and sweeps, optional coarse stage):
+// solves A x = b from x = 0; `iters` is set on every thread.
 template <class Team, int NS, int LPR, typename KT>
 __device__ bool team_bicgstab_ilu(Team& team, const KrylovData<NS, KT>& d, const IluData<KT>& il, const KrylovCtl& c,
                                   int64_t nvals, int& iters) {
@@ -679,63 +574,6 @@ __device__ void bilu_factor(const Subdomain& sd, const KrylovData<NS, KT>& d, co
   }
 }
 
-// CTA-local z = (LU)^-1 y on the subdomain's rows; ends with __syncthreads
-template <int NS, typename KT>
-__device__ void bilu_apply(const Subdomain& sd, const KrylovData<NS, KT>& d, const IluData<KT>& il,
-                           const KT* __restrict__ y, KT* __restrict__ z) {
-  for (int c = 0; c < il.ncolors; ++c) {
-    for (int idx = sd.cb[c] + threadIdx.x; idx < sd.ce[c]; idx += blockDim.x) {
-      const int K = il.color_nodes[idx];
-      KT w[NS];
-#pragma unroll
-      for (int i = 0; i < NS; ++i) w[i] = y[(size_t)K * NS + i];
-      for (int q = il.lower_ptr[K]; q < il.lower_ptr[K + 1]; ++q) {
-        const int s = il.lower_slots[q];
-        const int k = d.col[s];
-        if (k < sd.K0 || k >= sd.K1) continue;
-        const KT* Lb = il.ilu + (size_t)s * NS * NS;
-#pragma unroll
-        for (int j = 0; j < NS; ++j) {
-          const KT wk = z[(size_t)k * NS + j];
-#pragma unroll
-          for (int i = 0; i < NS; ++i) w[i] -= Lb[i * NS + j] * wk;
-        }
-      }
-#pragma unroll
-      for (int i = 0; i < NS; ++i) z[(size_t)K * NS + i] = w[i];
-    }
-    __syncthreads();
-  }
-  for (int c = il.ncolors - 1; c >= 0; --c) {
-    for (int idx = sd.cb[c] + threadIdx.x; idx < sd.ce[c]; idx += blockDim.x) {
-      const int K = il.color_nodes[idx];
-      KT w[NS];
-#pragma unroll
-      for (int i = 0; i < NS; ++i) w[i] = z[(size_t)K * NS + i];
-      for (int s = d.rowptr[K]; s < d.rowptr[K + 1]; ++s) {
-        const int j = d.col[s];
-        if (j < sd.K0 || j >= sd.K1 || il.node_color[j] <= c) continue;
-        const KT* Ub = il.ilu + (size_t)s * NS * NS;
-#pragma unroll
-        for (int jj = 0; jj < NS; ++jj) {
-          const KT zj = z[(size_t)j * NS + jj];
-#pragma unroll
-          for (int i = 0; i < NS; ++i) w[i] -= Ub[i * NS + jj] * zj;
-        }
-      }
-      const KT* D = d.dinv + (size_t)K * NS * NS;
-#pragma unroll
-      for (int i = 0; i < NS; ++i) {
-        KT acc = KT(0);
-#pragma unroll
-        for (int j = 0; j < NS; ++j) acc += D[i * NS + j] * w[j];
-        z[(size_t)K * NS + i] = acc;
-      }
-    }
-    __syncthreads();
-  }
-}
-
 // CTA-local z = (LU)^-1 y on the subdomain's positions with the ELL couplings
 // (couplings that leave the subdomain were packed as 0); ends with __syncthreads
 template <int NS, typename KT>
@@ -748,43 +586,6 @@ __device__ void bilu_apply_ell(const Subdomain& sd, const KrylovData<NS, KT>& d,
   for (int c = il.ncolors - 1; c >= 0; --c) {
     ilu_bwd_positions<NS, KT>(il, d.dinv, d.N, z, sd.cb[c], sd.ce[c], threadIdx.x, blockDim.x);
     __syncthreads();
-  }
-}
-
-// y = A x on the subdomain's rows, LPR lanes per block row, CTA threads only
-template <int NS, int LPR, typename KT>
-__device__ __forceinline__ void cta_spmv(const Subdomain& sd, const KrylovData<NS, KT>& d, const KT* __restrict__ xin,
-                                         KT* __restrict__ out) {
-  const int sub = threadIdx.x % LPR;
-  const int group = threadIdx.x / LPR;
-  const int ngroups = blockDim.x / LPR;
-  const int warp_first_group = (threadIdx.x & ~31) / LPR;
-  for (int base = sd.K0 + warp_first_group; base < sd.K1; base += ngroups) {
-    const int K = base + (group - warp_first_group);
-    KT y[NS];
-#pragma unroll
-    for (int i = 0; i < NS; ++i) y[i] = KT(0);
-    if (K < sd.K1) {
-      const int beg = d.rowptr[K], end = d.rowptr[K + 1];
-      for (int s = beg + sub; s < end; s += LPR) {
-        const int m = d.col[s];
-        const KT* Ab = d.A + (size_t)s * NS * NS;
-#pragma unroll
-        for (int j = 0; j < NS; ++j) {
-          const KT xm = xin[(size_t)m * NS + j];
-#pragma unroll
-          for (int i = 0; i < NS; ++i) y[i] += Ab[i * NS + j] * xm;
-        }
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < NS; ++i)
-#pragma unroll
-      for (int o = LPR / 2; o > 0; o >>= 1) y[i] += __shfl_down_sync(0xffffffffu, y[i], o, LPR);
-    if (K < sd.K1 && sub == 0) {
-#pragma unroll
-      for (int i = 0; i < NS; ++i) out[(size_t)K * NS + i] = y[i];
-    }
   }
 }
 
