@@ -661,13 +661,16 @@ def run_bipolar(args):
     inival = np.asfortranarray(np.stack([np.arcsinh(0.5 * C), nn, 1.0 / nn]))
     embed = np.linspace(0.0, 1.0, 11)
     out = {}
-    forms = (("mixed_block_jacobi", "mixed", "jacobi", 0), ("fp64_block_jacobi", "fp64", "jacobi", 0),
-             ("mixed_ilu0_coarse", "mixed", "ilu0", 150))
-    for form, prec, precon, coarse in forms:
+    # (form, precision, preconditioner, coarse unknowns, relative BiCGStab tolerance): the FP32
+    # Krylov solve cannot reach 1e-6 on this badly scaled system (densities 1e-3..1e3), so the
+    # mixed forms ask for less and let the FP64 Newton iteration refine
+    forms = (("mixed_block_jacobi", "mixed", "jacobi", 0, 1e-3), ("fp64_block_jacobi", "fp64", "jacobi", 0, 1e-6),
+             ("mixed_block_jacobi_2", "mixed", "jacobi", 0, 1e-2), ("mixed_ilu0_coarse", "mixed", "ilu0", 150, 1e-3))
+    for form, prec, precon, coarse, rtl in forms:
         # fixed embedding steps of 0.1 (the 10-step bias ramp; no step-size control by the change
         # of the solution, whose densities span 1e-3..1e3), residual control max|F| <= 1e-10
         c = vfvm.SolverControl(precision=prec, precon_linear=precon, coarse=coarse, engine="graph",
-                               maxiters_linear=2000, reltol_linear=1e-6, updatecontrol=False, abstol=FTOL,
+                               maxiters_linear=2000, reltol_linear=rtl, updatecontrol=False, abstol=FTOL,
                                reltol=0.0)
         c.Δp = c.Δp_max = c.Δp_min = 0.1
         c.Δu_opt = np.finfo(np.float64).max

@@ -197,6 +197,30 @@ def test_bipolar_embedding_vs_oracle(vfvm, oracle):
     assert rel_err(tsol.u[-1], osols[-1]) <= SOL_TOL
 
 
+@pytest.mark.parametrize("precision,reltol_linear", [("fp64", 1e-6), ("mixed", 1e-3)])
+def test_bipolar_fixed_ramp_block_jacobi_vs_oracle(vfvm, oracle, precision, reltol_linear):
+    # the 3D drift-diffusion benchmark's form on a small grid: block-Jacobi (3x3)
+    # BiCGStab, fixed embedding steps of 0.1 (no step control by the solution
+    # change), FP32 Krylov refined by the FP64 Newton iteration in the mixed form
+    g = vfvm.simplexgrid(lin(7), lin(7), lin(7))
+    sys = vfvm.System(g, vfvm.Physics("bipolar", BIPOLAR), species=[1, 2, 3])
+    C = np.where(g.coord[0] < 0.5, BIPOLAR[5], -BIPOLAR[5])
+    nn = 0.5 * C + np.sqrt(0.25 * C * C + 1.0)
+    inival = np.asfortranarray(np.stack([np.arcsinh(0.5 * C), nn, 1.0 / nn]))
+    control = vfvm.SolverControl(precon_linear="jacobi", precision=precision, engine="graph", maxiters_linear=2000,
+                                 reltol_linear=reltol_linear, updatecontrol=False, abstol=1e-10, reltol=0.0)
+    control.Δp = control.Δp_max = control.Δp_min = 0.1
+    control.Δu_opt = np.finfo(np.float64).max
+    embed = np.linspace(0.0, 1.0, 11)
+    tsol = vfvm.solve(sys, inival=inival, embed=embed, control=control)
+    osys = oracle.OracleSystem(g, "bipolar", BIPOLAR)
+    oc = oracle.Control()
+    oc.Δp = oc.Δp_max = oc.Δp_min = 0.1
+    oc.Δu_opt = np.finfo(np.float64).max
+    _, osols, _ = oracle.solve_transient(osys, inival.ravel(order="F"), embed, oc, transient=False)
+    assert rel_err(tsol.u[-1], osols[-1]) <= SOL_TOL
+
+
 def test_convergence_error(vfvm):
     sys = vfvm.System(vfvm.simplexgrid(lin(16), lin(16)), vfvm.Physics("nlpoisson"))
     with pytest.raises(vfvm.ConvergenceError):
