@@ -471,6 +471,9 @@ def run_learned(args, rank, world):
         return float(np.mean(ms)), out
 
     ctl_l = learned_control(vfvm, "learned")
+    # the in-project autotuner: blocks per system of the sweep engine (timed on the batch itself)
+    best_bpi, tune_ms = sweep.solver.tune(zeros.data_ptr(), learned_control(vfvm, "batched_mixed"),
+                                          candidates=(16, 32, 64, 128))
 
     def learned_step():
         model.predict_device(Xe, scale=Se, out=guess)
@@ -566,6 +569,7 @@ def run_learned(args, rank, world):
                      "data_s": t_data, "train_s": t_train, "setup_s": t_setup},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "engine": sweep.solver.engine,
+        "autotune": {"blocks_per_system": best_bpi, "ms": tune_ms},
         "roofline": {"kernel": "batched Newton solve (sweep engine: one CUDA graph of whole-GPU kernels over all "
                                "instances: assembly, ILU0, coarse stage, BiCGStab)",
                      "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

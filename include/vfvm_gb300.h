@@ -244,9 +244,10 @@ int vfvm_batch_solve_device(vfvm_batch* batch, const vfvm_control* control, cons
 int vfvm_batch_solve_guarded_device(vfvm_batch* batch, const vfvm_control* control, const double* guess_dev,
                                     const double* inival_dev, double* U_dev, double time, double tstep,
                                     double lambda, vfvm_history* hist, int32_t* from_guess);
-/* Autotuner: times the batch from inival_dev (device) for each candidate number
- * of CTAs per system, keeps the fastest for later solves of this batch and
- * reports it in *best_ctas; times_ms[k] = -1 for candidates that do not fit. */
+/* Autotuner: times the batch from inival_dev (device) for each candidate -- CTAs
+ * per system on the CTA-team engine, blocks per system on the sweep engine --
+ * keeps the fastest for later solves of this batch and reports it in
+ * *best_ctas; times_ms[k] = -1 for candidates that do not fit. */
 int vfvm_batch_tune(vfvm_batch* batch, const vfvm_control* control, const double* inival_dev, int32_t* best_ctas,
                     float* times_ms, int32_t ncand, const int32_t* candidates);
 

@@ -129,7 +129,7 @@ cudaError_t wait_legacy_stream(vfvm_batch* b) {
 
 int batch_ctas(vfvm_batch* b, const vfvm_control* ctl) {
   if (ctl->team_ctas > 0) return ctl->team_ctas;
-  if (b->tuned_ctas > 0) return b->tuned_ctas;
+  if (b->tuned_ctas > 0 && b->tuned_engine == 0) return b->tuned_ctas;
   return 2;
 }
 
@@ -212,17 +212,22 @@ extern "C" int vfvm_batch_tune(vfvm_batch* b, const vfvm_control* ctl, const dou
   float best = 1e30f;
   int bestc = candidates[0];
   VFVM_CUDA(wait_legacy_stream(b));
+  // the candidates are CTAs per system (team engine) or blocks per system (sweep
+  // engine), passed as the control's team_ctas
+  vfvm_control c = *ctl;
   for (int k = 0; k < ncand; ++k) {
     VFVM_CUDA(cudaMemcpyAsync(b->U.p, inival_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
     VFVM_CUDA(cudaMemcpyAsync(b->Uold.p, inival_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
     float ms = 0;
-    int rc = batch_run(b, ctl, candidates[k], 0.0, INFINITY, 0.0, &ms);
+    c.team_ctas = candidates[k];
+    int rc = batch_run(b, &c, candidates[k], 0.0, INFINITY, 0.0, &ms);
     if (rc == VFVM_ERR_INPUT) { if (times_ms) times_ms[k] = -1.0f; continue; }  // does not fit the device
     if (rc) return rc;
     if (times_ms) times_ms[k] = ms;
     if (batch_results(b, nullptr, ms) == VFVM_OK && ms < best) { best = ms; bestc = candidates[k]; }
   }
   b->tuned_ctas = bestc;
+  b->tuned_engine = b->last_engine;
   if (best_ctas) *best_ctas = bestc;
   return VFVM_OK;
 }

@@ -9,7 +9,7 @@
 namespace vfvm {
 // device memory and the captured graph of the sweep engine (vfvm_sweep.cuh)
 struct SweepHost {
-  int precision = -1, coarse = -1;
+  int precision = -1, coarse = -1, bpi = -1;
   bool valid = false;                 // false after vfvm_batch_set_instance: parameters are re-gathered
   DBuf<char> F, J, ilu, dinv, ell, lo, up, vecs, params, nodedata, cA, crc, czc, st, partials, tickets, call, klist,
       runs;
@@ -41,7 +41,8 @@ struct vfvm_batch {
   vfvm::DBuf<int> failed;
   cudaStream_t stream = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  int tuned_ctas = 0;
+  int tuned_ctas = 0;                // autotuned CTAs per system (team engine) or blocks per system (sweep)
+  int tuned_engine = -1;             // engine the tuned value belongs to
   cudaGraphExec_t exec = nullptr;  // the captured solve (resets + persistent launch)
   bool use_graph = true, last_graphed = false;
   bool shared_grid = false;          // all systems are clones of ctx[0] (one grid)

@@ -424,9 +424,11 @@ int sweep_eager(const SweepArgs<Ph, KT>& a, cudaStream_t s) {
   return rc;
 }
 
+// bpi_req: blocks per system (0: chosen from the system size; the autotuner
+// passes its candidates here)
 template <class Ph, typename KT>
-int sweep_run(vfvm_batch* b, const vfvm_control* ctl, double time, double tstep, double lambda, const double* guess,
-              const double* fallback, float* ms) {
+int sweep_run(vfvm_batch* b, const vfvm_control* ctl, int bpi_req, double time, double tstep, double lambda,
+              const double* guess, const double* fallback, float* ms) {
   constexpr int NS = Ph::NS, B = NS * NS;
   vfvm_ctx* c0 = b->ctx[0];
   const int S = b->ninst, N = c0->N;
@@ -437,8 +439,9 @@ int sweep_run(vfvm_batch* b, const vfvm_control* ctl, double time, double tstep,
   if (!b->sweep) b->sweep = new SweepHost;
   SweepHost& h = *b->sweep;
   const int nc = c0->coarse ? c0->coarse->nc : 0;
-  const int bpi = std::max(1, std::min(64, (N + kSweepThreads * 4 - 1) / (kSweepThreads * 4)));
-  if (h.precision != ctl->precision || h.coarse != ctl->coarse || !h.exec) {
+  const int bpi = bpi_req > 0 ? std::min(bpi_req, kSweepMaxBpi)
+                              : std::max(1, std::min(64, (N + kSweepThreads * 4 - 1) / (kSweepThreads * 4)));
+  if (h.precision != ctl->precision || h.coarse != ctl->coarse || h.bpi != bpi || !h.exec) {
     auto take = [](DBuf<char>& d, size_t bytes) { return d.n == bytes ? cudaSuccess : d.alloc(bytes); };
     const size_t kt = sizeof(KT);
     const int np = std::max(1, c0->nparams), nnd = c0->nnd;
@@ -498,6 +501,7 @@ int sweep_run(vfvm_batch* b, const vfvm_control* ctl, double time, double tstep,
     if ((rc = sweep_build_graph<Ph, KT>(h, a, b->stream))) return rc;
     h.precision = ctl->precision;
     h.coarse = ctl->coarse;
+    h.bpi = bpi;
     h.valid = false;
   }
   if (!h.valid) {  // gather every system's parameters and node data
@@ -562,9 +566,11 @@ int batch_run_t(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, d
   // shared-grid batches with ILU0 run on the sweep engine unless the persistent engine is asked for
   if (b->shared_grid && ctl->precon == VFVM_PRECON_ILU0 && ctl->engine != VFVM_ENGINE_PERSISTENT &&
       !b->ctx[0]->has_legacy && !b->ctx[0]->multireg) {
+    // blocks per system: the control's team_ctas, else the autotuned value, else automatic
+    const int bpi = ctl->team_ctas > 0 ? ctas : b->tuned_engine == 1 ? b->tuned_ctas : 0;
     return ctl->precision == VFVM_PRECISION_FP64
-               ? sweep_run<Ph, double>(b, ctl, time, tstep, lambda, guess, fallback, ms)
-               : sweep_run<Ph, float>(b, ctl, time, tstep, lambda, guess, fallback, ms);
+               ? sweep_run<Ph, double>(b, ctl, bpi, time, tstep, lambda, guess, fallback, ms)
+               : sweep_run<Ph, float>(b, ctl, bpi, time, tstep, lambda, guess, fallback, ms);
   }
   b->last_engine = 0;
   b->last_launches = 1;

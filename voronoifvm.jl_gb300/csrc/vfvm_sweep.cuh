@@ -486,13 +486,19 @@ __global__ void __launch_bounds__(kSweepThreads) sw_spmv_kernel(SweepArgs<Ph, KT
   });
 }
 
-// z += P zc (coarse prolongation) fused with acc += (w.z, z.z)
+// z += P zc (coarse prolongation) fused with acc += (w.z, z.z); the system's
+// coarse solution is staged in shared memory first (one L2 read per block
+// instead of one per unknown)
 template <class Ph, typename KT>
 __device__ __forceinline__ void sw_prolong_dot(const SweepArgs<Ph, KT>& a, const SwUnit& u, const KT* __restrict__ w,
                                                KT* __restrict__ z, double (&acc)[2]) {
-  const int i = u.i;
   constexpr int NS = Ph::NS;
-  const float* __restrict__ zc = a.cd0.zc + (int64_t)i * a.cd0.nc;
+  __shared__ float zcs[kCoarseMax];
+  const int i = u.i;
+  const int nc = a.cd0.nc;
+  const float* zc = a.cd0.zc + (int64_t)i * nc;
+  for (int k = threadIdx.x; k < nc; k += blockDim.x) zcs[k] = __ldcg(&zc[k]);
+  __syncthreads();
   const int* __restrict__ agg = a.cd0.agg_of_node;
   const uint8_t* __restrict__ dd = a.dirdof;
   for (int64_t q = u.tid(); q < a.n; q += u.nt()) {
@@ -500,12 +506,13 @@ __device__ __forceinline__ void sw_prolong_dot(const SweepArgs<Ph, KT>& a, const
     const KT wq = w[q];
     if (!dd[q]) {
       const int64_t K = q / NS;
-      zq += KT(__ldcg(&zc[agg[K] * NS + (int)(q - K * NS)]));
+      zq += KT(zcs[agg[K] * NS + (int)(q - K * NS)]);
       z[q] = zq;
     }
     acc[0] += double(wq) * double(zq);
     acc[1] += double(zq) * double(zq);
   }
+  __syncthreads();  // zcs is reloaded by the block's next unit
 }
 
 // alpha = rho / (r0 . v); s = r - alpha v happens in the next kernel
