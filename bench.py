@@ -473,7 +473,7 @@ def run_learned(args, rank, world):
     ctl_l = learned_control(vfvm, "learned")
     # the in-project autotuner: blocks per system of the sweep engine (timed on the batch itself)
     best_bpi, tune_ms = sweep.solver.tune(zeros.data_ptr(), learned_control(vfvm, "batched_mixed"),
-                                          candidates=(16, 32, 64, 128))
+                                          candidates=(8, 16, 32, 64))
 
     def learned_step():
         model.predict_device(Xe, scale=Se, out=guess)
