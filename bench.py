@@ -36,6 +36,7 @@ import math
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -102,7 +103,7 @@ class ClockSampler:
     def __init__(self, device_index=0):
         self.dev = device_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"vfvm_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
