@@ -66,7 +66,11 @@ extern "C" {
 
 /* linear solver / preconditioner / precision selectors */
 #define VFVM_KRYLOV_BICGSTAB 0
-#define VFVM_KRYLOV_GMRES 1
+#define VFVM_KRYLOV_GMRES 1    /* restarted GMRES(gmres_restart), left-preconditioned (KrylovJL_GMRES in
+                                  examples/DevEx004_EquationBlock3D.jl:187); single-system solves only:
+                                  it runs on the persistent engine (VFVM_ENGINE_GRAPH, multi-region
+                                  systems and batched solves return VFVM_ERR_INPUT) */
+#define VFVM_GMRES_MAX_RESTART 32
 #define VFVM_PRECON_JACOBI 0   /* (block-)Jacobi: inverse of the nspec x nspec diagonal blocks */
 #define VFVM_PRECON_ILU0 1     /* ILU(0) in multicolour order */
 #define VFVM_PRECON_BLOCK_ILU0 2 /* ILU(0) restricted to each CTA's node range (block-Jacobi with ILU0
@@ -111,7 +115,7 @@ typedef struct vfvm_control {
   int32_t krylov;              /* VFVM_KRYLOV_* */
   int32_t precon;              /* VFVM_PRECON_* */
   int32_t precision;           /* VFVM_PRECISION_* */
-  int32_t gmres_restart;
+  int32_t gmres_restart;       /* GMRES: Krylov basis size before a restart, 1..VFVM_GMRES_MAX_RESTART */
   /* time / embedding step control (solve_transient!) */
   double dt, dt_min, dt_max, dt_grow, dt_decrease;
   double dp, dp_min, dp_max, dp_grow, dp_decrease;

@@ -28,6 +28,8 @@ int set_time(vfvm_ctx* c, double time, double tstep, double lambda) {
 
 int set_control(vfvm_ctx* c, const vfvm_control* ctl) {
   if (ctl->precon == VFVM_PRECON_BLOCK_ILU0 && c->ncolors > kMaxBlockIluColors) return VFVM_ERR_INPUT;
+  // GMRES runs on the single-system persistent engine only
+  if (ctl->krylov == VFVM_KRYLOV_GMRES && (c->multireg || ctl->engine == VFVM_ENGINE_GRAPH)) return VFVM_ERR_INPUT;
   if (int rc = ensure_coarse(c, ctl->coarse)) return rc;
   static thread_local DevControl staged;
   staged = make_devcontrol(*ctl);
@@ -41,7 +43,9 @@ int check_control(const vfvm_control* ctl) {
   if (ctl->precision != VFVM_PRECISION_FP64 && ctl->precision != VFVM_PRECISION_MIXED) return VFVM_ERR_INPUT;
   if (ctl->precon != VFVM_PRECON_JACOBI && ctl->precon != VFVM_PRECON_ILU0 && ctl->precon != VFVM_PRECON_BLOCK_ILU0)
     return VFVM_ERR_INPUT;
-  if (ctl->krylov != VFVM_KRYLOV_BICGSTAB) return VFVM_ERR_INPUT;
+  if (ctl->krylov != VFVM_KRYLOV_BICGSTAB && ctl->krylov != VFVM_KRYLOV_GMRES) return VFVM_ERR_INPUT;
+  if (ctl->krylov == VFVM_KRYLOV_GMRES && (ctl->gmres_restart < 1 || ctl->gmres_restart > VFVM_GMRES_MAX_RESTART))
+    return VFVM_ERR_INPUT;
   if (ctl->coarse < 0 || ctl->coarse > VFVM_COARSE_MAX) return VFVM_ERR_INPUT;
   return VFVM_OK;
 }
@@ -50,6 +54,7 @@ int check_control(const vfvm_control* ctl) {
 // values set in the state; leaves the result in c->U and the state in st_host.
 bool use_persistent(const vfvm_ctx* c, const vfvm_control* ctl) {
   if (c->multireg) return false;
+  if (ctl->krylov == VFVM_KRYLOV_GMRES) return true;
   if (ctl->engine == VFVM_ENGINE_AUTO) return (int64_t)c->N * c->ns <= kAutoPersistentDofs;
   return ctl->engine == VFVM_ENGINE_PERSISTENT;
 }

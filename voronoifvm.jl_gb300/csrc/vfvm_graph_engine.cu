@@ -623,6 +623,7 @@ DevControl make_devcontrol(const vfvm_control& c) {
   d.reltol_linear = c.reltol_linear; d.abstol_linear = c.abstol_linear;
   d.maxiters = c.maxiters; d.max_round = c.max_round; d.is_linear = c.is_linear;
   d.updatecontrol = c.updatecontrol; d.maxiters_linear = c.maxiters_linear;
+  d.krylov = c.krylov; d.gmres_restart = c.gmres_restart;
   return d;
 }
 

@@ -24,6 +24,7 @@ struct KrylovData {
   const int* ell_col;
   const int* ell_slot;      // block slot of each ELL entry
   KT* ell_val;              // packed from A after each assembly
+  KT* gv;                   // GMRES Krylov basis: (restart + 1) vectors of N * NS (null: BiCGStab only)
 };
 
 struct KrylovCtl {

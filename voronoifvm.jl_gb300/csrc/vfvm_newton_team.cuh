@@ -1,5 +1,6 @@
 // Team-generic damped Newton (solve_step!, src/vfvm_solver.jl:13-222) with
-// the linear solve done by team BiCGStab (block-Jacobi or multicolour ILU0).
+// the linear solve done by team BiCGStab or, in the single-system persistent
+// kernel, GMRES (block-Jacobi, multicolour or subdomain ILU0).
 // Runs inside one persistent launch: the whole grid for one system, or a group
 // of CTAs per system in the batched solver.  Every decision of the Newton
 // logic is taken redundantly by all threads from the same (deterministic)
@@ -7,7 +8,7 @@
 #pragma once
 #include "vfvm_assembly.cuh"
 #include "vfvm_solver.cuh"
-#include "vfvm_team_ilu.cuh"
+#include "vfvm_team_gmres.cuh"
 
 namespace vfvm {
 
@@ -38,7 +39,8 @@ struct NewtonData {
 // time-step values in nd.Uold).  Returns false if a team barrier expired.
 // guard: give up (VFVM_ERR_CONVERGENCE) as soon as an iteration fails to reduce
 // the FP64 residual max-norm below that of the iteration before.
-template <class Team, class Ph, typename KT, int PRECON>
+// GM: the kernel carries GMRES (ctl.krylov selects it; nd.kd.gv holds the basis).
+template <class Team, class Ph, typename KT, int PRECON, bool GM = false>
 __device__ bool team_newton(Team& team, const NewtonData<Ph, KT>& nd, const DevControl& ctl, double time,
                             double tstepinv, double lambda, NewtonOut& res, bool guard = false) {
   constexpr int NS = Ph::NS;
@@ -86,10 +88,21 @@ __device__ bool team_newton(Team& team, const NewtonData<Ph, KT>& nd, const DevC
     }
     // linear solve J x = F
     int kit = 0;
-    bool ok;
-    if (PRECON == VFVM_PRECON_JACOBI) ok = team_bicgstab_jacobi<Team, NS, kPersistLPR, KT>(team, nd.kd, kctl, nullptr, &kit);
-    else if (PRECON == VFVM_PRECON_ILU0) ok = team_bicgstab_ilu<Team, NS, kPersistLPR, KT>(team, nd.kd, nd.il, kctl, nd.nvals, kit);
-    else ok = team_bicgstab_bilu<Team, NS, kPersistLPR, KT>(team, nd.kd, nd.il, kctl, kit);
+    bool ok = true, solved = false;
+    if constexpr (GM) {
+      if (ctl.krylov == VFVM_KRYLOV_GMRES) {
+        ok = team_gmres<Team, NS, kPersistLPR, KT, PRECON>(team, nd.kd, nd.il, kctl, nd.nvals, ctl.gmres_restart, kit);
+        solved = true;
+      }
+    }
+    if (solved) {
+    } else if (PRECON == VFVM_PRECON_JACOBI) {
+      ok = team_bicgstab_jacobi<Team, NS, kPersistLPR, KT>(team, nd.kd, kctl, nullptr, &kit);
+    } else if (PRECON == VFVM_PRECON_ILU0) {
+      ok = team_bicgstab_ilu<Team, NS, kPersistLPR, KT>(team, nd.kd, nd.il, kctl, nd.nvals, kit);
+    } else {
+      ok = team_bicgstab_bilu<Team, NS, kPersistLPR, KT>(team, nd.kd, nd.il, kctl, kit);
+    }
     if (!ok) return false;
     res.nlin += kit;
     // u -= damp * x
@@ -144,7 +157,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1) newton_persistent_kernel(N
   NewtonOut tot{VFVM_OK, 0, 0, 0, 0.0, 0.0};
   bool ok = true;
   if (run.nsteps == 0) {
-    ok = team_newton<GroupTeam, Ph, KT, PRECON>(team, nd, ctl, run.time, run.tstepinv, run.lambda, tot);
+    ok = team_newton<GroupTeam, Ph, KT, PRECON, true>(team, nd, ctl, run.time, run.tstepinv, run.lambda, tot);
   } else {
     const int64_t n = (int64_t)nd.t.N * Ph::NS;
     double time = run.t0;
@@ -153,7 +166,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1) newton_persistent_kernel(N
       if (!(ok = team.sync())) break;
       time += run.dt;
       NewtonOut one;
-      ok = team_newton<GroupTeam, Ph, KT, PRECON>(team, nd, ctl, time, 1.0 / run.dt, 0.0, one);
+      ok = team_newton<GroupTeam, Ph, KT, PRECON, true>(team, nd, ctl, time, 1.0 / run.dt, 0.0, one);
       tot.nnewton += one.nnewton;
       tot.nlin += one.nlin;
       tot.updnorm = one.updnorm;

@@ -113,6 +113,7 @@ namespace {
 
 int batch_run(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, double tstep, double lambda, float* ms,
               const double* guess = nullptr, const double* fallback = nullptr) {
+  if (ctl->krylov != VFVM_KRYLOV_BICGSTAB) return VFVM_ERR_INPUT;  // batched solves run BiCGStab only
   if (ctl->precon == VFVM_PRECON_BLOCK_ILU0)
     for (auto* c : b->ctx)
       if (c->ncolors > kMaxBlockIluColors) return VFVM_ERR_INPUT;

@@ -58,6 +58,7 @@ NewtonData<Ph, KT> make_newton_data(vfvm_ctx* c, double* U, double* Uold, bool c
   nd.il.up_val = k.up_val.p;
   nd.nvals = c->nnzb * (int64_t)c->ns * c->ns;
   nd.kd.cd = coarse ? c->coarse_data() : CoarseData{};
+  nd.kd.gv = k.gv.p;
   return nd;
 }
 
@@ -73,6 +74,11 @@ int persistent_launch(vfvm_ctx* c, const vfvm_control* ctl, const PersistRunHost
                              float* ms) {
   Workspace* w = c->ws;
   auto kern = newton_persistent_kernel<Ph, KT, PRECON>;
+  if (ctl->krylov == VFVM_KRYLOV_GMRES) {
+    KVecs<KT>& k = *reinterpret_cast<KVecs<KT>*>(std::is_same<KT, double>::value ? (void*)&w->k64 : (void*)&w->k32);
+    const size_t need = (size_t)(ctl->gmres_restart + 1) * c->N * c->ns;
+    if (k.gv.n < need) VFVM_CUDA(k.gv.alloc(need));
+  }
   NewtonData<Ph, KT> nd = make_newton_data<Ph, KT>(c, c->U.p, c->Uold.p, PRECON != VFVM_PRECON_JACOBI);
   const size_t smem = nd.kd.cd.nc ? coarse_smem_bytes(nd.kd.cd.nc) : 0;
   VFVM_CUDA(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

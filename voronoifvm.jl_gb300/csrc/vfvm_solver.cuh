@@ -13,6 +13,7 @@ struct DevControl {
   double abstol, reltol, tol_round, tol_mono, damp_initial, damp_growth;
   double reltol_linear, abstol_linear;
   int maxiters, max_round, is_linear, updatecontrol, maxiters_linear;
+  int krylov, gmres_restart;  // VFVM_KRYLOV_*; GMRES basis size (persistent engine only)
   int pad;
 };
 
@@ -47,6 +48,7 @@ template <typename KT>
 struct KVecs {
   DBuf<KT> b, x, r, r0, p, ph, v, s, sh, t, dinv, ilu;
   DBuf<KT> ell_val, lo_val, up_val;  // ELL values (matrix, ILU0 L and U couplings), packed per Newton step
+  DBuf<KT> gv;                       // GMRES basis, (restart + 1) x N*NS, allocated on first use
 };
 
 struct Workspace {
