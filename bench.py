@@ -529,25 +529,40 @@ def run_learned(args, rank, world):
             nl.append(h.nlin)
         forms[name] = dict(solves_per_s=args.single_sample / secs, newton_per_solve=float(np.mean(nn)),
                            krylov_per_solve=float(np.mean(nl)), sample=args.single_sample)
-    # --- e2e through the public API with host buffers
-    inival_h = np.zeros(NEVAL * N)
+    # --- e2e through the public API with host buffers: the user's inputs are the
+    # node data kappa = exp(G), the sources f and inival in pinned host memory;
+    # per step: features (log kappa at the coarse subgrid nodes) on the host,
+    # H2D copies, load of all instances on the device, prediction, guarded
+    # solve, D2H of the solutions
+    kappa_h = torch.from_numpy(np.exp(logk_e)).pin_memory()
+    f_h = torch.from_numpy(np.ascontiguousarray(f_e, dtype=np.float64)).pin_memory()
+    inival_h = torch.zeros(NEVAL * N, dtype=torch.float64).pin_memory()
+    U_h = torch.empty(NEVAL * N, dtype=torch.float64).pin_memory()
+    kappa_d, f_d = torch.empty_like(kappa_h, device=cuda), torch.empty_like(f_h, device=cuda)
+    ini_d = torch.empty_like(inival_h, device=cuda)
+    kappa_np, f_np = kappa_h.numpy(), f_h.numpy()
     e2e = []
     for it in range(args.warmup + max(1, min(args.steps, 3))):
         flush.fill_(float(it))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        sweep.load(logk_e, f_e)
-        Xh = torch.from_numpy(model.features(logk_e, f_e)).to(cuda)
-        ini = torch.from_numpy(inival_h).to(cuda)
-        g = model.predict_device(Xh, scale=torch.from_numpy(lk.kappa_scale(f_e)).to(cuda))
-        sweep.solve_device(ini.data_ptr(), U.data_ptr(), ctl_l, guess_dev=g.data_ptr())
-        Uh = U.cpu().numpy()
+        Xh = torch.from_numpy(model.features_from_kappa(kappa_np, f_np)).pin_memory()
+        Sh = torch.from_numpy(lk.kappa_scale(f_np)).pin_memory()
+        kappa_d.copy_(kappa_h, non_blocking=True)
+        f_d.copy_(f_h, non_blocking=True)
+        ini_d.copy_(inival_h, non_blocking=True)
+        Xd, Sd = Xh.to(cuda, non_blocking=True), Sh.to(cuda, non_blocking=True)
+        sweep.load_device(kappa_d, f_d)
+        g = model.predict_device(Xd, scale=Sd)
+        sweep.solve_device(ini_d.data_ptr(), U.data_ptr(), ctl_l, guess_dev=g.data_ptr())
+        U_h.copy_(U.view(-1))
         t1 = time.perf_counter()
         if it >= args.warmup:
             e2e.append(t1 - t0)
     e2e_value = NEVAL / float(np.mean(e2e))
-    h2d = int(logk_e.nbytes + f_e.nbytes + Xh.numel() * 4 + inival_h.nbytes)
-    d2h = int(Uh.nbytes)
+    e2e_vs_device = float(np.max(np.abs(U_h.numpy().reshape(NEVAL, N) - U_learned)))
+    h2d = int(kappa_h.numel() * 8 + f_h.numel() * 8 + Xh.numel() * 4 + Sh.numel() * 8 + inival_h.numel() * 8)
+    d2h = int(U_h.numel() * 8)
     # --- roofline of the dominant kernel (the batched Newton launch)
     peak, peak_kind = peaks()
     info = sweep.systems[0].info()
@@ -568,7 +583,8 @@ def run_learned(args, rank, world):
         "learned_vs_plain": forms["learned_mixed_batched"]["solves_per_s"] / forms["plain"]["solves_per_s"],
         "training": {"instances": args.ntrain, "epochs": args.epochs, "loss_first": losses[0], "loss_last": losses[-1],
                      "data_s": t_data, "train_s": t_train, "setup_s": t_setup},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "max_abs_diff_vs_device": e2e_vs_device},
         "engine": sweep.solver.engine,
         "autotune": {"blocks_per_system": best_bpi, "ms": tune_ms},
         "roofline": {"kernel": "batched Newton solve (sweep engine: one CUDA graph of whole-GPU kernels over all "

@@ -221,6 +221,15 @@ int vfvm_batch_offsets(vfvm_batch* batch, int64_t* offsets);
  * one set of device grid tables. */
 int vfvm_batch_set_instance(vfvm_batch* batch, int32_t inst, const double* params, int32_t nparams,
                             const double* nodedata, int32_t nnodedata);
+/* Replace every system's parameters and/or node data (NULL keeps them) from
+ * DEVICE arrays: params_dev = ninst x nparams (system-major), nodedata_dev = the
+ * systems' nnodes_i x nnodedata blocks (node-major) one after another in system
+ * order.  Device-to-device copies on the batch stream after the work already
+ * queued on the legacy default stream (the stream frameworks write inputs on);
+ * returns once they are complete.  The many-systems form of the reference's
+ * new physics `data` between solves (src/vfvm_solver.jl:578-581). */
+int vfvm_batch_load_device(vfvm_batch* batch, const double* params_dev, int32_t nparams,
+                           const double* nodedata_dev, int32_t nnodedata);
 /* out[0] = systems, out[1] = packed unknowns, out[2] = CTAs per system chosen
  * by vfvm_batch_tune (0: not tuned), out[3] = 1 if the last solve ran as a
  * captured CUDA graph, out[4] = engine of the last solve (0: persistent CTA

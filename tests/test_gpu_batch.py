@@ -89,3 +89,38 @@ def test_sweep_engine_matches_cta_teams(vfvm, oracle, precision):
         uo, _ = oracle.solve_step(osys, np.zeros(g.nnodes), oracle.Control(abstol=1e-12, reltol=1e-20))
         u = out["sweep"][batch.offsets[i]:batch.offsets[i + 1]]
         assert np.max(np.abs(u - uo)) <= 1e-8 * np.max(np.abs(uo))
+
+
+@pytest.mark.parametrize("engine", ["auto", "persistent"])
+def test_load_device_matches_set_instance(vfvm, engine):
+    # all instances replaced from device arrays in one call give the same
+    # solutions, bit for bit, as per-instance host updates; both engines
+    import torch
+    g = vfvm.simplexgrid(lin(20), lin(20))
+    rng = np.random.default_rng(21)
+    S = 6
+    systems = [vfvm.System(g, vfvm.Physics("kappa_exp", [0.0], np.ones(g.nnodes))) for _ in range(S)]
+    batch = vfvm.BatchSolver(systems)
+    c = vfvm.SolverControl(precision="mixed", coarse=40, engine=engine, maxiters_linear=500)
+    U0 = torch.zeros(batch.ndofs, dtype=torch.float64, device="cuda")
+    batch.solve_device(U0.data_ptr(), torch.empty_like(U0).data_ptr(), c)  # builds the engine's state first
+    runs = []
+    for _ in range(2):
+        kappa = np.exp(rng.normal(size=(S, g.nnodes)))
+        f = rng.uniform(-1.0, 1.0, size=S)
+        for i in range(S):
+            batch.set_instance(i, data=[f[i]], nodedata=kappa[i])
+        Ua = torch.empty_like(U0)
+        batch.solve_device(U0.data_ptr(), Ua.data_ptr(), c)
+        batch.load_device(params=torch.from_numpy(np.flip(f).copy()).reshape(-1, 1).cuda(),
+                          nodedata=torch.from_numpy(np.flip(kappa, 0).copy()).cuda())  # other values first
+        batch.load_device(params=torch.from_numpy(f).reshape(-1, 1).cuda(), nodedata=torch.from_numpy(kappa).cuda())
+        Ub = torch.empty_like(U0)
+        hist = batch.solve_device(U0.data_ptr(), Ub.data_ptr(), c)
+        assert all(h.status == 0 for h in hist)
+        assert torch.equal(Ua, Ub)
+        runs.append(Ub.cpu().numpy())
+    assert batch.engine == ("sweep" if engine == "auto" else "persistent")
+    assert np.max(np.abs(runs[0] - runs[1])) > 0  # the second load changed the problems
+    with pytest.raises(ValueError):
+        batch.load_device(params=torch.zeros((S, 2), dtype=torch.float64, device="cuda"))

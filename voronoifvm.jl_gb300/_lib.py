@@ -88,6 +88,7 @@ SIGNATURES = {
     "vfvm_batch_offsets": (ctypes.c_int, [c_vp, P(c_i64)]),
     "vfvm_batch_info": (ctypes.c_int, [c_vp, P(c_i64)]),
     "vfvm_batch_set_instance": (ctypes.c_int, [c_vp, c_i32, P(c_d), c_i32, P(c_d), c_i32]),
+    "vfvm_batch_load_device": (ctypes.c_int, [c_vp, c_vp, c_i32, c_vp, c_i32]),
     "vfvm_set_nodedata": (ctypes.c_int, [c_vp, P(c_d), c_i32]),
     "vfvm_batch_solve": (ctypes.c_int, [c_vp, P(Control_t), P(c_d), P(c_d), c_d, c_d, c_d, P(History_t)]),
     "vfvm_batch_solve_device": (ctypes.c_int, [c_vp, P(Control_t), c_vp, c_vp, c_d, c_d, c_d, P(History_t)]),

@@ -16,6 +16,11 @@ import numpy as np
 from . import _lib as L
 from .system import NewtonSolverHistory, SolverControl, System, _flat, _raise, _shape
 
+
+def _check_f64_device(t):
+    if not (getattr(t, "is_cuda", False) and str(t.dtype) == "torch.float64" and t.is_contiguous()):
+        raise ValueError("expected a contiguous float64 CUDA tensor")
+
 __all__ = ["BatchSolver"]
 
 
@@ -99,6 +104,22 @@ class BatchSolver:
             nda = np.ascontiguousarray(a.T)
             nd, ndp = a.shape[0], L.ptr(nda)
         _raise(L.load().vfvm_batch_set_instance(self.h, i, L.ptr(p), p.size, ndp, nd), "vfvm_batch_set_instance")
+
+    def load_device(self, params=None, nodedata=None):
+        """Replace every system's parameters and/or node data from device tensors:
+        ``params`` (ninst, nparams) float64, ``nodedata`` the systems' (nnodes_i,
+        nnodedata) node-major blocks packed in system order (for one shared grid:
+        (ninst, nnodes) when nnodedata == 1).  No host copies; the Python-side
+        ``physics`` records of the systems are not updated."""
+        pp, npar, nd, nnd = None, 0, None, 0
+        if params is not None:
+            _check_f64_device(params)
+            pp, npar = ctypes.c_void_p(params.data_ptr()), int(params.shape[-1]) if params.dim() > 1 else 1
+        if nodedata is not None:
+            _check_f64_device(nodedata)
+            total = sum(s.grid.nnodes for s in self.systems)
+            nd, nnd = ctypes.c_void_p(nodedata.data_ptr()), nodedata.numel() // total
+        _raise(L.load().vfvm_batch_load_device(self.h, pp, npar, nd, nnd), "vfvm_batch_load_device")
 
     def _control(self, control):
         c = (control or SolverControl()).to_c(False)

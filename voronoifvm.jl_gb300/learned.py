@@ -175,6 +175,11 @@ class KappaSweep:
         for i in range(len(f)):
             self.solver.set_instance(i, data=[float(f[i])], nodedata=np.exp(logk[i]))
 
+    def load_device(self, kappa, f):
+        """All instances at once from device tensors: kappa (batch, nnodes) and
+        f (batch,), both float64."""
+        self.solver.load_device(params=f.reshape(-1, 1), nodedata=kappa)
+
     def solve_device(self, inival_dev: int, U_dev: int, control: SolverControl, guess_dev: Optional[int] = None):
         """Solve all instances (packed device arrays of batch * nnodes doubles);
         with guess_dev, the guarded start.  Returns (histories, from_guess)."""
@@ -218,6 +223,11 @@ class LearnedInitialIterate:
 
     def features(self, logk: np.ndarray, f: np.ndarray) -> np.ndarray:
         return np.concatenate([self.coarse(logk), np.asarray(f).reshape(-1, 1)], axis=1).astype(np.float32)
+
+    def features_from_kappa(self, kappa: np.ndarray, f: np.ndarray) -> np.ndarray:
+        """The same features from the node data kappa = exp(G) (logarithms at the
+        coarse subgrid nodes only)."""
+        return np.concatenate([np.log(self.coarse(kappa)), np.asarray(f).reshape(-1, 1)], axis=1).astype(np.float32)
 
     def fit(self, X: np.ndarray, U: np.ndarray, scale=None, epochs: int = 200, batch: int = 256, lr: float = 1e-3,
             lr_final: float = 1e-5, seed: int = 0, log_every: int = 0):
