@@ -551,25 +551,31 @@ def run_learned(args, rank, world):
     kappa_d, f_d = torch.empty_like(kappa_h, device=cuda), torch.empty_like(f_h, device=cuda)
     ini_d = torch.empty_like(inival_h, device=cuda)
     kappa_np, f_np = kappa_h.numpy(), f_h.numpy()
-    e2e = []
+    e2e, phases = [], []
     for it in range(args.warmup + max(1, min(args.steps, 3))):
         flush.fill_(float(it))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         Xh = torch.from_numpy(model.features_from_kappa(kappa_np, f_np)).pin_memory()
         Sh = torch.from_numpy(lk.kappa_scale(f_np)).pin_memory()
+        ta = time.perf_counter()
         kappa_d.copy_(kappa_h, non_blocking=True)
         f_d.copy_(f_h, non_blocking=True)
         ini_d.copy_(inival_h, non_blocking=True)
         Xd, Sd = Xh.to(cuda, non_blocking=True), Sh.to(cuda, non_blocking=True)
-        sweep.load_device(kappa_d, f_d)
+        sweep.load_device(kappa_d, f_d)  # returns once the copies before it are complete
+        tb = time.perf_counter()
         g = model.predict_device(Xd, scale=Sd)
         sweep.solve_device(ini_d.data_ptr(), U.data_ptr(), ctl_l, guess_dev=g.data_ptr())
+        tc = time.perf_counter()
         U_h.copy_(U.view(-1))
         t1 = time.perf_counter()
         if it >= args.warmup:
             e2e.append(t1 - t0)
+            phases.append([ta - t0, tb - ta, tc - tb, t1 - tc])
     e2e_value = NEVAL / float(np.mean(e2e))
+    e2e_phases = dict(zip(("features_ms", "h2d_and_load_ms", "predict_and_solve_ms", "d2h_ms"),
+                          (1e3 * np.mean(phases, axis=0)).tolist()))
     e2e_vs_device = float(np.max(np.abs(U_h.numpy().reshape(NEVAL, N) - U_learned)))
     h2d = int(kappa_h.numel() * 8 + f_h.numel() * 8 + Xh.numel() * 4 + Sh.numel() * 8 + inival_h.numel() * 8)
     d2h = int(U_h.numel() * 8)
@@ -594,7 +600,7 @@ def run_learned(args, rank, world):
         "training": {"instances": args.ntrain, "epochs": args.epochs, "loss_first": losses[0], "loss_last": losses[-1],
                      "data_s": t_data, "train_s": t_train, "setup_s": t_setup},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "max_abs_diff_vs_device": e2e_vs_device},
+                "max_abs_diff_vs_device": e2e_vs_device, "phases": e2e_phases},
         "engine": sweep.solver.engine,
         "autotune": {"blocks_per_system": best_bpi, "ms": tune_ms},
         "roofline": {"kernel": "batched Newton solve (sweep engine: one CUDA graph of whole-GPU kernels over all "
