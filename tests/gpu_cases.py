@@ -1,5 +1,7 @@
 """Small problem definitions shared by the GPU parity tests: one per registered
 physics, on grids small enough for the oracle to finish in well under a second."""
+import os
+
 import numpy as np
 
 
@@ -52,6 +54,10 @@ def case(vfvm, name, seed=0):
         legacy = (bf, bv)
     elif name == "ex440":
         g, kind, params = sg(lin(20)), "ex440", [3.0]
+    elif name == "kappa_unstructured":  # Delaunay grid read from a SimplexGrid file
+        g = sg(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "jittered_square.sg"))
+        kind, params = "kappa_exp", [0.3]
+        nodedata = np.exp(rng.normal(size=g.nnodes))
     elif name == "laplace_dirichlet":
         g, kind, params = sg(lin(9)), "laplace_dirichlet", []
     else:
@@ -73,4 +79,4 @@ def random_state(c, nspec, rng):
 
 
 NAMES = ["nlpoisson", "porous", "bipolar", "rd2", "kappa_exp", "ex105", "ex106", "ex110", "ex160", "ex207",
-         "ex301", "ex440", "laplace_dirichlet"]
+         "ex301", "ex440", "laplace_dirichlet", "kappa_unstructured"]

@@ -221,6 +221,16 @@ def test_bipolar_fixed_ramp_block_jacobi_vs_oracle(vfvm, oracle, precision, relt
     assert rel_err(tsol.u[-1], osols[-1]) <= SOL_TOL
 
 
+@pytest.mark.parametrize("coarse", [0, 40])
+def test_unstructured_grid_vs_oracle(vfvm, oracle, coarse):
+    # Delaunay grid of a jittered lattice, read from a SimplexGrid text file
+    g = vfvm.simplexgrid(os.path.join(GOLDEN, "jittered_square.sg"))
+    kappa = np.exp(np.random.default_rng(9).normal(size=g.nnodes))
+    sys = vfvm.System(g, vfvm.Physics("kappa_exp", [0.7], kappa))
+    U = vfvm.solve(sys, inival=0.0, control=vfvm.SolverControl(maxiters_linear=400, coarse=coarse))
+    assert rel_err(U, oracle_solution(oracle, g, "kappa_exp", [0.7], nodedata=kappa)) <= SOL_TOL
+
+
 def test_convergence_error(vfvm):
     sys = vfvm.System(vfvm.simplexgrid(lin(16), lin(16)), vfvm.Physics("nlpoisson"))
     with pytest.raises(vfvm.ConvergenceError):

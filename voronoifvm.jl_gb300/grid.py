@@ -30,6 +30,8 @@ All index arrays here are 0-based int32; coordinates are float64 with shape
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
 
 __all__ = ["Grid", "simplexgrid"]
@@ -90,6 +92,83 @@ class Grid:
                 f"nbfaces={self.nbfaces})")
 
 
+# --- SimplexGrid text files (ExtendableGrids' ``.sg`` format, e.g. assets/rz2d.sg)
+#
+#   SimplexGrid 2.1            version line (2.0 and 2.1 share this layout)
+#   # ...                      comment lines anywhere
+#   DIMENSION  d
+#   NODES      nnodes d        then nnodes * d coordinates, node after node
+#   CELLS      ncells          then per cell: d+1 node numbers (1-based), region
+#   FACES      nbfaces         then per boundary face: d node numbers (1-based), region
+#   END
+
+SG_VERSION = "2.1"
+
+
+def read_sg(path) -> Grid:
+    """Read a SimplexGrid text file into a Grid (node numbers become 0-based)."""
+    with open(path) as f:
+        lines = [ln.split("#", 1)[0].strip() for ln in f]
+    lines = [ln for ln in lines if ln]
+    if not lines or not lines[0].startswith("SimplexGrid"):
+        raise ValueError(f"{path}: not a SimplexGrid file")
+    version = lines[0].split()[1] if len(lines[0].split()) > 1 else ""
+    if not version.startswith("2."):
+        raise ValueError(f"{path}: unsupported SimplexGrid version {version!r}")
+    tok = " ".join(lines[1:]).split()
+    pos = 0
+
+    def take(n, conv):
+        nonlocal pos
+        if pos + n > len(tok):
+            raise ValueError(f"{path}: truncated")
+        out = [conv(t) for t in tok[pos:pos + n]]
+        pos += n
+        return out
+
+    def expect(key):
+        if take(1, str)[0] != key:
+            raise ValueError(f"{path}: expected {key} at token {pos - 1}")
+
+    expect("DIMENSION")
+    dim = take(1, int)[0]
+    if dim not in (1, 2, 3):
+        raise ValueError(f"{path}: dimension {dim}")
+    expect("NODES")
+    nn, d2 = take(2, int)
+    if d2 != dim:
+        raise ValueError(f"{path}: node dimension {d2} != {dim}")
+    coord = np.array(take(nn * dim, float)).reshape(nn, dim).T
+    expect("CELLS")
+    nc = take(1, int)[0]
+    cells = np.array(take(nc * (dim + 2), int), dtype=np.int64).reshape(nc, dim + 2)
+    expect("FACES")
+    nf = take(1, int)[0]
+    faces = np.array(take(nf * (dim + 1), int), dtype=np.int64).reshape(nf, dim + 1)
+    expect("END")
+    for a in (cells[:, :dim + 1], faces[:, :dim]):
+        if a.size and (a.min() < 1 or a.max() > nn):
+            raise ValueError(f"{path}: node number out of range")
+    return Grid(coord, (cells[:, :dim + 1] - 1).T, cells[:, dim + 1], (faces[:, :dim] - 1).T, faces[:, dim])
+
+
+def write_sg(grid: Grid, path):
+    """Write a Grid as a SimplexGrid 2.1 text file (node numbers 1-based)."""
+    d = grid.dim
+    with open(path, "w") as f:
+        f.write(f"SimplexGrid {SG_VERSION}\n#written by voronoifvm.jl_gb300\nDIMENSION\n{d}\n")
+        f.write(f"NODES\n{grid.nnodes} {d}\n")
+        for k in range(grid.nnodes):
+            f.write(" ".join(repr(float(x)) for x in grid.coord[:, k]) + "\n")
+        f.write(f"CELLS\n{grid.ncells}\n")
+        for c in range(grid.ncells):
+            f.write(" ".join(str(int(i) + 1) for i in grid.cellnodes[:, c]) + f" {int(grid.cellregions[c])}\n")
+        f.write(f"FACES\n{grid.nbfaces}\n")
+        for b in range(grid.nbfaces):
+            f.write(" ".join(str(int(i) + 1) for i in grid.bfacenodes[:, b]) + f" {int(grid.bfaceregions[b])}\n")
+        f.write("END\n")
+
+
 def _as_coords(X):
     X = np.asarray(X, dtype=np.float64).ravel()
     if X.size < 2 or np.any(np.diff(X) <= 0):
@@ -98,7 +177,11 @@ def _as_coords(X):
 
 
 def simplexgrid(*axes) -> Grid:
-    """Create a 1D, 2D or 3D simplex grid from tensor-product coordinate vectors."""
+    """Create a 1D, 2D or 3D simplex grid from tensor-product coordinate vectors,
+    or read one from a SimplexGrid text file (``simplexgrid(path)``, as in
+    ``examples/Example203_CoordinateSystems.jl:105``)."""
+    if len(axes) == 1 and isinstance(axes[0], (str, os.PathLike)):
+        return read_sg(axes[0])
     if len(axes) == 1:
         return _grid1d(_as_coords(axes[0]))
     if len(axes) == 2:
