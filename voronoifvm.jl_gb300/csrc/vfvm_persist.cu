@@ -91,52 +91,6 @@ extern "C" int vfvm_batch_set_instance(vfvm_batch* b, int32_t inst, const double
   return VFVM_OK;
 }
 
-namespace {
-cudaError_t wait_legacy_stream(vfvm_batch* b);
-}
-
-extern "C" int vfvm_batch_load_device(vfvm_batch* b, const double* params_dev, int32_t nparams,
-                                      const double* nodedata_dev, int32_t nnodedata) {
-  if (!b) return VFVM_ERR_INPUT;
-  vfvm_ctx* c0 = b->ctx[0];
-  if (params_dev && (nparams < physics_nparams(c0->phys) || nparams < 1)) return VFVM_ERR_INPUT;
-  if (nodedata_dev && (nnodedata != c0->nnd || nnodedata < 1)) return VFVM_ERR_INPUT;
-  for (auto* c : b->ctx) {
-    if (params_dev && nparams != c->nparams) return VFVM_ERR_INPUT;  // the parameter count stays
-    if (nodedata_dev && !c->nodedata.own) return VFVM_ERR_INPUT;
-  }
-  VFVM_CUDA(wait_legacy_stream(b));
-  const size_t pb = (size_t)nparams * sizeof(double);
-  int64_t off = 0;
-  for (int i = 0; i < b->ninst; ++i) {
-    vfvm_ctx* c = b->ctx[i];
-    if (params_dev)
-      VFVM_CUDA(cudaMemcpyAsync(c->params.p, params_dev + (size_t)i * nparams, pb, cudaMemcpyDeviceToDevice, b->stream));
-    if (nodedata_dev) {
-      const size_t nb = (size_t)c->N * nnodedata;
-      VFVM_CUDA(cudaMemcpyAsync(c->nodedata.p, nodedata_dev + off, nb * sizeof(double), cudaMemcpyDeviceToDevice,
-                                b->stream));
-      off += (int64_t)nb;
-    }
-  }
-  b->desc_precision = -1;
-  if (SweepHost* h = b->sweep) {
-    // the sweep engine's packed copies have the same system-major layout: refill them in one copy each
-    const bool pfit = !params_dev || (size_t)b->ninst * pb == h->params.n;
-    const bool nfit = !nodedata_dev || (size_t)off * sizeof(double) == h->nodedata.n;
-    if (h->valid && pfit && nfit) {
-      if (params_dev)
-        VFVM_CUDA(cudaMemcpyAsync(h->params.p, params_dev, h->params.n, cudaMemcpyDeviceToDevice, b->stream));
-      if (nodedata_dev)
-        VFVM_CUDA(cudaMemcpyAsync(h->nodedata.p, nodedata_dev, h->nodedata.n, cudaMemcpyDeviceToDevice, b->stream));
-    } else {
-      h->valid = false;
-    }
-  }
-  VFVM_CUDA(cudaStreamSynchronize(b->stream));
-  return VFVM_OK;
-}
-
 extern "C" int vfvm_batch_info(vfvm_batch* b, int64_t out[7]) {
   if (!b || !out) return VFVM_ERR_INPUT;
   out[0] = b->ninst;
@@ -201,6 +155,48 @@ int batch_results(vfvm_batch* b, vfvm_history* hist, float ms, int32_t* from_gue
 }
 
 }  // namespace
+
+extern "C" int vfvm_batch_load_device(vfvm_batch* b, const double* params_dev, int32_t nparams,
+                                      const double* nodedata_dev, int32_t nnodedata) {
+  if (!b) return VFVM_ERR_INPUT;
+  vfvm_ctx* c0 = b->ctx[0];
+  if (params_dev && (nparams < physics_nparams(c0->phys) || nparams < 1)) return VFVM_ERR_INPUT;
+  if (nodedata_dev && (nnodedata != c0->nnd || nnodedata < 1)) return VFVM_ERR_INPUT;
+  for (auto* c : b->ctx) {
+    if (params_dev && nparams != c->nparams) return VFVM_ERR_INPUT;  // the parameter count stays
+    if (nodedata_dev && !c->nodedata.own) return VFVM_ERR_INPUT;
+  }
+  VFVM_CUDA(wait_legacy_stream(b));
+  const size_t pb = (size_t)nparams * sizeof(double);
+  int64_t off = 0;
+  for (int i = 0; i < b->ninst; ++i) {
+    vfvm_ctx* c = b->ctx[i];
+    if (params_dev)
+      VFVM_CUDA(cudaMemcpyAsync(c->params.p, params_dev + (size_t)i * nparams, pb, cudaMemcpyDeviceToDevice, b->stream));
+    if (nodedata_dev) {
+      const size_t nb = (size_t)c->N * nnodedata;
+      VFVM_CUDA(cudaMemcpyAsync(c->nodedata.p, nodedata_dev + off, nb * sizeof(double), cudaMemcpyDeviceToDevice,
+                                b->stream));
+      off += (int64_t)nb;
+    }
+  }
+  b->desc_precision = -1;
+  if (SweepHost* h = b->sweep) {
+    // the sweep engine's packed copies have the same system-major layout: refill them in one copy each
+    const bool pfit = !params_dev || (size_t)b->ninst * pb == h->params.n;
+    const bool nfit = !nodedata_dev || (size_t)off * sizeof(double) == h->nodedata.n;
+    if (h->valid && pfit && nfit) {
+      if (params_dev)
+        VFVM_CUDA(cudaMemcpyAsync(h->params.p, params_dev, h->params.n, cudaMemcpyDeviceToDevice, b->stream));
+      if (nodedata_dev)
+        VFVM_CUDA(cudaMemcpyAsync(h->nodedata.p, nodedata_dev, h->nodedata.n, cudaMemcpyDeviceToDevice, b->stream));
+    } else {
+      h->valid = false;
+    }
+  }
+  VFVM_CUDA(cudaStreamSynchronize(b->stream));
+  return VFVM_OK;
+}
 
 extern "C" int vfvm_batch_solve_device(vfvm_batch* b, const vfvm_control* ctl, const double* inival_dev,
                                        double* U_dev, double time, double tstep, double lambda, vfvm_history* hist) {
