@@ -2,7 +2,7 @@
 
 Run in the build container, where the reference checkout is readable:
 
-    python tests/golden/make_fixtures.py [/path/to/reference]
+    python tests/golden/make_fixtures.py /path/to/reference
 
 * ``reference_testvals.json``: the ``testval``/golden numbers of the reference
   examples and tests used to pin the oracle, read from the reference sources as
@@ -21,7 +21,7 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = None  # the reference checkout, the required command-line argument
 
 EXAMPLES = {
     "Example105_NonlinearPoisson1D": r"testval\s*=\s*([-0-9.e]+)",
@@ -66,6 +66,9 @@ def bernoulli_kat(stride=100):
 
 
 if __name__ == "__main__":
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_fixtures.py /path/to/reference")
+    REF = sys.argv[1]
     tv = testvals()
     with open(os.path.join(HERE, "reference_testvals.json"), "w") as f:
         json.dump(tv, f, indent=1, sort_keys=True)

@@ -64,6 +64,28 @@ def test_noalloc_matches_allocating_solve_twice(vfvm, oracle, torch):
         assert it == it_ref
 
 
+def test_noalloc_near_its_row_limit(vfvm, oracle, torch):
+    """A 362 x 362 grid (131044 rows, just below the limit of 131072) exercises
+    the fixed layout of the work array at nearly full size.  The matrix is an
+    implicit Euler Jacobian with a short time step, so Jacobi BiCGStab
+    converges quickly."""
+    lib = vfvm._lib.load()
+    g = vfvm.simplexgrid(lin(361), lin(361))
+    assert vfvm._lib.NOALLOC_MAX_ROWS - 64 < g.nnodes <= vfvm._lib.NOALLOC_MAX_ROWS
+    osys = oracle.OracleSystem(g, "porous")
+    rng = np.random.default_rng(5)
+    u = rng.uniform(0.2, 0.8, size=g.nnodes)
+    F, J = osys.assemble(u, rng.uniform(0.2, 0.8, size=g.nnodes), 0.0, 1e-6)
+    rc_ref, x_ref, it_ref = run(lib, "vfvm_linsolve_csr", torch, J, F)
+    rc, x, it = run(lib, "vfvm_linsolve_csr_noalloc", torch, J, F)
+    assert rc_ref == 0 and rc == 0
+    assert np.all(np.isfinite(x))
+    assert np.max(np.abs(x - x_ref)) <= TOL * np.max(np.abs(x_ref))
+    assert it == it_ref
+    # the solution solves the system
+    assert np.max(np.abs(J @ x - F)) <= 1e-9 * np.max(np.abs(F))
+
+
 def test_noalloc_rejects_oversized_system(vfvm, torch):
     lib = vfvm._lib.load()
     n = vfvm._lib.NOALLOC_MAX_ROWS + 1

@@ -5,10 +5,14 @@
 // LinearSolve algorithm chosen by control.method_linear
 // (src/vfvm_solvercontrol.jl:106).  vfvm_linsolve_csr is such an algorithm on the
 // device: left-Jacobi-preconditioned BiCGStab in one persistent cooperative launch.
+#include <mutex>
+
 #include "vfvm_krylov.cuh"
 #include "vfvm_linsolve.cuh"
 
 namespace vfvm {
+
+constexpr int kMaxGridDevices = 64;
 
 // Validates the CSR structure (row pointers inside [0, nnz], monotone, columns
 // inside [0, n)) and records the diagonal slot of every row.  err bit 1: bad
@@ -49,18 +53,28 @@ size_t linsolve_scratch_bytes(int64_t n, int grid) {
 }
 
 int linsolve_grid(int n) {
-  static int cached_dev = -1, cached_grid = 0;
+  // grid size per device ordinal, computed once; guarded because both CSR entry
+  // points are context-free and may be called from several host threads
+  static std::mutex mu;
+  static int cached[kMaxGridDevices] = {0};
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
-  if (dev != cached_dev) {
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 0;
+  int full = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < kMaxGridDevices) full = cached[dev];
+  }
+  if (full == 0) {
     int sms = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, linsolve_kernel<8>, kLinThreads, 0) != cudaSuccess) return 0;
-    cached_grid = sms * (per_sm < 2 ? per_sm : 2);
-    cached_dev = dev;
+    full = sms * (per_sm < 2 ? per_sm : 2);
+    if (full < 1) return 0;
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < kMaxGridDevices) cached[dev] = full;
   }
   const int need = (int)((n + kLinThreads - 1) / kLinThreads);
-  return need < cached_grid ? (need > 0 ? need : 1) : cached_grid;
+  return need < full ? (need > 0 ? need : 1) : full;
 }
 
 int linsolve_run(int32_t n, int64_t nnz, const int32_t* rowptr, const int32_t* colind, const double* vals,

@@ -14,7 +14,6 @@
 // calls whose work overlaps on the GPU (other host threads, other streams)
 // race on it and must be serialised by the caller.
 #include <cstdio>
-#include <mutex>
 #include "vfvm_linsolve.cuh"
 
 namespace vfvm {
@@ -33,27 +32,21 @@ constexpr size_t kNoallocBytes = a256(7 * (size_t)kNoallocMaxRows * sizeof(doubl
 static __device__ __align__(256) char g_noalloc_scratch[kNoallocBytes];
 
 namespace {
-constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-char* g_scratch_ptr[kMaxDevices] = {nullptr};
-
-// Device address of the work array on the current device; resolved once per
-// device, with that device current.
+// Device address of the work array in the CUDA context current on this thread.
+// It is looked up on every call rather than cached: a __device__ symbol's
+// address belongs to the context that loaded the module, and the context of a
+// device ordinal can change (cudaDeviceReset, a driver-API caller making its
+// own context current).  The lookup allocates nothing; the first one in a
+// context loads the module, which is why the first call should come before any
+// stream capture.
 int scratch_address(char** out) {
-  int dev = 0;
-  VFVM_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return VFVM_ERR_INPUT;
-  std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) {
-      fprintf(stderr, "vfvm_linsolve_csr_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
-      return VFVM_ERR_CUDA;
-    }
-    g_scratch_ptr[dev] = static_cast<char*>(p);
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "vfvm_linsolve_csr_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+    return VFVM_ERR_CUDA;
   }
-  *out = g_scratch_ptr[dev];
+  *out = static_cast<char*>(p);
   return VFVM_OK;
 }
 }  // namespace

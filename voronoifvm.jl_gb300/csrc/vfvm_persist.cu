@@ -251,9 +251,12 @@ extern "C" int vfvm_batch_solve(vfvm_batch* b, const vfvm_control* ctl, const do
 extern "C" int vfvm_batch_tune(vfvm_batch* b, const vfvm_control* ctl, const double* inival_dev, int32_t* best_ctas,
                                float* times_ms, int32_t ncand, const int32_t* candidates) {
   if (!b || !ctl || !inival_dev || ncand < 1 || !candidates) return VFVM_ERR_INPUT;
+  // a control no candidate can run (batched solves are BiCGStab only) is an
+  // input error, not "no candidate fits"
+  if (ctl->krylov != VFVM_KRYLOV_BICGSTAB) return VFVM_ERR_INPUT;
   const size_t n = (size_t)b->offsets[b->ninst];
   float best = 1e30f;
-  int bestc = candidates[0];
+  int bestc = -1, failed_rc = VFVM_ERR_INPUT;
   VFVM_CUDA(wait_legacy_stream(b));
   // the candidates are CTAs per system (team engine) or blocks per system (sweep
   // engine), passed as the control's team_ctas
@@ -267,8 +270,13 @@ extern "C" int vfvm_batch_tune(vfvm_batch* b, const vfvm_control* ctl, const dou
     if (rc == VFVM_ERR_INPUT) { if (times_ms) times_ms[k] = -1.0f; continue; }  // does not fit the device
     if (rc) return rc;
     if (times_ms) times_ms[k] = ms;
-    if (batch_results(b, nullptr, ms) == VFVM_OK && ms < best) { best = ms; bestc = candidates[k]; }
+    const int res = batch_results(b, nullptr, ms);
+    if (res != VFVM_OK) { failed_rc = res; continue; }
+    if (ms < best) { best = ms; bestc = candidates[k]; }
   }
+  // no candidate solved the batch: keep the previous setting and say why
+  // (VFVM_ERR_INPUT: none fits the device; otherwise the solve's own status)
+  if (bestc < 0) return failed_rc;
   b->tuned_ctas = bestc;
   b->tuned_engine = b->last_engine;
   if (best_ctas) *best_ctas = bestc;
