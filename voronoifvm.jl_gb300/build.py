@@ -28,8 +28,8 @@ def _nvcc():
 
 
 # The persistent engine's kernels are instantiated once per registered physics
-# from one source (vfvm_persist_inst.cu), each into its own object, so these
-# heavy instantiations compile in parallel.
+# and precision from one source (vfvm_persist_inst.cu), each pair into its own
+# object, so these heavy instantiations compile in parallel.
 INST_SOURCE = "vfvm_persist_inst.cu"
 INST_PHYSICS = ["PhysEx105", "PhysEx106", "PhysEx110", "PhysEx160", "PhysEx207", "PhysEx301", "PhysEx440",
                 "PhysLaplaceDir", "PhysNLPoisson", "PhysPorous", "PhysBipolar", "PhysRD2", "PhysKappaExp"]
@@ -44,7 +44,9 @@ def _units():
     units = [(s, os.path.join(BUILD, os.path.basename(s)[:-3] + ".o"), []) for s in sources()]
     inst = os.path.join(CSRC, INST_SOURCE)
     for ph in INST_PHYSICS:
-        units.append((inst, os.path.join(BUILD, f"vfvm_persist_inst_{ph}.o"), [f"-DVFVM_INST_PHYS=vfvm::{ph}"]))
+        for kt in ("double", "float"):
+            units.append((inst, os.path.join(BUILD, f"vfvm_persist_inst_{ph}_{kt}.o"),
+                          [f"-DVFVM_INST_PHYS=vfvm::{ph}", f"-DVFVM_INST_KT={kt}"]))
     return units
 
 

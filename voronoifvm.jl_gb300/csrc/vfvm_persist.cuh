@@ -1,7 +1,7 @@
 // Declarations of the persistent engine and batched solver templates.  Their
 // definitions (vfvm_persist_impl.cuh) are instantiated once per physics in
-// separate objects (vfvm_persist_inst.cu, compiled with -DVFVM_INST_PHYS=...) so
-// the heavy kernels build in parallel.
+// separate objects (vfvm_persist_inst.cu, compiled with -DVFVM_INST_PHYS=... and
+// -DVFVM_INST_KT=double|float) so the heavy kernels build in parallel.
 #pragma once
 #include <vector>
 #include "vfvm_solver.cuh"
@@ -61,9 +61,24 @@ struct vfvm_batch {
 };
 
 namespace vfvm {
+// one precision (KT = double: FP64 form, float: mixed form); instantiated per
+// (physics, precision) pair in vfvm_persist_inst.cu
+template <class Ph, typename KT>
+int persistent_solve_kt(vfvm_ctx* c, const vfvm_control* ctl, const PersistRunHost& run, vfvm_history* hist, float* ms);
+template <class Ph, typename KT>
+int batch_run_kt(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, double tstep, double lambda,
+                 const double* guess, const double* fallback, float* ms);
+
 template <class Ph>
-int persistent_solve_t(vfvm_ctx* c, const vfvm_control* ctl, const PersistRunHost& run, vfvm_history* hist, float* ms);
+int persistent_solve_t(vfvm_ctx* c, const vfvm_control* ctl, const PersistRunHost& run, vfvm_history* hist, float* ms) {
+  return ctl->precision == VFVM_PRECISION_FP64 ? persistent_solve_kt<Ph, double>(c, ctl, run, hist, ms)
+                                               : persistent_solve_kt<Ph, float>(c, ctl, run, hist, ms);
+}
 template <class Ph>
 int batch_run_t(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, double tstep, double lambda,
-                const double* guess, const double* fallback, float* ms);
+                const double* guess, const double* fallback, float* ms) {
+  return ctl->precision == VFVM_PRECISION_FP64
+             ? batch_run_kt<Ph, double>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms)
+             : batch_run_kt<Ph, float>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms);
+}
 }  // namespace vfvm

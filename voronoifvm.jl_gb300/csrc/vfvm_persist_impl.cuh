@@ -127,19 +127,13 @@ int persistent_launch(vfvm_ctx* c, const vfvm_control* ctl, const PersistRunHost
   return h.status;
 }
 
-template <class Ph>
-int persistent_solve_t(vfvm_ctx* c, const vfvm_control* ctl, const PersistRunHost& run, vfvm_history* hist, float* ms) {
-  const bool f64 = ctl->precision == VFVM_PRECISION_FP64;
+template <class Ph, typename KT>
+int persistent_solve_kt(vfvm_ctx* c, const vfvm_control* ctl, const PersistRunHost& run, vfvm_history* hist,
+                        float* ms) {
   switch (ctl->precon) {
-    case VFVM_PRECON_JACOBI:
-      return f64 ? persistent_launch<Ph, double, VFVM_PRECON_JACOBI>(c, ctl, run, hist, ms)
-                 : persistent_launch<Ph, float, VFVM_PRECON_JACOBI>(c, ctl, run, hist, ms);
-    case VFVM_PRECON_ILU0:
-      return f64 ? persistent_launch<Ph, double, VFVM_PRECON_ILU0>(c, ctl, run, hist, ms)
-                 : persistent_launch<Ph, float, VFVM_PRECON_ILU0>(c, ctl, run, hist, ms);
-    default:
-      return f64 ? persistent_launch<Ph, double, VFVM_PRECON_BLOCK_ILU0>(c, ctl, run, hist, ms)
-                 : persistent_launch<Ph, float, VFVM_PRECON_BLOCK_ILU0>(c, ctl, run, hist, ms);
+    case VFVM_PRECON_JACOBI: return persistent_launch<Ph, KT, VFVM_PRECON_JACOBI>(c, ctl, run, hist, ms);
+    case VFVM_PRECON_ILU0: return persistent_launch<Ph, KT, VFVM_PRECON_ILU0>(c, ctl, run, hist, ms);
+    default: return persistent_launch<Ph, KT, VFVM_PRECON_BLOCK_ILU0>(c, ctl, run, hist, ms);
   }
 }
 
@@ -566,37 +560,28 @@ int sweep_run(vfvm_batch* b, const vfvm_control* ctl, int bpi_req, double time, 
   return VFVM_OK;
 }
 
-template <class Ph>
-int batch_run_t(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, double tstep, double lambda,
-                const double* guess, const double* fallback, float* ms) {
+template <class Ph, typename KT>
+int batch_run_kt(vfvm_batch* b, const vfvm_control* ctl, int ctas, double time, double tstep, double lambda,
+                 const double* guess, const double* fallback, float* ms) {
   // shared-grid batches with ILU0 run on the sweep engine unless the persistent engine is asked for
   if (b->shared_grid && ctl->precon == VFVM_PRECON_ILU0 && ctl->engine != VFVM_ENGINE_PERSISTENT &&
       !b->ctx[0]->has_legacy && !b->ctx[0]->multireg) {
     // blocks per system: the control's team_ctas, else the autotuned value, else automatic
     const int bpi = ctl->team_ctas > 0 ? ctas : b->tuned_engine == 1 ? b->tuned_ctas : 0;
-    return ctl->precision == VFVM_PRECISION_FP64
-               ? sweep_run<Ph, double>(b, ctl, bpi, time, tstep, lambda, guess, fallback, ms)
-               : sweep_run<Ph, float>(b, ctl, bpi, time, tstep, lambda, guess, fallback, ms);
+    return sweep_run<Ph, KT>(b, ctl, bpi, time, tstep, lambda, guess, fallback, ms);
   }
   b->last_engine = 0;
   b->last_launches = 1;
-  const bool f64 = ctl->precision == VFVM_PRECISION_FP64;
-  const bool jac = ctl->precon == VFVM_PRECON_JACOBI;
   const int coarse = ctl->precon == VFVM_PRECON_JACOBI ? 0 : ctl->coarse;
-  int rc = f64 ? batch_prepare<Ph, double>(b, ctl->precision, coarse)
-               : batch_prepare<Ph, float>(b, ctl->precision, coarse);
+  int rc = batch_prepare<Ph, KT>(b, ctl->precision, coarse);
   if (rc) return rc;
-  (void)jac;
   switch (ctl->precon) {
     case VFVM_PRECON_JACOBI:
-      return f64 ? batch_launch<Ph, double, VFVM_PRECON_JACOBI>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms)
-                 : batch_launch<Ph, float, VFVM_PRECON_JACOBI>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms);
+      return batch_launch<Ph, KT, VFVM_PRECON_JACOBI>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms);
     case VFVM_PRECON_ILU0:
-      return f64 ? batch_launch<Ph, double, VFVM_PRECON_ILU0>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms)
-                 : batch_launch<Ph, float, VFVM_PRECON_ILU0>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms);
+      return batch_launch<Ph, KT, VFVM_PRECON_ILU0>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms);
     default:
-      return f64 ? batch_launch<Ph, double, VFVM_PRECON_BLOCK_ILU0>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms)
-                 : batch_launch<Ph, float, VFVM_PRECON_BLOCK_ILU0>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms);
+      return batch_launch<Ph, KT, VFVM_PRECON_BLOCK_ILU0>(b, ctl, ctas, time, tstep, lambda, guess, fallback, ms);
   }
 }
 

@@ -1,15 +1,16 @@
 // Explicit instantiation of the persistent engine and batched solver for one
-// physics, selected at compile time with -DVFVM_INST_PHYS=<functor type>
-// (build.py compiles this file once per registered physics, in parallel).
+// physics and one precision, selected at compile time with
+// -DVFVM_INST_PHYS=<functor type> -DVFVM_INST_KT=<double|float> (build.py
+// compiles this file once per pair, in parallel).
 #include "vfvm_persist_impl.cuh"
 
-#ifndef VFVM_INST_PHYS
-#error "compile with -DVFVM_INST_PHYS=vfvm::Phys..."
+#if !defined(VFVM_INST_PHYS) || !defined(VFVM_INST_KT)
+#error "compile with -DVFVM_INST_PHYS=vfvm::Phys... -DVFVM_INST_KT=double|float"
 #endif
 
 namespace vfvm {
-template int persistent_solve_t<VFVM_INST_PHYS>(vfvm_ctx*, const vfvm_control*, const PersistRunHost&, vfvm_history*,
-                                                float*);
-template int batch_run_t<VFVM_INST_PHYS>(vfvm_batch*, const vfvm_control*, int, double, double, double, const double*,
-                                         const double*, float*);
+template int persistent_solve_kt<VFVM_INST_PHYS, VFVM_INST_KT>(vfvm_ctx*, const vfvm_control*, const PersistRunHost&,
+                                                               vfvm_history*, float*);
+template int batch_run_kt<VFVM_INST_PHYS, VFVM_INST_KT>(vfvm_batch*, const vfvm_control*, int, double, double, double,
+                                                        const double*, const double*, float*);
 }  // namespace vfvm
