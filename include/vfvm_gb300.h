@@ -1,8 +1,8 @@
 /*
  * vfvm_gb300.h -- C ABI of the GB300-native assembly + Newton library.
  *
- * This is the boundary a VoronoiFVM.jl shim binds with `ccall` (see
- * INTEGRATION.md).  Each entry point replaces one piece of the reference's
+ * This is the boundary a VoronoiFVM.jl shim binds with `ccall`.  Each entry
+ * point replaces one piece of the reference's
  * hot path (paths relative to the VoronoiFVM.jl project):
  *
  *   vfvm_create            SystemState(sys) + update_grid_edgewise!
@@ -260,7 +260,10 @@ int vfvm_batch_solve_guarded_device(vfvm_batch* batch, const vfvm_control* contr
 /* Autotuner: times the batch from inival_dev (device) for each candidate -- CTAs
  * per system on the CTA-team engine, blocks per system on the sweep engine --
  * keeps the fastest for later solves of this batch and reports it in
- * *best_ctas; times_ms[k] = -1 for candidates that do not fit. */
+ * *best_ctas; times_ms[k] = -1 for candidates that do not fit.  Returns
+ * VFVM_ERR_INPUT for a control batched solves do not run (GMRES) or when no
+ * candidate fits, and the solve's status when none converged; the previous
+ * setting is kept in both cases. */
 int vfvm_batch_tune(vfvm_batch* batch, const vfvm_control* control, const double* inival_dev, int32_t* best_ctas,
                     float* times_ms, int32_t ncand, const int32_t* candidates);
 
@@ -285,14 +288,24 @@ int vfvm_linsolve_csr(int32_t n, int64_t nnz, const int32_t* rowptr, const int32
  * b and x as for vfvm_linsolve_csr; the work vectors live in a fixed
  * file-scope device array (about 7.7 MB, held by every GPU that loads the
  * library until exit), which limits n to VFVM_NOALLOC_MAX_ROWS rows: larger
- * systems return VFVM_ERR_NOALLOC_LIMIT.  The first call on a device looks up
- * the array's device address (once per device), so make that first call before
- * any stream capture.  All calls share the array: calls that overlap on the GPU
- * race on it and must be serialised by the caller. */
+ * systems return VFVM_ERR_NOALLOC_LIMIT.  Every call looks up the array's
+ * address in the current CUDA context (no allocation); the first call in a
+ * context also loads the library's device code there, so make that first call
+ * before any stream capture.  All calls share the array: calls that overlap on
+ * the GPU race on it and must be serialised by the caller. */
 #define VFVM_NOALLOC_MAX_ROWS 131072
 int vfvm_linsolve_csr_noalloc(int32_t n, int64_t nnz, const int32_t* rowptr, const int32_t* colind,
                               const double* vals, const double* b, double* x, double reltol, double abstol,
                               int32_t maxiters, int32_t* iters, double* resnorm);
+
+/* Self-check of the bounded device waits behind VFVM_ERR_TIMEOUT (the
+ * reference maps solver failures to exceptions, src/vfvm_logging_exceptions.jl:6-29;
+ * a device wait that never ends has no counterpart there).  Runs the team
+ * barrier of the persistent solvers in `ctas` CTAs told to expect one CTA more,
+ * so every wait must give up after its spin limit (about a second): on return
+ * *wait_status is VFVM_ERR_TIMEOUT when the limit worked, *ms (optional) the
+ * kernel's duration.  The CUDA context stays usable; nothing traps or faults. */
+int vfvm_check_bounded_wait(int32_t ctas, int32_t* wait_status, float* ms);
 
 /* ---- learned initial iterate: a small multilayer perceptron ----
  * There is no counterpart in the reference: the network predicts a coarse
