@@ -354,6 +354,18 @@ METRIC_L = ("Newton solves/s at ||F||<=1e-10 (stationary -div(kappa grad u) + ex
             "512 held-out GRF instances): learned+mixed+batched form")
 
 
+# DRAM bytes (read + write) of one BiCGStab iteration of the sweep engine per
+# system, from an ncu capture of every kernel of one iteration with all 512
+# systems active (kappa-exp 257 x 257, mixed form); None until measured.
+SWEEP_DRAM_BYTES_PER_SYSTEM_ITERATION = None
+
+
+def heldout_seeds(rank):
+    """Held-out instance seeds of a rank: disjoint blocks of NEVAL per rank, so
+    replicas on several GPUs solve different instances."""
+    return np.arange(EVAL_SEED0 + rank * NEVAL, EVAL_SEED0 + (rank + 1) * NEVAL)
+
+
 MAXITERS_LINEAR = 50   # BiCGStab iterations per Newton step in the batched forms (inexact Newton)
 MAXITERS_SINGLE = 300  # one system at a time: the faster cap for those forms
 
@@ -399,43 +411,162 @@ def kappa_instances(lk, n, seeds):
 
 
 def batch_bytes(info, hist, ncoarse, jbytes=4, vbytes=4):
-    """Algorithmic bytes of a batched solve: per Newton step one assembly, the
-    ILU0 factorisation and the Galerkin product; per BiCGStab iteration two
-    SpMVs, two ILU0 applications, two coarse corrections and the vector updates
-    (each array touched once per use; index arrays counted, L2 reuse not)."""
+    """Algorithmic bytes of a batched solve on one shared grid.
+
+    Per system: per Newton step one assembly, the ILU0 factorisation and the
+    Galerkin product; per BiCGStab iteration two SpMVs, two ILU0 applications,
+    two coarse corrections and the vector updates -- the value arrays, each
+    touched once per use.  The index tables (ELL columns, ILU0 couplings,
+    aggregates, edge table) are shared by all systems: they are counted once per
+    iteration of the batched loop (as many Newton rounds and BiCGStab rounds as
+    the slowest system takes), not once per system.  Returns (total, per-system
+    part, shared part)."""
     N, E, nnzb = info["nnodes"], info["nedges"], info["nblocks"]
     n = N  # one species
-    asm = algorithmic_assembly_bytes(N, E, nnzb, 1, False, jbytes)
-    factor = nnzb * (jbytes + vbytes + 4) + N * vbytes
-    galerkin = nnzb * (jbytes + 8) + ncoarse * ncoarse * 4
-    newton = asm + factor + galerkin + 4 * n * 8  # + F -> b, update of U
-    spmv = nnzb * (vbytes + 4) + (N + 1) * 4 + 2 * n * vbytes
-    ilu = nnzb * (vbytes + 4) + N * 4 + 3 * n * vbytes
-    coarse = n * (4 + vbytes) + n * 2 * vbytes + ncoarse * ncoarse * 4
+    # per-system value bytes
+    asm = N * (8 + 8 + 8) + jbytes * nnzb            # node factor, U, F; Jacobian values
+    factor = nnzb * (jbytes + vbytes) + N * vbytes     # read J, write the ILU0 factors, inverted diagonal
+    galerkin = nnzb * jbytes + ncoarse * ncoarse * 4
+    newton = asm + factor + galerkin + 4 * n * 8       # + F -> b, update of U
+    spmv = nnzb * vbytes + 2 * n * vbytes
+    ilu = nnzb * vbytes + 3 * n * vbytes
+    coarse = n * vbytes + n * 2 * vbytes + ncoarse * ncoarse * 4
     vec = (4 + 3 + 7 + 2 + 2) * n * vbytes
     it = 2 * spmv + 2 * ilu + 2 * coarse + vec
-    return sum(h.nnewton * newton + h.nlin * it for h in hist)
+    per_system = sum(h.nnewton * newton + h.nlin * it for h in hist)
+    # shared index tables, once per round of the batched loop
+    idx_newton = E * (2 * 4 + 8) + nnzb * 4 * 3 + N * 4 * 2  # edge table; ELL/ILU0 slot tables; aggregates
+    idx_iter = 2 * (nnzb * 4 + (N + 1) * 4) + 2 * (nnzb * 4 + N * 4) + 2 * n * 4
+    rounds_newton = max(h.nnewton for h in hist)
+    rounds_iter = max(h.nlin for h in hist)
+    shared = rounds_newton * idx_newton + rounds_iter * idx_iter
+    return per_system + shared, per_system, shared
 
 
-def cpu_leg_learned(vfvm, nsolves, logk, f):
-    """CPU restatement of the reference path (C++ assembly + SuperLU) on the
-    first `nsolves` held-out instances, from inival 0, same stopping rule."""
+def _oracle_instance(seed):
+    """Worker: one held-out instance solved by the CPU restatement of the
+    reference path (C++ assembly + SuperLU) from inival 0 with the benchmark's
+    stopping rule; returns (seconds, solution)."""
+    import __graft_entry__ as ge
+    vfvm = ge.load_package()
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
+    logk, f = vfvm.learned.kappa_instance(LN, seed)
     x = np.linspace(0.0, 1.0, LN)
     g = vfvm.simplexgrid(x, x)
     c = O.Control()
     c.updatecontrol = False
     c.abstol = FTOL_L
     c.reltol = 0.0
-    sols, secs = [], 0.0
-    for i in range(nsolves):
-        osys = O.OracleSystem(g, "kappa_exp", [float(f[i])], nodedata=np.exp(logk[i]))
-        t0 = time.perf_counter()
-        u, _ = O.solve_step(osys, np.zeros(g.nnodes), c)
-        secs += time.perf_counter() - t0
-        sols.append(u)
-    return nsolves / secs, secs, sols
+    t0 = time.perf_counter()
+    osys = O.OracleSystem(g, "kappa_exp", [float(f)], nodedata=np.exp(logk))
+    u, _ = O.solve_step(osys, np.zeros(g.nnodes), c)
+    return time.perf_counter() - t0, u
+
+
+def _oracle_instance_solve(seed):
+    """Worker of the reference arm: seconds of one held-out instance's solve."""
+    return _oracle_instance(seed)[0]
+
+
+def oracle_pool(cores):
+    """Process pool for the oracle legs.  The `spawn` start method keeps it safe
+    to create after CUDA is initialised in this process."""
+    import multiprocessing as mp
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    return mp.get_context("spawn").Pool(cores)
+
+
+def cpu_leg_learned(pool, cores, seeds):
+    """CPU restatement of the reference path on `seeds` (held-out instances),
+    one instance per process on `cores` host cores: (solves/s, wall seconds,
+    solutions)."""
+    t0 = time.perf_counter()
+    out = pool.map(_oracle_instance, [int(s) for s in seeds])
+    wall = time.perf_counter() - t0
+    return len(seeds) / wall, wall, [u for _, u in out]
+
+
+def time_assembly(vfvm, lib, sysm, U, Uold, tstep, lam, flush, steps, warmup):
+    """Mean CUDA-event time (ms) of one assembly launch on the context stream
+    for the mixed (FP32 Jacobian) and FP64 forms with the edge-once tile kernel,
+    and for the mixed form with the node-centric kernel (every edge evaluated
+    from both ends; VFVM_ASSEMBLY_KERNEL=node), L2 flushed before each launch."""
+    import ctypes
+    import torch
+    stream = torch.cuda.ExternalStream(lib.vfvm_stream(sysm.ctx))
+    F = torch.empty_like(U)
+    out = {}
+    for form, prec in (("mixed", 1), ("fp64", 0), ("mixed_node_kernel", 1)):
+        if form == "mixed_node_kernel":
+            os.environ["VFVM_ASSEMBLY_KERNEL"] = "node"
+        times = []
+        for it in range(warmup + steps):
+            flush.fill_(float(it))
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rc = lib.vfvm_assemble_device(sysm.ctx, ctypes.c_void_p(U.data_ptr()), ctypes.c_void_p(Uold.data_ptr()),
+                                          0.0, tstep, lam, ctypes.c_void_p(F.data_ptr()), prec)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if rc != 0:
+                raise RuntimeError(f"vfvm_assemble_device failed: {rc}")
+            if it >= warmup:
+                times.append(e0.elapsed_time(e1))
+        out[form] = float(np.mean(times))
+        os.environ.pop("VFVM_ASSEMBLY_KERNEL", None)
+    return out
+
+
+def assembly_records(vfvm, flush, steps, warmup):
+    """Assembly alone on the grids of configuration 2 (porous medium, 513 x 513,
+    one transient assembly) and configuration 3 (bipolar drift-diffusion, 64^3
+    points, 3 species, embedding 0.5): time per launch and fraction of the
+    measured HBM bandwidth on the algorithmic bytes."""
+    import torch
+    lib = vfvm._lib.load()
+    peak, peak_kind = peaks()
+    recs = {}
+    # configuration 2
+    g, u0 = workload(vfvm, NX)
+    sysm = vfvm.System(g, vfvm.Physics("porous"))
+    info = sysm.info()
+    U = torch.from_numpy(u0).cuda()
+    t = time_assembly(vfvm, lib, sysm, U, U.clone(), DT, 0.0, flush, steps, warmup)
+    rec = {"grid": f"{NX}x{NX} triangles", "nodes": info["nnodes"], "edges": info["nedges"], "nnz": info["nnz"]}
+    for form, jb in (("mixed", 4), ("fp64", 8), ("mixed_node_kernel", 4)):
+        B = algorithmic_assembly_bytes(info["nnodes"], info["nedges"], info["nnz"], 1, True, jb)
+        rec[form] = {"ms": t[form], "algorithmic_bytes": B, "achieved_gbs": B / (t[form] * 1e-3) / 1e9,
+                     "frac": B / (t[form] * 1e-3) / 1e9 / peak}
+    recs["porous_513"] = rec
+    sysm.close()
+    # configuration 3
+    X = np.linspace(0.0, 1.0, 64)
+    g = vfvm.simplexgrid(X, X, X)
+    params = [1.0, 1.0, 1.0, 1.0, 1.0, 1.0e3, 0.5]
+    sysm = vfvm.System(g, vfvm.Physics("bipolar", params), species=[1, 2, 3])
+    info = sysm.info()
+    C = np.where(g.coord[0] < 0.5, params[5], -params[5])
+    nn = 0.5 * C + np.sqrt(0.25 * C * C + 1.0)
+    u = np.asfortranarray(np.stack([np.arcsinh(0.5 * C), nn, 1.0 / nn])).ravel(order="F")
+    U = torch.from_numpy(u).cuda()
+    t = time_assembly(vfvm, lib, sysm, U, U, math.inf, 0.5, flush, steps, warmup)
+    rec = {"grid": "64^3 points, tetrahedra", "nodes": info["nnodes"], "edges": info["nedges"], "nnz": info["nnz"],
+           "species": 3}
+    for form, jb in (("mixed", 4), ("fp64", 8), ("mixed_node_kernel", 4)):
+        B = algorithmic_assembly_bytes(info["nnodes"], info["nedges"], info["nnz"], 3, False, jb)
+        rec[form] = {"ms": t[form], "algorithmic_bytes": B, "achieved_gbs": B / (t[form] * 1e-3) / 1e9,
+                     "frac": B / (t[form] * 1e-3) / 1e9 / peak}
+    recs["bipolar_64cubed"] = rec
+    sysm.close()
+    recs["peak_gbs"] = peak
+    recs["peak_kind"] = peak_kind
+    recs["l2"] = "flushed (512 MB write) before each launch"
+    return recs
 
 
 def run_learned(args, rank, world):
@@ -475,7 +606,8 @@ def run_learned(args, rank, world):
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t_train
     # --- held-out set
-    logk_e, f_e = kappa_instances(lk, LN, np.arange(EVAL_SEED0, EVAL_SEED0 + NEVAL))
+    eval_seeds = heldout_seeds(rank)
+    logk_e, f_e = kappa_instances(lk, LN, eval_seeds)
     sweep.load(logk_e, f_e)
     Xe = torch.from_numpy(model.features(logk_e, f_e)).to(cuda)
     Se = torch.from_numpy(lk.kappa_scale(f_e)).to(cuda)
@@ -544,7 +676,7 @@ def run_learned(args, rank, world):
     for name in ("plain", "single_coarse"):
         ctl = learned_control(vfvm, name)
         vfvm.solve(single, inival=0.0, control=ctl)  # warm-up: graph build
-        nn, nl, secs = [], [], 0.0
+        nn, nl, secs, dev_s = [], [], 0.0, 0.0
         for i in range(args.single_sample):
             single.physics.data = [float(f_e[i])]
             single.physics.nodedata = np.exp(logk_e[i])
@@ -553,10 +685,14 @@ def run_learned(args, rank, world):
             vfvm.solve(single, inival=0.0, control=ctl)
             secs += time.perf_counter() - t0
             h = vfvm.solve.last_history
+            dev_s += h.time  # the solve's own CUDA-event time on the device
             nn.append(h.nnewton)
             nl.append(h.nlin)
-        forms[name] = dict(solves_per_s=args.single_sample / secs, newton_per_solve=float(np.mean(nn)),
-                           krylov_per_solve=float(np.mean(nl)), sample=args.single_sample)
+        # solves_per_s: device clock (CUDA events around the device solve, as `value`);
+        # host_solves_per_s: wall clock through solve() with its host<->device copies
+        forms[name] = dict(solves_per_s=args.single_sample / dev_s, host_solves_per_s=args.single_sample / secs,
+                           newton_per_solve=float(np.mean(nn)), krylov_per_solve=float(np.mean(nl)),
+                           sample=args.single_sample)
     # --- e2e through the public API with host buffers: the user's inputs are the
     # node data kappa = exp(G), the sources f and inival in pinned host memory;
     # per step: features (log kappa at the coarse subgrid nodes) on the host,
@@ -570,7 +706,7 @@ def run_learned(args, rank, world):
     ini_d = torch.empty_like(inival_h, device=cuda)
     kappa_np, f_np = kappa_h.numpy(), f_h.numpy()
     e2e, phases = [], []
-    for it in range(args.warmup + max(1, min(args.steps, 3))):
+    for it in range(args.warmup + max(1, args.steps)):
         flush.fill_(float(it))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -600,8 +736,10 @@ def run_learned(args, rank, world):
     # --- roofline of the dominant kernel (the batched Newton launch)
     peak, peak_kind = peaks()
     info = sweep.systems[0].info()
-    B = batch_bytes(info, hist_l, COARSE)
+    B, B_sys, B_shared = batch_bytes(info, hist_l, COARSE)
     achieved = B / (kernel_ms * 1e-3) / 1e9
+    sys_iters = int(sum(h.nlin for h in hist_l))
+    traffic = SWEEP_DRAM_BYTES_PER_SYSTEM_ITERATION * sys_iters if SWEEP_DRAM_BYTES_PER_SYSTEM_ITERATION else None
     # `forms` are per GPU; `value` and `e2e` are whole-job (replicas: all ranks' solves / slowest rank)
     value = replica_throughput(len(ok_l), ms_l * 1e-3, world)
     line = {
@@ -626,40 +764,32 @@ def run_learned(args, rank, world):
         "roofline": {"kernel": "batched Newton solve (sweep engine: one CUDA graph of whole-GPU kernels over all "
                                "instances: assembly, ILU0, coarse stage, BiCGStab)",
                      "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes": B, "ms_per_launch": kernel_ms},
+                     "peak_kind": peak_kind, "traffic": traffic, "algorithmic_bytes": B,
+                     "algorithmic_bytes_per_system": B_sys, "algorithmic_bytes_shared_tables": B_shared,
+                     "system_iterations": sys_iters, "ms_per_launch": kernel_ms,
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one BiCGStab iteration with "
+                                       "all 512 systems active (ncu), per system-iteration, times the system-iterations "
+                                       "of this solve" if traffic else None},
         "gpu_launches": int(args.steps * launches_per_step),
         "clocks": clocks,
     }
+    line["assembly"] = assembly_records(vfvm, flush, 20, args.warmup)
     if rank == 0 and not args.no_cpu:
-        sps, secs, osols = cpu_leg_learned(vfvm, args.cpu_solves, logk_e, f_e)
-        line["cpu_baseline"] = {"value": sps, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": f"{args.cpu_solves} held-out instance(s) from inival 0 (C++ assembly "
-                                          f"restatement + SuperLU), {secs:.1f} s"}
-        err = max(float(np.max(np.abs(U_learned[i] - u)) / np.max(np.abs(u))) for i, u in enumerate(osols))
-        line["max_rel_err_vs_oracle"] = err
+        cores = os.cpu_count() or 1
+        nchk = min(args.oracle_check, NEVAL)
+        with oracle_pool(cores) as pool:
+            sps, secs, osols = cpu_leg_learned(pool, cores, eval_seeds[:nchk])
+        line["cpu_baseline"] = {"value": sps, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"{nchk} held-out instances from inival 0, one process per core (C++ "
+                                          f"assembly restatement + SuperLU), {secs:.1f} s wall"}
+        errs = np.array([float(np.max(np.abs(U_learned[i] - u)) / np.max(np.abs(u))) for i, u in enumerate(osols)])
+        line["max_rel_err_vs_oracle"] = float(errs.max())
+        line["oracle_check"] = {"instances": int(nchk), "max_rel_err": float(errs.max()),
+                                "median_rel_err": float(np.median(errs)), "tolerance": 1e-8,
+                                "all_within": bool(np.all(errs <= 1e-8))}
     if rank == 0:
         print(json.dumps(line))
     return line
-
-
-def _oracle_instance_solve(seed):
-    """Worker of the reference arm: one held-out instance solved by the CPU
-    restatement (C++ assembly + SuperLU) from inival 0; returns seconds."""
-    import __graft_entry__ as ge
-    vfvm = ge.load_package()
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    logk, f = vfvm.learned.kappa_instance(LN, seed)
-    x = np.linspace(0.0, 1.0, LN)
-    g = vfvm.simplexgrid(x, x)
-    c = O.Control()
-    c.updatecontrol = False
-    c.abstol = FTOL_L
-    c.reltol = 0.0
-    t0 = time.perf_counter()
-    osys = O.OracleSystem(g, "kappa_exp", [float(f)], nodedata=np.exp(logk))
-    O.solve_step(osys, np.zeros(g.nnodes), c)
-    return time.perf_counter() - t0
 
 
 def run_reference_learned(args, rank, world):
@@ -852,6 +982,7 @@ def main():
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--nsteps", type=int, default=NSTEPS)
     ap.add_argument("--cpu-solves", type=int, default=3)
+    ap.add_argument("--oracle-check", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--engine", choices=["persistent", "graph"], default="graph")
     ap.add_argument("--precon", choices=["ilu0", "jacobi", "block_ilu0"], default=PRECON)

@@ -48,3 +48,30 @@ def test_replica_throughput_one_rank():
     sys.path.insert(0, ROOT)
     import bench
     assert bench.replica_throughput(512, 0.5, 1) == 1024.0
+
+
+def test_heldout_seeds_are_disjoint_across_ranks():
+    """Each replica solves its own block of held-out instances: the work is
+    sharded, not repeated, and no rank's block overlaps the training seeds."""
+    sys.path.insert(0, ROOT)
+    import bench
+    blocks = [set(bench.heldout_seeds(r).tolist()) for r in range(8)]
+    for r, b in enumerate(blocks):
+        assert len(b) == bench.NEVAL
+        assert min(b) >= bench.NTRAIN
+        for q in range(r):
+            assert not (b & blocks[q])
+
+
+def test_batch_bytes_counts_shared_tables_once():
+    """The index tables of the shared grid are charged once per round of the
+    batched loop, so doubling the systems doubles only the per-system part."""
+    sys.path.insert(0, ROOT)
+    import types
+    import bench
+    info = {"nnodes": 66049, "nedges": 197120, "nblocks": 460289}
+    h = [types.SimpleNamespace(nnewton=3, nlin=90 + i % 7) for i in range(8)]
+    tot1, sys1, sh1 = bench.batch_bytes(info, h, 196)
+    tot2, sys2, sh2 = bench.batch_bytes(info, h + h, 196)
+    assert tot1 == sys1 + sh1 and tot2 == sys2 + sh2
+    assert sys2 == 2 * sys1 and sh2 == sh1
