@@ -1,4 +1,5 @@
-"""GPU assembly parity against the oracle, through the C ABI.
+"""GPU assembly parity against the oracle, through the C ABI, for both assembly
+kernels (edge-once over node tiles, and node-centric).
 
 * pattern: bit-exact against the entries the reference creates (the oracle's
   _addnz flags, unioned over several states as ExtendableSparse keeps them);
@@ -28,8 +29,13 @@ def make_pair(vfvm, oracle, c):
     return sys, osys
 
 
+@pytest.mark.parametrize("kernel", ["tile", "node"])
 @pytest.mark.parametrize("name", NAMES)
-def test_assembly_parity(vfvm, oracle, name):
+def test_assembly_parity(vfvm, oracle, name, kernel, monkeypatch):
+    # tile: the edge-once kernel over shared-memory node tiles (the default);
+    # node: the node-centric kernel (multi-region grids; selectable for comparison)
+    if kernel == "node":
+        monkeypatch.setenv("VFVM_ASSEMBLY_KERNEL", "node")
     c = case(vfvm, name)
     sys, osys = make_pair(vfvm, oracle, c)
     rng = np.random.default_rng(42)

@@ -12,25 +12,22 @@
 
 namespace vfvm {
 
+// NaN test on the bit pattern (integer instructions; keeps the check off the
+// FP64 pipe, which GB300 runs at a small fraction of the FP32 rate)
+__device__ __forceinline__ bool nan_bits(double x) {
+  return (__double_as_longlong(x) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+}
+__device__ __forceinline__ bool nan_bits(float x) { return (__float_as_uint(x) & 0x7fffffffu) > 0x7f800000u; }
+
+// Node terms of K: reaction - source + (storage - oldstorage)/tstep
+// (src/vfvm_assembly.jl:38-126), added to fK and the diagonal block jd.
 template <class Ph, typename P, bool MR>
-__device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, int K, const double* __restrict__ U,
-                                              const double* __restrict__ Uold, double time, double tstepinv,
-                                              double lambda, double* __restrict__ F, P* __restrict__ J) {
+__device__ __forceinline__ void node_terms(const AsmTables& t, const Ph& ph, int K, const double* uK, const P* uKs,
+                                           const double* __restrict__ Uold, double time, double tstepinv,
+                                           double lambda, double* fK, P* jd) {
   constexpr int NS = Ph::NS;
-  double uK[NS];
-  P uKs[NS];  // the values in the partials' precision, converted once per node
-#pragma unroll
-  for (int i = 0; i < NS; ++i) { uK[i] = U[(size_t)K * NS + i]; uKs[i] = P(uK[i]); }
-  double fK[NS];
-  P jd[NS * NS];
-#pragma unroll
-  for (int i = 0; i < NS; ++i) fK[i] = 0.0;
-#pragma unroll
-  for (int i = 0; i < NS * NS; ++i) jd[i] = P(0);
   const double* xK = t.coord + (size_t)K * t.dim;
   const double* dK = t.nodedata ? t.nodedata + (size_t)K * t.nnd : nullptr;
-
-  // ---- node terms: reaction - source + (storage - oldstorage)/tstep
   const int nbeg = MR ? t.nitem_ptr[K] : 0, nend = MR ? t.nitem_ptr[K + 1] : 1;
   for (int it = nbeg; it < nend; ++it) {
     const int reg = MR ? t.nitem_reg[it] : t.region;
@@ -59,6 +56,68 @@ __device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, 
       for (int j = 0; j < NS; ++j) jd[i * NS + j] += (r[i].d[j] + s[i].d[j] * tip) * facp;
     }
   }
+}
+
+// Boundary-face items of K in bface order: legacy Dirichlet/Robin data
+// (src/vfvm_assembly.jl:355-387) and breaction (src/vfvm_assembly.jl:388-407).
+template <class Ph, typename P>
+__device__ __forceinline__ void bnode_terms(const AsmTables& t, const Ph& ph, int K, const double* uK, const P* uKs,
+                                            double time, double lambda, double* fK, P* jd) {
+  constexpr int NS = Ph::NS;
+  const double* xK = t.coord + (size_t)K * t.dim;
+  const int bbeg = t.bn_ptr[K], bend = t.bn_ptr[K + 1];
+  for (int it = bbeg; it < bend; ++it) {
+    const int reg = t.bn_reg[it];
+    const double fac = t.bn_fac[it];
+    double Dir = kDirichlet;
+    if (t.has_legacy && reg - 1 < t.nbregions) {
+      Dir = kDirichlet / fac;
+#pragma unroll
+      for (int i = 0; i < NS; ++i) {
+        const double bf = t.bfactors[i + NS * (reg - 1)], bv = t.bvalues[i + NS * (reg - 1)];
+        if (bf == kDirichlet) {
+          fK[i] += bf * (uK[i] - bv);
+          jd[i * NS + i] += P(bf);
+        } else {
+          fK[i] += fac * (bf * uK[i] - bv);
+          if (bf != 0.0) jd[i * NS + i] += P(bf) * P(fac);
+        }
+      }
+    }
+    if (Ph::has_breaction) {
+      BNodeItem bi{K, reg, xK, time, lambda, fac, Dir, nullptr};
+      Dual<NS, P> u[NS], y[NS];
+#pragma unroll
+      for (int i = 0; i < NS; ++i) { u[i] = dseed<NS, P>(uK[i], uKs[i], i); y[i] = dconst<NS, P>(0.0); }
+      ph.breaction(y, u, bi);
+      const P facp = P(fac);
+#pragma unroll
+      for (int i = 0; i < NS; ++i) {
+        fK[i] += fac * y[i].v;
+#pragma unroll
+        for (int j = 0; j < NS; ++j) jd[i * NS + j] += y[i].d[j] * facp;
+      }
+    }
+  }
+}
+
+template <class Ph, typename P, bool MR>
+__device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, int K, const double* __restrict__ U,
+                                              const double* __restrict__ Uold, double time, double tstepinv,
+                                              double lambda, double* __restrict__ F, P* __restrict__ J) {
+  constexpr int NS = Ph::NS;
+  double uK[NS];
+  P uKs[NS];  // the values in the partials' precision, converted once per node
+#pragma unroll
+  for (int i = 0; i < NS; ++i) { uK[i] = U[(size_t)K * NS + i]; uKs[i] = P(uK[i]); }
+  double fK[NS];
+  P jd[NS * NS];
+#pragma unroll
+  for (int i = 0; i < NS; ++i) fK[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < NS * NS; ++i) jd[i] = P(0);
+
+  node_terms<Ph, P, MR>(t, ph, K, uK, uKs, Uold, time, tstepinv, lambda, fK, jd);
 
   // ---- edges incident to K, in edge order (columns sorted by node index)
   const int sbeg = t.browptr[K], send = t.browptr[K + 1];
@@ -121,54 +180,20 @@ __device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, 
     }
   }
 
-  // ---- boundary-face items of K (bface order): legacy Dirichlet/Robin + breaction
-  const int bbeg = t.bn_ptr[K], bend = t.bn_ptr[K + 1];
-  for (int it = bbeg; it < bend; ++it) {
-    const int reg = t.bn_reg[it];
-    const double fac = t.bn_fac[it];
-    double Dir = kDirichlet;
-    if (t.has_legacy && reg - 1 < t.nbregions) {
-      Dir = kDirichlet / fac;
-#pragma unroll
-      for (int i = 0; i < NS; ++i) {
-        const double bf = t.bfactors[i + NS * (reg - 1)], bv = t.bvalues[i + NS * (reg - 1)];
-        if (bf == kDirichlet) {
-          fK[i] += bf * (uK[i] - bv);
-          jd[i * NS + i] += P(bf);
-        } else {
-          fK[i] += fac * (bf * uK[i] - bv);
-          if (bf != 0.0) jd[i * NS + i] += P(bf) * P(fac);
-        }
-      }
-    }
-    if (Ph::has_breaction) {
-      BNodeItem bi{K, reg, xK, time, lambda, fac, Dir, nullptr};
-      Dual<NS, P> u[NS], y[NS];
-#pragma unroll
-      for (int i = 0; i < NS; ++i) { u[i] = dseed<NS, P>(uK[i], uKs[i], i); y[i] = dconst<NS, P>(0.0); }
-      ph.breaction(y, u, bi);
-      const P facp = P(fac);
-#pragma unroll
-      for (int i = 0; i < NS; ++i) {
-        fK[i] += fac * y[i].v;
-#pragma unroll
-        for (int j = 0; j < NS; ++j) jd[i * NS + j] += y[i].d[j] * facp;
-      }
-    }
-  }
+  bnode_terms<Ph, P>(t, ph, K, uK, uKs, time, lambda, fK, jd);
 
   bool bad = false;
 #pragma unroll
   for (int i = 0; i < NS; ++i) {
     F[(size_t)K * NS + i] = fK[i];
-    bad |= isnan(fK[i]);
+    bad |= nan_bits(fK[i]);
   }
   if (J) {
     P* Jd = J + (size_t)t.diag[K] * NS * NS;
 #pragma unroll
     for (int i = 0; i < NS * NS; ++i) {
       Jd[i] = jd[i];
-      bad |= isnan((double)jd[i]);
+      bad |= nan_bits(jd[i]);
     }
   }
   return bad;

@@ -590,6 +590,11 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
   SETUP_CUDA(c->J.alloc((size_t)c->nnzb * ns * ns));
   SETUP_CUDA(c->errflag.alloc(4));
   SETUP_CUDA(cudaMemset(c->errflag.p, 0, 4 * sizeof(int)));
+  {
+    int rc = build_assembly_tiles(c, slot_fac);
+    if (rc == VFVM_OK) rc = prepare_tiled_assembly(c);
+    if (rc != VFVM_OK) { *status = rc; delete c; return nullptr; }
+  }
   *status = VFVM_OK;
   return c;
 }

@@ -56,6 +56,45 @@ struct AsmTables {
   const double* bfactors; const double* bvalues; int nbregions; int has_legacy;
 };
 
+// Node tiles of the edge-once assembly (vfvm_tiles.cu builds them, the tiled
+// kernel in vfvm_assembly.cu reads them).  Tile t owns a compact set of nodes
+// (a run of the Z-order curve through the node coordinates); its local node
+// list is the owned nodes followed by the halo (neighbours owned by other
+// tiles).  Its edge list holds every edge with an owned endpoint once: edges
+// between two owned nodes once, edges to the halo once per tile that owns an
+// endpoint.  slot_le maps every off-diagonal Jacobian slot of an owned row to
+// the local index of its edge.
+struct TileTables {
+  int ntiles, maxloc, maxedges;
+  const int* tile_ptr;             // ntiles+1 offsets into lnodes
+  const int* tile_nown;            // owned nodes per tile (the first entries of its lnodes)
+  const int* tile_eptr;            // ntiles+1 offsets into the edge arrays
+  const int* lnodes;               // local node lists (global node ids)
+  const unsigned* edge_ab;         // local endpoints: first | second << 16 (low -> high node index)
+  const double* edge_fac;          // edge form factor
+  const float* edge_facf;          // the same in FP32 (mixed-form partials)
+  const unsigned short* slot_le;   // nnzb: local edge index of an off-diagonal slot
+};
+
+// Shared-memory layout of one tile (byte offsets), identical on host and device.
+struct TileSmem {
+  size_t lnodes, uv, us, ef, ja, jb, total;
+};
+template <int NS, typename P>
+VFVM_HD TileSmem tile_smem_layout(int maxloc, int maxedges) {
+  auto up = [](size_t b) { return (b + 15) & ~(size_t)15; };
+  TileSmem L;
+  L.lnodes = 0;
+  L.uv = up((size_t)maxloc * 4);
+  L.us = up(L.uv + (size_t)maxloc * NS * 8);
+  const size_t us_bytes = std::is_same<P, double>::value ? 0 : (size_t)maxloc * NS * sizeof(P);
+  L.ef = up(L.us + us_bytes);
+  L.ja = up(L.ef + (size_t)maxedges * NS * 8);
+  L.jb = up(L.ja + (size_t)maxedges * NS * NS * sizeof(P));
+  L.total = up(L.jb + (size_t)maxedges * NS * NS * sizeof(P));
+  return L;
+}
+
 struct Workspace;  // Krylov / Newton work buffers (vfvm_solver.cu)
 
 // Aggregation tables of the coarse-grid correction (vfvm_coarse.cuh), built for
@@ -110,6 +149,15 @@ struct vfvm_ctx {
   int ell_w = 0, lo_w = 0, up_w = 0;
   vfvm::DBuf<int> ell_col, ell_slot, lo_node, lo_slot, up_node, up_slot;
 
+  // node tiles of the edge-once assembly (single-region grids; ntiles = 0: none)
+  int ntiles = 0, tile_nodes = 0, tile_maxloc = 0, tile_maxedges = 0, tile_threads = 0;
+  int64_t tile_edge_evals = 0;              // edges evaluated per assembly (cross-tile edges twice)
+  vfvm::DBuf<int> tile_ptr, tile_nown, tile_eptr, tile_lnodes;
+  vfvm::DBuf<unsigned> tile_edge_ab;
+  vfvm::DBuf<double> tile_edge_fac;
+  vfvm::DBuf<float> tile_edge_facf;
+  vfvm::DBuf<uint16_t> slot_le;
+
   // assembly buffers
   vfvm::DBuf<double> U, Uold, F, J;         // J: nnzb*ns*ns
   vfvm::DBuf<float> Jf;
@@ -121,6 +169,7 @@ struct vfvm_ctx {
   const vfvm_ctx* grid_base = nullptr;     // clones: the context whose grid tables they view
 
   vfvm::AsmTables tables() const;
+  vfvm::TileTables tile_tables() const;
   // the coarse stage's device view (nc == 0 when it is off)
   vfvm::CoarseData coarse_data() const;
 };
@@ -132,6 +181,30 @@ int launch_assemble(vfvm_ctx* c, const double* U, const double* Uold, const doub
                     float* Jf, cudaStream_t s);
 int launch_init_dirichlet(vfvm_ctx* c, double* U, const double* tv, cudaStream_t s);
 int launch_pattern_gather(vfvm_ctx* c, const double* J, double* out, cudaStream_t s);
+// node tiles of the edge-once assembly (vfvm_tiles.cu): plan_tiles is the
+// host-only planner (ntiles = 0 where the grid does not suit tiles),
+// build_assembly_tiles plans from the context's host tables and uploads
+struct TileInput {
+  int N, dim, ns;
+  int64_t nnzb;
+  const double* coord;       // N x dim, node-major
+  const int* browptr;        // N+1
+  const int* bcol;           // nnzb, sorted per row
+  const int* diag;           // N
+  const double* slot_fac;    // nnzb: edge factor per off-diagonal slot
+};
+struct TilePlan {
+  int ntiles = 0, tile_nodes = 0, maxloc = 0, maxedges = 0;
+  std::vector<int> tile_ptr, tile_nown, tile_eptr, lnodes;
+  std::vector<unsigned> edge_ab;
+  std::vector<double> edge_fac;
+  std::vector<uint16_t> slot_le;
+};
+int plan_tiles(const TileInput& in, TilePlan& out);
+int build_assembly_tiles(vfvm_ctx* c, const std::vector<double>& slot_fac);
+// per-physics launch attributes of the tiled assembly (shared memory above the
+// default limit); called once per context, outside any stream capture
+int prepare_tiled_assembly(vfvm_ctx* c);
 int probe_masks(int phys, const double* params, int nparams, int dim, std::vector<uint8_t>& node_mask,
                 std::vector<uint8_t>& edge_mask, std::vector<uint8_t>& bnode_mask);
 void destroy_workspace(Workspace* w);

@@ -43,6 +43,11 @@ vfvm_ctx* clone_context(const vfvm_ctx* b, const vfvm_physics_desc* ph, int* sta
   c->ell_w = b->ell_w; c->lo_w = b->lo_w; c->up_w = b->up_w;
   c->ell_col.view(b->ell_col); c->ell_slot.view(b->ell_slot); c->lo_node.view(b->lo_node);
   c->lo_slot.view(b->lo_slot); c->up_node.view(b->up_node); c->up_slot.view(b->up_slot);
+  c->ntiles = b->ntiles; c->tile_nodes = b->tile_nodes; c->tile_maxloc = b->tile_maxloc;
+  c->tile_maxedges = b->tile_maxedges; c->tile_threads = b->tile_threads; c->tile_edge_evals = b->tile_edge_evals;
+  c->tile_ptr.view(b->tile_ptr); c->tile_nown.view(b->tile_nown); c->tile_eptr.view(b->tile_eptr);
+  c->tile_lnodes.view(b->tile_lnodes); c->tile_edge_ab.view(b->tile_edge_ab); c->tile_edge_fac.view(b->tile_edge_fac);
+  c->tile_edge_facf.view(b->tile_edge_facf); c->slot_le.view(b->slot_le);
   // own physics data; the legacy boundary data must match the base's structure
   c->h_params.assign(ph->params, ph->params + ph->nparams);
   c->nparams = ph->nparams;
