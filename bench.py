@@ -345,11 +345,12 @@ NTRAIN = 4096
 NEVAL = 512
 EVAL_SEED0 = 1_000_000
 COARSE = 196           # coarse-grid correction unknowns
-# Stopping rule of the learned workload: max|F| <= 1e-12, which implies the
+# Stopping rule of the learned workload: max|F| <= 1e-13, which implies the
 # metric's 1e-10.  On this grid (h^2 = 1.5e-5) max|F| <= 1e-10 still leaves
 # about 6e-8 relative solution error, above the 1e-8 agreement asked of every
-# form; 1e-12 brings it to about 1e-9.
-FTOL_L = 1.0e-12
+# form; 1e-12 leaves up to 2.4e-8 on the instances whose solution is small
+# (source f close to 1; checked on 32 held-out instances), 1e-13 a tenth of it.
+FTOL_L = 1.0e-13
 METRIC_L = ("Newton solves/s at ||F||<=1e-10 (stationary -div(kappa grad u) + exp(u) = f, 257x257 triangles, "
             "512 held-out GRF instances): learned+mixed+batched form")
 
@@ -747,7 +748,7 @@ def run_learned(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_l, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"kappa-exp {LN}x{LN} triangles, {NEVAL} held-out GRF instances per step "
-                               f"(network trained on {args.ntrain} plain solves), stopping rule max|F|<=1e-12 (implies the metric's 1e-10)",
+                               f"(network trained on {args.ntrain} plain solves), stopping rule max|F|<=1e-13 (implies the metric's 1e-10)",
                    "form": "network start (guarded) + FP64 residual/update, FP32 Jacobian + FP32 BiCGStab with "
                            f"multicolour ILU0 and a {COARSE}-unknown Galerkin coarse stage (at most {MAXITERS_LINEAR} "
                            "iterations per Newton step), all instances solved together (one CUDA graph)",
@@ -819,7 +820,7 @@ def run_reference_learned(args, rank, world):
         "impl": "reference", "metric": METRIC_L, "value": sps, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / len(walls),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"kappa-exp {LN}x{LN} triangles, held-out GRF instances, stopping rule max|F|<=1e-12",
+        "config": {"workload": f"kappa-exp {LN}x{LN} triangles, held-out GRF instances, stopping rule max|F|<=1e-13",
                    "sample": f"{cores} held-out instances per step, one process per core, one Newton solve each "
                              "from inival 0"},
         "cpu_baseline": {"value": sps, "unit": UNIT, "cores": cores, "kind": "port",
@@ -949,31 +950,112 @@ def run_batch_only(args):
                       "krylov": float(np.mean([h.nlin for h in hist]))}))
 
 
+def run_learned_bound(args):
+    """Measurement mode: what a learned initial iterate can gain on the learned
+    workload.  The held-out instances are solved once (FP64, tight tolerance);
+    their solutions, restricted to an nc x nc subgrid and prolonged bilinearly
+    like the network's output, serve as "perfect predictions" at output
+    resolutions 33^2, 65^2 and 129^2, next to the exact solution itself and to
+    inival 0.  Each guess is timed through the same guarded batched solve as the
+    benchmark's learned form (CUDA events, L2 flushed)."""
+    import torch
+    import __graft_entry__ as ge
+    vfvm = ge.load_package()
+    lk = vfvm.learned
+    L = vfvm._lib
+    lib = L.load()
+    n = args.batch_n
+    seeds = heldout_seeds(0)[:n]
+    logk, f = kappa_instances(lk, LN, seeds)
+    sweep = lk.KappaSweep(LN, n)
+    sweep.load(logk, f)
+    N = sweep.nnodes
+    zeros = torch.zeros(n * N, dtype=torch.float64, device="cuda")
+    U = torch.empty_like(zeros)
+    ref = learned_control(vfvm, "batched_fp64", maxiters_linear=400)
+    ref.abstol = 1e-14
+    sweep.solve_device(zeros.data_ptr(), U.data_ptr(), ref)
+    Uex = U.clone()
+    flush = torch.empty(int(512 * 2 ** 20 // 4), dtype=torch.float32, device="cuda")
+    ctl = learned_control(vfvm, "learned")
+
+    def timed(guess):
+        out = []
+        for it in range(args.warmup + args.steps):
+            flush.fill_(float(it))
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            if guess is None:
+                hist, _ = sweep.solve_device(zeros.data_ptr(), U.data_ptr(), ctl)
+            else:
+                hist, _ = sweep.solve_device(zeros.data_ptr(), U.data_ptr(), ctl, guess_dev=guess.data_ptr())
+            e1.record()
+            torch.cuda.synchronize()
+            if it >= args.warmup:
+                out.append(e0.elapsed_time(e1))
+        ms = float(np.mean(out))
+        err = float((U - Uex).abs().max().item() / Uex.abs().max().item())
+        return {"solves_per_s": n / (ms * 1e-3), "newton_per_solve": float(np.mean([h.nnewton for h in hist])),
+                "krylov_per_solve": float(np.mean([h.nlin for h in hist])), "max_rel_err_vs_fp64": err}
+
+    res = {"inival_0": timed(None), "exact_solution": timed(Uex)}
+    Uh = Uex.view(n, LN, LN)
+    for nc in (33, 65, 129):
+        r = (LN - 1) // (nc - 1)
+        coarse = Uh[:, ::r, ::r].contiguous().to(torch.float32)
+        guess = torch.empty_like(zeros)
+        rc = lib.vfvm_prolong_bilinear(n, nc, r, coarse.data_ptr(), nc * nc, 1.0, 0.0, None, guess.data_ptr(), N, None)
+        if rc != 0:
+            raise RuntimeError(f"vfvm_prolong_bilinear failed: {rc}")
+        g_err = float((guess - Uex).abs().max().item() / Uex.abs().max().item())
+        res[f"perfect_{nc}x{nc}"] = dict(timed(guess), guess_rel_err=g_err)
+    base = res["inival_0"]["solves_per_s"]
+    for k, v in res.items():
+        v["speedup_vs_inival_0"] = v["solves_per_s"] / base
+    print(json.dumps({"mode": "learned-bound", "instances": n, "steps": args.steps, "forms": res}))
+
+
 def run_assembly_only(args):
     """Profiling mode: build the workload and launch the assembly kernel
-    `--steps` times (FP32-Jacobian form), nothing else."""
+    `--steps` times (FP32-Jacobian form), nothing else: the porous medium on
+    nx x nx points, or with `--workload bipolar` the 3D drift-diffusion system
+    on nx^3 points (nx = 64 unless given) at embedding parameter 0.5."""
     import ctypes
     import torch
     import __graft_entry__ as ge
     vfvm = ge.load_package()
     lib = vfvm._lib.load()
-    g, u0 = workload(vfvm, args.nx)
-    sysm = vfvm.System(g, vfvm.Physics("porous"))
+    tstep, lam = DT, 0.0
+    if args.workload == "bipolar":
+        n = args.nx if args.nx != NX else 64
+        X = np.linspace(0.0, 1.0, n)
+        g = vfvm.simplexgrid(X, X, X)
+        params = [1.0, 1.0, 1.0, 1.0, 1.0, 1.0e3, 0.5]
+        sysm = vfvm.System(g, vfvm.Physics("bipolar", params), species=[1, 2, 3])
+        C = np.where(g.coord[0] < 0.5, params[5], -params[5])
+        nn = 0.5 * C + np.sqrt(0.25 * C * C + 1.0)
+        u0 = np.asfortranarray(np.stack([np.arcsinh(0.5 * C), nn, 1.0 / nn])).ravel(order="F")
+        tstep, lam = math.inf, 0.5
+    else:
+        g, u0 = workload(vfvm, args.nx)
+        sysm = vfvm.System(g, vfvm.Physics("porous"))
     h = sysm.ctx
     U = torch.from_numpy(u0).cuda()
     F = torch.empty_like(U)
     for _ in range(args.warmup + args.steps):
-        rc = lib.vfvm_assemble_device(h, ctypes.c_void_p(U.data_ptr()), ctypes.c_void_p(U.data_ptr()), 0.0, DT, 0.0,
+        rc = lib.vfvm_assemble_device(h, ctypes.c_void_p(U.data_ptr()), ctypes.c_void_p(U.data_ptr()), 0.0, tstep, lam,
                                       ctypes.c_void_p(F.data_ptr()), 1)
         if rc != 0:
             raise RuntimeError(f"assembly failed: {rc}")
     torch.cuda.synchronize()
-    print(json.dumps({"mode": "assembly", "nx": args.nx, "launches": args.warmup + args.steps, **sysm.info()}))
+    print(json.dumps({"mode": "assembly", "workload": args.workload, "nx": args.nx, "launches": args.warmup + args.steps,
+                      **sysm.info()}))
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--mode", choices=["bench", "assembly", "batch"], default="bench")
+    ap.add_argument("--mode", choices=["bench", "assembly", "batch", "learned-bound"], default="bench")
     ap.add_argument("--batch-n", type=int, default=16)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -1002,6 +1084,9 @@ def main():
         return
     if args.mode == "batch":
         run_batch_only(args)
+        return
+    if args.mode == "learned-bound":
+        run_learned_bound(args)
         return
     if args.impl == "reference":
         if world > 1 and rank != 0:

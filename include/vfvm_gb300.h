@@ -192,6 +192,19 @@ int vfvm_evolve(vfvm_ctx* ctx, const vfvm_control* control, const double* inival
                 double* U_store, double* t_store, int32_t max_store, int32_t* nstored,
                 vfvm_history* hist);
 
+/* solve_transient! with the step-size control on the device: the same
+ * arguments and results as vfvm_evolve (lambdas must increase strictly;
+ * max_store >= 1), but the step loop -- tentative step, Newton, the solution
+ * change, accept / reject / grow (src/vfvm_solver.jl:350-513) -- runs as one
+ * launch of a CUDA graph whose controller kernel decides every step on the
+ * device; stored solutions are copied to the host once, at the end.  Uses the
+ * graph engine with BiCGStab (GMRES: VFVM_ERR_INPUT).  *host_syncs (optional)
+ * receives the number of host synchronisations of the call (independent of the
+ * number of steps). */
+int vfvm_evolve_device(vfvm_ctx* ctx, const vfvm_control* control, const double* inival, const double* lambdas,
+                       int32_t nlambdas, int32_t transient, double time, double* U_store, double* t_store,
+                       int32_t max_store, int32_t* nstored, vfvm_history* hist, int32_t* host_syncs);
+
 /* Device-resident variants: U_dev / inival_dev are device pointers (n doubles).
  * These run the same device loop without host<->device copies; the stream is
  * the context's stream (vfvm_stream). */

@@ -38,16 +38,22 @@ def barenblatt(x, t, m):
     return tx * xx ** (1.0 / (m - 1.0))
 
 
-def test_example106_transient(vfvm, testvals):
+@pytest.mark.parametrize("step_control", ["device", "host"])
+def test_example106_transient(vfvm, testvals, step_control):
     X = np.array([(i - 10) / 10 for i in range(21)])
     sys = vfvm.System(vfvm.simplexgrid(X), vfvm.Physics("ex106", [2.0]))
     inival = vfvm.unknowns(sys)
     inival[0, :] = [barenblatt(x, 0.001, 2.0) for x in X]
-    control = vfvm.SolverControl()
+    control = vfvm.SolverControl(step_control=step_control)
     control.Δt_min = control.Δt_max = control.Δt = 1e-4
     control.Δu_opt = 1.0
     tsol = vfvm.solve(sys, inival=inival, times=[0.001, 0.01], control=control)
     assert tsol.u[-1].sum() == pytest.approx(testvals["Example106_NonlinearDiffusion1D"]["value"], rel=RTOL)
+    assert len(tsol.t) == 91 and tsol.history.nsteps == 90
+    if step_control == "device":
+        # the 90 steps ran inside one graph launch: the call synchronised with
+        # the host three times in all (set-up, end of the loop, stored solutions)
+        assert vfvm.solve.last_host_syncs == 3
 
 
 def test_example110_two_species(vfvm, testvals):
@@ -64,14 +70,40 @@ def test_example110_two_species(vfvm, testvals):
     assert U.ravel(order="F")[4] == pytest.approx(testvals["Example110_ReactionDiffusion1D_TwoSpecies"]["value"], rel=RTOL)
 
 
-def test_example160_bernoulli_sedan(vfvm, testvals):
+@pytest.mark.parametrize("step_control", ["device", "host"])
+def test_example160_bernoulli_sedan(vfvm, testvals, step_control):
     sys = vfvm.System(vfvm.simplexgrid(lin(20)), vfvm.Physics("ex160", [1e-3, -1.0, 5.0]), species=[1, 2])
     inival = vfvm.unknowns(sys)
     inival[0, :] = 0.0
     inival[1, :] = 0.5
-    control = vfvm.SolverControl(Δt_min=1e-5, Δt=1e-5, Δt_grow=1.1, Δt_max=0.1, Δu_opt=0.1, damp_initial=0.5)
+    control = vfvm.SolverControl(Δt_min=1e-5, Δt=1e-5, Δt_grow=1.1, Δt_max=0.1, Δu_opt=0.1, damp_initial=0.5,
+                                 step_control=step_control)
     tsol = vfvm.solve(sys, inival=inival, times=[0.0, 10.0], control=control)
     assert tsol.u[-1].sum() == pytest.approx(testvals["Example160_UnipolarDriftDiffusion1D"]["value"], rel=1e-5)
+    if step_control == "device":
+        # adaptive steps (accepted, rejected and grown on the device), one graph launch
+        assert tsol.history.nsteps > 50 and vfvm.solve.last_host_syncs == 3
+
+
+def test_device_step_control_matches_host(vfvm):
+    """The device controller takes the host controller's decisions: the same
+    accepted times and solutions that agree to the solution-parity bar, with
+    rejected steps (a du_opt that forces retries) and several output intervals."""
+    g = vfvm.simplexgrid(lin(12), lin(12))
+    x, y = g.coord
+    u0 = 1e-3 + np.exp(-((x - 0.5) ** 2 + (y - 0.5) ** 2) / 0.1 ** 2)
+    out = {}
+    for mode in ("host", "device"):
+        sys = vfvm.System(g, vfvm.Physics("porous"))
+        control = vfvm.SolverControl(step_control=mode, engine="graph", Δt=2e-3, Δt_min=1e-5, Δt_max=5e-3,
+                                     Δu_opt=0.05, Δt_grow=1.5, maxiters_linear=400, reltol_linear=1e-8)
+        out[mode] = vfvm.solve(sys, inival=u0.reshape(1, -1), times=[0.0, 0.004, 0.01, 0.02], control=control)
+    h, d = out["host"], out["device"]
+    assert len(h.t) == len(d.t) > 8
+    np.testing.assert_allclose(d.t, h.t, rtol=1e-12, atol=1e-15)
+    for uh, ud in zip(h.u, d.u):
+        assert np.max(np.abs(ud - uh)) <= 1e-8 * np.max(np.abs(uh))
+    assert d.history.nsteps == h.history.nsteps
 
 
 def test_example207_2d_timesteps(vfvm, testvals):

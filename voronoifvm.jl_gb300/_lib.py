@@ -77,6 +77,8 @@ SIGNATURES = {
     "vfvm_solve": (ctypes.c_int, [c_vp, P(Control_t), P(c_d), P(c_d), c_d, c_d, c_d, P(History_t)]),
     "vfvm_evolve": (ctypes.c_int, [c_vp, P(Control_t), P(c_d), P(c_d), c_i32, c_i32, c_d, P(c_d), P(c_d),
                                    c_i32, P(c_i32), P(History_t)]),
+    "vfvm_evolve_device": (ctypes.c_int, [c_vp, P(Control_t), P(c_d), P(c_d), c_i32, c_i32, c_d, P(c_d), P(c_d),
+                                          c_i32, P(c_i32), P(History_t), P(c_i32)]),
     "vfvm_solve_device": (ctypes.c_int, [c_vp, P(Control_t), c_vp, c_vp, c_d, c_d, c_d, P(History_t)]),
     "vfvm_evolve_fixed_device": (ctypes.c_int, [c_vp, P(Control_t), c_vp, c_d, c_d, c_i32, P(History_t)]),
     "vfvm_stream": (c_vp, [c_vp]),

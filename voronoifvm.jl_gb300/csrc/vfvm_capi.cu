@@ -363,3 +363,101 @@ extern "C" int vfvm_evolve(vfvm_ctx* c, const vfvm_control* ctl, const double* i
   if (hist) hist->status = final_status;
   return final_status;
 }
+
+// solve_transient! with the step control on the device: the whole step loop is
+// one launch of the step graph (graph kind 2), with no host round trip per step;
+// the stored solutions stay on the device until the loop ends.  Same decisions
+// as vfvm_evolve (src/vfvm_solver.jl:350-513); lambdas must increase strictly.
+// host_syncs (optional) receives the number of host synchronisations of the
+// call: 3 for implicit Euler (set-up, end of the loop, stored solutions), 4 for
+// embedding (the first solve at lambdas[0] comes before the loop), whatever
+// the number of steps.
+extern "C" int vfvm_evolve_device(vfvm_ctx* c, const vfvm_control* ctl, const double* inival, const double* lambdas,
+                                  int32_t nlambdas, int32_t transient, double time, double* U_store,
+                                  double* t_store, int32_t max_store, int32_t* nstored, vfvm_history* hist,
+                                  int32_t* host_syncs) {
+  if (!c || !inival || !lambdas || nlambdas < 1 || !nstored || max_store < 1 || !U_store || !t_store)
+    return VFVM_ERR_INPUT;
+  for (int i = 0; i + 1 < nlambdas; ++i)
+    if (!(lambdas[i] < lambdas[i + 1])) return VFVM_ERR_INPUT;
+  int rc = check_control(ctl);
+  if (rc) return rc;
+  if (ctl->krylov == VFVM_KRYLOV_GMRES) return VFVM_ERR_INPUT;  // the step graph runs BiCGStab
+  if ((rc = ensure_workspace(c, ctl->precision))) return rc;
+  if ((rc = set_control(c, ctl))) return rc;  // (one synchronisation)
+  int syncs = 1;
+  Workspace* w = c->ws;
+  const size_t n = (size_t)c->N * c->ns;
+  if (!w->sc) VFVM_CUDA(cudaMalloc(&w->sc, sizeof(StepCtl)));
+  DBuf<double> dlam, ustore, tstore;
+  VFVM_CUDA(dlam.alloc((size_t)nlambdas));
+  VFVM_CUDA(ustore.alloc((size_t)max_store * n));
+  VFVM_CUDA(tstore.alloc((size_t)max_store));
+  VFVM_CUDA(cudaMemcpyAsync(dlam.p, lambdas, (size_t)nlambdas * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (hist) std::memset(hist, 0, sizeof(*hist));
+
+  StepCtl h;
+  std::memset(&h, 0, sizeof(h));
+  if (transient) {
+    h.dl = ctl->dt; h.dl_min = ctl->dt_min; h.dl_max = ctl->dt_max; h.dl_grow = ctl->dt_grow; h.dl_dec = ctl->dt_decrease;
+  } else {
+    h.dl = ctl->dp; h.dl_min = ctl->dp_min; h.dl_max = ctl->dp_max; h.dl_grow = ctl->dp_grow; h.dl_dec = ctl->dp_decrease;
+  }
+  h.du_opt = ctl->du_opt; h.du_max_factor = ctl->du_max_factor; h.time0 = time;
+  h.lambdas = dlam.p; h.Ustore = ustore.p; h.tstore = tstore.p; h.oldsol = w->Uinit.p; h.n = (int64_t)n;
+  h.nlam = nlambdas; h.transient = transient ? 1 : 0; h.num_final_steps = ctl->num_final_steps;
+  h.force_first_step = ctl->force_first_step; h.handle_exceptions = ctl->handle_exceptions;
+  h.store_all = ctl->store_all; h.max_store = max_store; h.max_tries = 1 << 22;
+  h.status = VFVM_OK; h.store_slot = -1;
+
+  // the start value: u_old of the first step (after a first solve at lambdas[0] when embedding)
+  VFVM_CUDA(cudaMemcpyAsync(w->Uinit.p, inival, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  float ms = 0;
+  if (!transient) {
+    if ((rc = set_time(c, time, INFINITY, lambdas[0]))) return rc;
+    rc = run_newton(c, ctl, &ms);  // (one synchronisation)
+    ++syncs;
+    fill_history(w->st_host, hist, ms, true);
+    if (rc != VFVM_OK) return rc;
+    VFVM_CUDA(cudaMemcpyAsync(w->Uinit.p, c->U.p, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  }
+  VFVM_CUDA(cudaMemcpyAsync(ustore.p, w->Uinit.p, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  VFVM_CUDA(cudaMemcpyAsync(tstore.p, &lambdas[0], sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  h.nstored = 1;
+  static thread_local StepCtl staged;
+  staged = h;
+  VFVM_CUDA(cudaMemcpyAsync(w->sc, &staged, sizeof(StepCtl), cudaMemcpyHostToDevice, c->stream));
+  {  // Newton totals of the step loop start from zero
+    DevState* hs = w->st_host;
+    std::memset(hs, 0, sizeof(DevState));
+    VFVM_CUDA(cudaMemcpyAsync(w->st, hs, sizeof(DevState), cudaMemcpyHostToDevice, c->stream));
+  }
+  cudaGraphExec_t exec;
+  if ((rc = get_graph(c, ctl->precision, ctl->precon, 2, &exec))) return rc;
+  VFVM_CUDA(cudaEventRecord(w->ev0, c->stream));
+  VFVM_CUDA(cudaGraphLaunch(exec, c->stream));
+  VFVM_CUDA(cudaEventRecord(w->ev1, c->stream));
+  VFVM_CUDA(cudaMemcpyAsync(&staged, w->sc, sizeof(StepCtl), cudaMemcpyDeviceToHost, c->stream));
+  VFVM_CUDA(cudaMemcpyAsync(w->st_host, w->st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream));
+  VFVM_CUDA(cudaStreamSynchronize(c->stream));
+  ++syncs;
+  h = staged;
+  VFVM_CUDA(cudaEventElapsedTime(&ms, w->ev0, w->ev1));
+  const int nst = std::min(h.nstored, max_store);
+  VFVM_CUDA(cudaMemcpyAsync(U_store, ustore.p, (size_t)nst * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  VFVM_CUDA(cudaMemcpyAsync(t_store, tstore.p, (size_t)nst * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  VFVM_CUDA(cudaStreamSynchronize(c->stream));
+  ++syncs;
+  *nstored = nst;
+  if (hist) {
+    hist->nnewton += w->st_host->tot_newton;
+    hist->nlin += w->st_host->tot_lin;
+    hist->nsteps = h.istep;
+    hist->status = h.status;
+    hist->updatenorm = w->st_host->updnorm;
+    hist->resnorm = w->st_host->resnorm;
+    hist->time_ms += ms;
+  }
+  if (host_syncs) *host_syncs = syncs;
+  return h.status;
+}

@@ -23,6 +23,15 @@
 namespace vfvm {
 
 constexpr double kDirichlet = 1.0e30;  // src/vfvm_system.jl:329
+
+// Per-thread accumulator of the Krylov dot products.  FP32 vectors (the mixed
+// form) are summed in FP32 within a thread; only the per-thread partial is
+// widened to FP64 for the deterministic combination across threads.  GB300
+// runs FP64 at about 1/57 of its FP32 rate, so widening every element (two
+// conversions and an FP64 FMA each) made these reductions FP64-bound instead
+// of bandwidth-bound.  FP64 vectors accumulate in FP64.
+template <typename KT>
+using acc_t = typename std::conditional<std::is_same<KT, float>::value, float, double>::type;
 constexpr int kMaxBlockIluColors = 32; // colour limit of the subdomain ILU0 preconditioner
 
 // -----------------------------------------------------------------------------

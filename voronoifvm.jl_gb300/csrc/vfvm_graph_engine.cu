@@ -185,11 +185,13 @@ template <typename KT>
 __global__ void kr_start_kernel(int64_t n, const KT* __restrict__ r, KT* __restrict__ r0, DevState* st,
                                 const DevControl* ctl, double* partials, cudaGraphConditionalHandle kcond) {
   double acc[1] = {0.0};
+  acc_t<KT> a0 = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const KT ri = r[i];
     r0[i] = ri;
-    acc[0] += double(ri) * double(ri);
+    a0 += acc_t<KT>(ri) * acc_t<KT>(ri);
   }
+  acc[0] = double(a0);
   double out[1];
   if (grid_reduce<1>(acc, 0u, partials, &st->ticket[7], out) && threadIdx.x == 0) {
     st->bnorm2 = out[0];
@@ -434,6 +436,7 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(int N, const int* __rest
   const int sub = threadIdx.x % LPR;
   const int rows_per_block = kThreads / LPR;
   double acc[2] = {0.0, 0.0};
+  acc_t<KT> a0 = 0, a1 = 0;
   for (int K0 = blockIdx.x * rows_per_block; K0 < N; K0 += gridDim.x * rows_per_block) {
     const int K = K0 + threadIdx.x / LPR;
     KT y[NS];
@@ -450,14 +453,15 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(int N, const int* __rest
 #pragma unroll
           for (int j = 0; j < NS; ++j) z += D[i * NS + j] * y[j];
           out[(size_t)K * NS + i] = z;
-          const double wz = double(w[(size_t)K * NS + i]);
-          acc[0] += wz * double(z);
-          acc[1] += double(z) * double(z);
+          a0 += acc_t<KT>(w[(size_t)K * NS + i]) * acc_t<KT>(z);
+          a1 += acc_t<KT>(z) * acc_t<KT>(z);
         }
       }
     }
   }
   if (MODE == 0) return;
+  acc[0] = double(a0);
+  acc[1] = double(a1);
   double res[2];
   if (grid_reduce<2>(acc, 0u, partials, &st->ticket[2], res) && threadIdx.x == 0) {
     if (MODE == 1) {
@@ -475,11 +479,14 @@ template <typename KT, int MODE>
 __global__ void dot_kernel(int64_t n, const KT* __restrict__ z, const KT* __restrict__ w, DevState* st,
                            double* partials) {
   double acc[2] = {0.0, 0.0};
+  acc_t<KT> a0 = 0, a1 = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double zz = double(z[i]);
-    acc[0] += double(w[i]) * zz;
-    acc[1] += zz * zz;
+    const acc_t<KT> zz = acc_t<KT>(z[i]);
+    a0 += acc_t<KT>(w[i]) * zz;
+    a1 += zz * zz;
   }
+  acc[0] = double(a0);
+  acc[1] = double(a1);
   double res[2];
   if (grid_reduce<2>(acc, 0u, partials, &st->ticket[3], res) && threadIdx.x == 0) {
     if (MODE == 1) {
@@ -508,13 +515,16 @@ __global__ void bi_xr_kernel(int64_t n, KT* __restrict__ x, KT* __restrict__ r, 
                              DevState* st, const DevControl* ctl, double* partials, cudaGraphConditionalHandle kcond) {
   const KT alpha = KT(st->alpha), omega = KT(st->omega);
   double acc[2] = {0.0, 0.0};
+  acc_t<KT> a0 = 0, a1 = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     x[i] += alpha * p[i] + omega * s[i];
     const KT rn = s[i] - omega * t[i];
     r[i] = rn;
-    acc[0] += double(r0[i]) * double(rn);
-    acc[1] += double(rn) * double(rn);
+    a0 += acc_t<KT>(r0[i]) * acc_t<KT>(rn);
+    a1 += acc_t<KT>(rn) * acc_t<KT>(rn);
   }
+  acc[0] = double(a0);
+  acc[1] = double(a1);
   double out[2];
   if (grid_reduce<2>(acc, 0u, partials, &st->ticket[4], out) && threadIdx.x == 0) {
     const double rho_new = out[0];
@@ -613,6 +623,150 @@ __global__ void maxdiff_kernel(int64_t n, const double* __restrict__ a, const do
 }
 
 // ---------------------------------------------------------------------------
+// Device step control (graph kind 2): the step loop of solve_transient!
+// (src/vfvm_solver.jl:350-513) advanced by a one-thread controller kernel after
+// every tentative step.  Same decisions in the same order as the reference:
+// retry with a smaller step when Newton fails (handle_exceptions) or the change
+// max|u - u_old| exceeds du_max_factor * du_opt; give up at the minimal step
+// (unless the first step is forced); grow the step by dl_grow and
+// du_opt / du, never past the next value of `lambdas`, and spread the last
+// num_final_steps steps evenly.
+// ---------------------------------------------------------------------------
+
+// Julia's isapprox(a, b; rtol, atol)
+__device__ __forceinline__ bool sc_approx(double a, double b, double rtol, double atol) {
+  return a == b || (isfinite(a) && isfinite(b) && fabs(a - b) <= fmax(atol, rtol * fmax(fabs(a), fabs(b))));
+}
+constexpr double kSqrtEps = 1.4901161193847656e-8;
+
+// the time / embedding values of the next tentative step from lam0 with size dl
+__device__ __forceinline__ void sc_setup_try(StepCtl* sc, DevState* st) {
+  sc->lam = sc->lam0 + sc->dl;
+  if (sc->transient) { st->time = sc->lam; st->tstepinv = 1.0 / sc->dl; st->lambda = 0.0; }
+  else { st->time = sc->time0; st->tstepinv = 0.0; st->lambda = sc->lam; }
+  st->abort = 0;
+}
+
+// reserve a slot for a stored solution (the last slot is overwritten when full)
+__device__ __forceinline__ void sc_store(StepCtl* sc, double t, int src) {
+  int slot = -1;
+  if (sc->nstored < sc->max_store) slot = sc->nstored++;
+  else if (sc->max_store > 0) slot = sc->max_store - 1;
+  if (slot >= 0) sc->tstore[slot] = t;
+  sc->store_slot = slot;
+  sc->store_src = src;
+}
+
+// first tentative step of interval i (lambdas strictly increase: checked on the host)
+__device__ __forceinline__ void sc_start_interval(StepCtl* sc, DevState* st) {
+  sc->dl = fmax(sc->dl, sc->dl_min);
+  sc->lam = sc->lambdas[sc->i];
+  sc->lam0 = sc->lam;
+  sc->du = 0.0;
+  sc_setup_try(sc, st);
+}
+
+__global__ void sc_begin_kernel(StepCtl* sc, DevState* st, cudaGraphConditionalHandle scond) {
+  sc->copy_old = 0;
+  sc->store_slot = -1;
+  sc->ntries = 0;
+  int go = 0;
+  if (sc->i + 1 < sc->nlam) {
+    sc_start_interval(sc, st);
+    go = 1;
+  }
+  cudaGraphSetConditional(scond, go);
+}
+
+// after a tentative step (Newton done, st->maxdiff = max|u - u_old|)
+__global__ void sc_finish_kernel(StepCtl* sc, DevState* st, cudaGraphConditionalHandle scond) {
+  sc->copy_old = 0;
+  sc->store_slot = -1;
+  sc->ntries += 1;
+  bool solved = true, errored = false, giveup = false;
+  const int newton = st->status;
+  if (newton != VFVM_OK) {
+    if (!sc->handle_exceptions) { sc->status = newton; cudaGraphSetConditional(scond, 0); return; }
+    solved = false;
+    errored = true;
+  }
+  if (solved) {
+    sc->du = st->maxdiff;
+    if (sc->du > sc->du_max_factor * sc->du_opt) solved = false;
+  }
+  if (!solved) {
+    if (sc_approx(sc->dl, sc->dl_min, kSqrtEps, 0.0)) {
+      if (!(sc->force_first_step && sc->istep == 0) || errored) {
+        sc->status = VFVM_ERR_EMBEDDING;
+        if (!sc->handle_exceptions) { cudaGraphSetConditional(scond, 0); return; }
+        giveup = true;
+      } else {
+        solved = true;  // forced first step
+      }
+    } else {
+      sc->dl = fmax(sc->dl_min, sc->dl * sc->dl_dec);
+      int go = 1;
+      if (sc->ntries >= sc->max_tries) { sc->status = VFVM_ERR_EMBEDDING; go = 0; }
+      else sc_setup_try(sc, st);  // retry from the same start
+      cudaGraphSetConditional(scond, go);
+      return;
+    }
+  }
+  if (giveup) {  // leave the step loop; the last accepted solution is the interval's result
+    if (!sc->store_all) sc_store(sc, sc->lam0, 1);
+    cudaGraphSetConditional(scond, 0);
+    return;
+  }
+  // accept the step
+  sc->istep += 1;
+  if (sc->store_all) sc_store(sc, sc->lam, 0);
+  sc->copy_old = 1;
+  const double lam = sc->lam, lend = sc->lambdas[sc->i + 1], dl = sc->dl;
+  const double steps_to_go = ceil((lend - lam) / dl);
+  double lam_predict = lend - lam;
+  if (steps_to_go < sc->num_final_steps) lam_predict = steps_to_go > 0 ? (lend - lam) / steps_to_go : NAN;
+  if (sc_approx(sc->dl_max, sc->dl_min, kSqrtEps, 0.0)) lam_predict = sc->dl_max;
+  if (lam < lend) {
+    // min over the candidates in order; a NaN candidate is skipped
+    double cand[5] = {sc->dl_max, dl * sc->dl_grow, dl * sc->du_opt / (sc->du + 1.0e-14), lam_predict, lend - lam};
+    double m = cand[0];
+    for (int k = 1; k < 5; ++k) if (cand[k] < m) m = cand[k];
+    sc->dl = m;
+    if (sc_approx(lam + sc->dl, lend, 1.0e-15, 1.0e-15)) sc->dl = lend - lam;
+    sc->lam0 = lam;
+    sc->du = 0.0;
+    int go = 1;
+    if (sc->ntries >= sc->max_tries) { sc->status = VFVM_ERR_EMBEDDING; go = 0; }
+    else sc_setup_try(sc, st);
+    cudaGraphSetConditional(scond, go);
+    return;
+  }
+  // end of interval i
+  if (!sc->store_all) sc_store(sc, sc->lam0, 0);  // (u_old becomes u in the copy kernel)
+  sc->i += 1;
+  int go = 0;
+  if (sc->i + 1 < sc->nlam && sc->ntries < sc->max_tries) {
+    sc_start_interval(sc, st);
+    go = 1;
+  }
+  cudaGraphSetConditional(scond, go);
+}
+
+// the copies the controller asked for: a stored solution, u_old = u
+__global__ void sc_copy_kernel(const StepCtl* __restrict__ sc, const double* __restrict__ U) {
+  const int slot = sc->store_slot, src = sc->store_src, cp = sc->copy_old;
+  if (slot < 0 && !cp) return;
+  const int64_t n = sc->n;
+  double* __restrict__ old = sc->oldsol;
+  double* __restrict__ dst = slot >= 0 ? sc->Ustore + (int64_t)slot * n : nullptr;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double u = U[i];
+    if (dst) dst[i] = src == 0 ? u : old[i];
+    if (cp) old[i] = u;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 DevControl make_devcontrol(const vfvm_control& c) {
@@ -634,6 +788,7 @@ void destroy_workspace(Workspace* w) {
   if (w->st) cudaFree(w->st);
   if (w->st_host) cudaFreeHost(w->st_host);
   if (w->ctl) cudaFree(w->ctl);
+  if (w->sc) cudaFree(w->sc);
   if (w->ev0) cudaEventDestroy(w->ev0);
   if (w->ev1) cudaEventDestroy(w->ev1);
   delete w;
@@ -807,24 +962,64 @@ static void record_precon_setup(vfvm_ctx* c, KVecs<KT>& k, const MT* J, int prec
 }
 
 // Build the Newton graph: [init] + WHILE(newton){ assemble; kr_init; precon; WHILE(krylov){iter}; update }.
+// appends a conditional WHILE node after the leaves of g (nodes without
+// dependents); returns the node and its body graph
+static cudaError_t add_while_node(cudaGraph_t g, cudaGraphConditionalHandle h, cudaGraphNode_t* node,
+                                  cudaGraph_t* body) {
+  size_t nn = 0;
+  cudaError_t e = cudaGraphGetNodes(g, nullptr, &nn);
+  if (e != cudaSuccess) return e;
+  std::vector<cudaGraphNode_t> nodes(nn), leaves;
+  if ((e = cudaGraphGetNodes(g, nodes.data(), &nn)) != cudaSuccess) return e;
+  for (auto nd : nodes) {
+    size_t nd_out = 0;
+    if ((e = cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &nd_out)) != cudaSuccess) return e;
+    if (nd_out == 0) leaves.push_back(nd);
+  }
+  cudaGraphNodeParams wp = {};
+  wp.type = cudaGraphNodeTypeConditional;
+  wp.conditional.handle = h;
+  wp.conditional.type = cudaGraphCondTypeWhile;
+  wp.conditional.size = 1;
+  if ((e = cudaGraphAddNode(node, g, leaves.data(), nullptr, leaves.size(), &wp)) != cudaSuccess) return e;
+  *body = wp.conditional.phGraph_out[0];
+  return cudaSuccess;
+}
+
+template <int NS, typename KT>
+static int record_newton_body(vfvm_ctx* c, int precision, int precon, cudaGraph_t body,
+                              cudaGraphConditionalHandle ncond, cudaGraphConditionalHandle kcond);
+
 // kind 0: full solve (copies Uinit -> U, Uinit -> Uold first); kind 1: fixed-step
-// implicit Euler step (advance Uold = U, time += dt, then solve).
+// implicit Euler step (advance Uold = U, time += dt, then solve); kind 2: the
+// whole step loop of solve_transient! with device step control: WHILE (step
+// controller) { U = Uold = u_old; Newton WHILE; max|U - u_old|; controller;
+// copies }.
 template <int NS, typename KT>
 static int build_graph_t(vfvm_ctx* c, int precision, int precon, int kind, cudaGraph_t* out) {
   Workspace* w = c->ws;
-  KVecs<KT>& k = *reinterpret_cast<KVecs<KT>*>(precision == VFVM_PRECISION_FP64 ? (void*)&w->k64 : (void*)&w->k32);
   const int N = c->N;
   const int64_t n = (int64_t)N * NS;
   cudaGraph_t g;
   VFVM_CUDA(cudaGraphCreate(&g, 0));
-  cudaGraphConditionalHandle ncond, kcond;
+  cudaGraphConditionalHandle ncond, kcond, scond;
   VFVM_CUDA(cudaGraphConditionalHandleCreate(&ncond, g, 0, 0));
   VFVM_CUDA(cudaGraphConditionalHandleCreate(&kcond, g, 0, 0));
   cudaStream_t s = c->stream;
+  cudaGraph_t gcap;
+  cudaGraph_t host = g;  // the graph that holds the Newton WHILE node
+  if (kind == 2) {
+    VFVM_CUDA(cudaGraphConditionalHandleCreate(&scond, g, 0, 0));
+    VFVM_CUDA(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    sc_begin_kernel<<<1, 1, 0, s>>>(w->sc, w->st, scond);
+    VFVM_CUDA(cudaStreamEndCapture(s, &gcap));
+    cudaGraphNode_t snode;
+    VFVM_CUDA(add_while_node(g, scond, &snode, &host));
+  }
 
-  // --- prologue
-  VFVM_CUDA(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  if (kind == 0) {
+  // --- prologue of a Newton solve
+  VFVM_CUDA(cudaStreamBeginCaptureToGraph(s, host, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  if (kind == 0 || kind == 2) {
     cudaMemcpyAsync(c->U.p, w->Uinit.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
     cudaMemcpyAsync(c->Uold.p, w->Uinit.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
   } else {
@@ -833,28 +1028,31 @@ static int build_graph_t(vfvm_ctx* c, int precision, int precon, int kind, cudaG
   cudaMemsetAsync(c->errflag.p, 0, sizeof(int), s);
   launch_init_dirichlet(c, c->U.p, &w->st->time, s);
   nt_init_kernel<<<red_blocks(n), kThreads, 0, s>>>(c->U.p, n, w->st, w->ctl, w->partials.p, ncond);
-  cudaGraph_t gcap;
   VFVM_CUDA(cudaStreamEndCapture(s, &gcap));
-  // the last captured node is the tail; add the while node after all leaves
-  size_t nleaf = 0;
-  VFVM_CUDA(cudaGraphGetNodes(g, nullptr, &nleaf));
-  std::vector<cudaGraphNode_t> nodes(nleaf);
-  VFVM_CUDA(cudaGraphGetNodes(g, nodes.data(), &nleaf));
-  // leaves = nodes without dependents
-  std::vector<cudaGraphNode_t> leaves;
-  for (auto nd : nodes) {
-    size_t nd_out = 0;
-    VFVM_CUDA(cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &nd_out));
-    if (nd_out == 0) leaves.push_back(nd);
-  }
-  cudaGraphNodeParams wp = {};
-  wp.type = cudaGraphNodeTypeConditional;
-  wp.conditional.handle = ncond;
-  wp.conditional.type = cudaGraphCondTypeWhile;
-  wp.conditional.size = 1;
   cudaGraphNode_t wnode;
-  VFVM_CUDA(cudaGraphAddNode(&wnode, g, leaves.data(), nullptr, leaves.size(), &wp));
-  cudaGraph_t body = wp.conditional.phGraph_out[0];
+  cudaGraph_t body;
+  VFVM_CUDA(add_while_node(host, ncond, &wnode, &body));
+  if (int rc = record_newton_body<NS, KT>(c, precision, precon, body, ncond, kcond)) return rc;
+  if (kind == 2) {  // step control after the Newton loop
+    VFVM_CUDA(cudaStreamBeginCaptureToGraph(s, host, &wnode, nullptr, 1, cudaStreamCaptureModeThreadLocal));
+    maxdiff_kernel<<<red_blocks(n), kThreads, 0, s>>>(n, c->U.p, w->Uinit.p, w->st, w->partials.p);
+    sc_finish_kernel<<<1, 1, 0, s>>>(w->sc, w->st, scond);
+    sc_copy_kernel<<<red_blocks(n), kThreads, 0, s>>>(w->sc, c->U.p);
+    VFVM_CUDA(cudaStreamEndCapture(s, &gcap));
+  }
+  *out = g;
+  return VFVM_OK;
+}
+
+// The Newton loop body: assembly, Krylov preparation, preconditioner setup,
+// WHILE (BiCGStab iteration), Newton update and the solve_step! logic.
+template <int NS, typename KT>
+static int record_newton_body(vfvm_ctx* c, int precision, int precon, cudaGraph_t body,
+                              cudaGraphConditionalHandle ncond, cudaGraphConditionalHandle kcond) {
+  Workspace* w = c->ws;
+  KVecs<KT>& k = *reinterpret_cast<KVecs<KT>*>(precision == VFVM_PRECISION_FP64 ? (void*)&w->k64 : (void*)&w->k32);
+  const int64_t n = (int64_t)c->N * NS;
+  cudaStream_t s = c->stream;
 
   // --- Newton body
   VFVM_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
@@ -901,7 +1099,6 @@ static int build_graph_t(vfvm_ctx* c, int precision, int precon, int kind, cudaG
   VFVM_CUDA(cudaStreamBeginCaptureToGraph(s, body, &knode, nullptr, 1, cudaStreamCaptureModeThreadLocal));
   nt_update_kernel<KT><<<red_blocks(n), kThreads, 0, s>>>(n, c->U.p, k.x.p, w->st, w->ctl, w->partials.p, ncond);
   VFVM_CUDA(cudaStreamEndCapture(s, &bcap));
-  *out = g;
   return VFVM_OK;
 }
 

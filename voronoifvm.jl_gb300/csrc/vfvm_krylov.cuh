@@ -86,6 +86,7 @@ __device__ __forceinline__ void team_spmv_jac(Team& team, const KrylovData<NS, K
   const int group = team.rank() / LPR;
   const int ngroups = team.size() / LPR;
   const int warp_first_group = (team.rank() & ~31) / LPR;
+  acc_t<KT> a0 = 0, a1 = 0;
   for (int base = warp_first_group; base < d.N; base += ngroups) {
     const int K = base + (group - warp_first_group);
     KT y[NS];
@@ -116,11 +117,13 @@ __device__ __forceinline__ void team_spmv_jac(Team& team, const KrylovData<NS, K
 #pragma unroll
         for (int j = 0; j < NS; ++j) z += D[i * NS + j] * y[j];
         out[(size_t)K * NS + i] = z;
-        acc[0] += double(w[(size_t)K * NS + i]) * double(z);
-        acc[1] += double(z) * double(z);
+        a0 += acc_t<KT>(w[(size_t)K * NS + i]) * acc_t<KT>(z);
+        a1 += acc_t<KT>(z) * acc_t<KT>(z);
       }
     }
   }
+  acc[0] += double(a0);
+  acc[1] += double(a1);
 }
 
 // Solves A x = b (x starts at 0).  Returns false if a team barrier expired.
@@ -182,14 +185,16 @@ __device__ bool team_bicgstab_jacobi(Team& team, const KrylovData<NS, KT>& d, co
     if (!team.template reduce<2>(acc, 0u, red)) return false;
     omega = red[1] > 0.0 ? red[0] / red[1] : 0.0;
     // x += alpha p + omega s ; r = s - omega t
-    acc[0] = acc[1] = 0.0;
+    acc_t<KT> a0 = 0, a1 = 0;
     for (int64_t q = team.rank(); q < n; q += team.size()) {
       d.x[q] += KT(alpha) * d.p[q] + KT(omega) * d.s[q];
       const KT rn = d.s[q] - KT(omega) * d.t[q];
       d.r[q] = rn;
-      acc[0] += double(d.r0[q]) * double(rn);
-      acc[1] += double(rn) * double(rn);
+      a0 += acc_t<KT>(d.r0[q]) * acc_t<KT>(rn);
+      a1 += acc_t<KT>(rn) * acc_t<KT>(rn);
     }
+    acc[0] = double(a0);
+    acc[1] = double(a1);
     if (!team.template reduce<2>(acc, 0u, red)) return false;
     ++it;
     rr = red[1];

@@ -51,6 +51,24 @@ struct KVecs {
   DBuf<KT> gv;                       // GMRES basis, (restart + 1) x N*NS, allocated on first use
 };
 
+// Device-side step control of vfvm_evolve_device: the step loop of
+// solve_transient! (src/vfvm_solver.jl:350-513) as a state record that a
+// one-thread controller kernel advances after every tentative step, inside the
+// step graph (graph kind 2), with no host round trip per step.
+struct StepCtl {
+  // settings
+  double dl_min, dl_max, dl_grow, dl_dec, du_opt, du_max_factor, time0;
+  const double* lambdas;  // nlam values
+  double* Ustore;         // max_store solutions of n values
+  double* tstore;         // max_store times / embedding values
+  double* oldsol;         // the last accepted solution (start of every tentative step)
+  int64_t n;
+  int nlam, transient, num_final_steps, force_first_step, handle_exceptions, store_all, max_store, max_tries;
+  // state
+  double lam, lam0, dl, du;
+  int i, istep, status, nstored, ntries, copy_old, store_slot, store_src;
+};
+
 struct Workspace {
   KVecs<double> k64;
   KVecs<float> k32;
@@ -61,6 +79,7 @@ struct Workspace {
   DevState* st = nullptr;       // device
   DevState* st_host = nullptr;  // pinned mirror
   DevControl* ctl = nullptr;    // device
+  StepCtl* sc = nullptr;        // device step control (vfvm_evolve_device), allocated on first use
   cudaGraphConditionalHandle ncond{}, kcond{};
   std::map<GraphKey, cudaGraphExec_t> graphs;
   std::map<GraphKey, cudaGraph_t> graph_defs;
@@ -79,7 +98,8 @@ struct PersistRunHost {
 int persistent_solve(vfvm_ctx* c, const vfvm_control* ctl, const PersistRunHost& run, vfvm_history* hist, float* ms);
 
 int ensure_workspace(vfvm_ctx* c, int precision);
-// cached, instantiated Newton graph; kind 0 = solve from Uinit, kind 1 = fixed implicit Euler step
+// cached, instantiated Newton graph; kind 0 = solve from Uinit, kind 1 = fixed implicit Euler step,
+// kind 2 = the whole step loop with device step control (ws->sc)
 int get_graph(vfvm_ctx* c, int precision, int precon, int kind, cudaGraphExec_t* out);
 int launch_maxdiff(vfvm_ctx* c, const double* a, const double* b);
 DevControl make_devcontrol(const vfvm_control& c);

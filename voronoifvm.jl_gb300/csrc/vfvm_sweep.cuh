@@ -445,6 +445,7 @@ __global__ void __launch_bounds__(kSweepThreads) sw_kstart_kernel(SweepArgs<Ph, 
   KT* p = a.p + o;
   KT* v = a.v + o;
   double acc[1] = {0.0}, out[1];
+  acc_t<KT> a0 = 0;
   const float* zc = a.cd0.nc ? a.cd0.zc + (int64_t)i * a.cd0.nc : nullptr;
   for (int64_t q = u.tid(); q < a.n; q += u.nt()) {
     KT rq = r[q];
@@ -454,8 +455,9 @@ __global__ void __launch_bounds__(kSweepThreads) sw_kstart_kernel(SweepArgs<Ph, 
       r[q] = rq;
     }
     r0[q] = rq; p[q] = KT(0); v[q] = KT(0);
-    acc[0] += double(rq) * double(rq);
+    a0 += acc_t<KT>(rq) * acc_t<KT>(rq);
   }
+  acc[0] = double(a0);
   if (sw_reduce<1>(acc, 0u, a.partials, a.tickets, i, u.lb, u.nb, out)) {
     const DevControl& ctl = a.call->ctl;
     s.rho = out[0]; s.rr = out[0]; s.alpha = 1.0; s.omega = 1.0; s.beta = 0.0; s.kit = 0; s.kbreak = 0;
@@ -501,6 +503,7 @@ __device__ __forceinline__ void sw_prolong_dot(const SweepArgs<Ph, KT>& a, const
   __syncthreads();
   const int* __restrict__ agg = a.cd0.agg_of_node;
   const uint8_t* __restrict__ dd = a.dirdof;
+  acc_t<KT> a0 = 0, a1 = 0;
   for (int64_t q = u.tid(); q < a.n; q += u.nt()) {
     KT zq = z[q];
     const KT wq = w[q];
@@ -509,9 +512,11 @@ __device__ __forceinline__ void sw_prolong_dot(const SweepArgs<Ph, KT>& a, const
       zq += KT(zcs[agg[K] * NS + (int)(q - K * NS)]);
       z[q] = zq;
     }
-    acc[0] += double(wq) * double(zq);
-    acc[1] += double(zq) * double(zq);
+    a0 += acc_t<KT>(wq) * acc_t<KT>(zq);
+    a1 += acc_t<KT>(zq) * acc_t<KT>(zq);
   }
+  acc[0] += double(a0);
+  acc[1] += double(a1);
   __syncthreads();  // zcs is reloaded by the block's next unit
 }
 

@@ -351,6 +351,7 @@ __device__ __forceinline__ void vec_s_update(KT* __restrict__ s, const KT* __res
 template <typename KT>
 __device__ __forceinline__ void vec_dots(const KT* __restrict__ w, const KT* __restrict__ z, int64_t q0, int64_t q1,
                                          int64_t st, double (&acc)[2]) {
+  acc_t<KT> a0 = 0, a1 = 0;
   for (int64_t q = q0; q < q1; q += kVecU * st) {
     KT ww[kVecU], zz[kVecU];
 #pragma unroll
@@ -361,10 +362,12 @@ __device__ __forceinline__ void vec_dots(const KT* __restrict__ w, const KT* __r
     }
 #pragma unroll
     for (int u = 0; u < kVecU; ++u) {
-      acc[0] += double(ww[u]) * double(zz[u]);
-      acc[1] += double(zz[u]) * double(zz[u]);
+      a0 += acc_t<KT>(ww[u]) * acc_t<KT>(zz[u]);
+      a1 += acc_t<KT>(zz[u]) * acc_t<KT>(zz[u]);
     }
   }
+  acc[0] += double(a0);
+  acc[1] += double(a1);
 }
 
 // x += alpha p + omega s;  r = s - omega t;  acc += (r0.r, r.r)
@@ -373,6 +376,7 @@ __device__ __forceinline__ void vec_xr_update(KT* __restrict__ x, KT* __restrict
                                               const KT* __restrict__ s, const KT* __restrict__ t,
                                               const KT* __restrict__ r0, KT alpha, KT omega, int64_t q0, int64_t q1,
                                               int64_t st, double (&acc)[2]) {
+  acc_t<KT> a0 = 0, a1 = 0;
   for (int64_t q = q0; q < q1; q += kVecU * st) {
     KT xx[kVecU], pp[kVecU], ss[kVecU], tt[kVecU], r0r[kVecU];
 #pragma unroll
@@ -387,11 +391,13 @@ __device__ __forceinline__ void vec_xr_update(KT* __restrict__ x, KT* __restrict
         x[e] = xx[u] + alpha * pp[u] + omega * ss[u];
         const KT rn = ss[u] - omega * tt[u];
         r[e] = rn;
-        acc[0] += double(r0r[u]) * double(rn);
-        acc[1] += double(rn) * double(rn);
+        a0 += acc_t<KT>(r0r[u]) * acc_t<KT>(rn);
+        a1 += acc_t<KT>(rn) * acc_t<KT>(rn);
       }
     }
   }
+  acc[0] += double(a0);
+  acc[1] += double(a1);
 }
 
 // z = (LU)^-1 y with the ELL couplings; ends with a team barrier
@@ -424,11 +430,13 @@ __device__ bool team_bicgstab_ilu(Team& team, const KrylovData<NS, KT>& d, const
   if (!team_ilu_apply_ell<Team, NS, KT>(team, d, il, d.b, d.r)) return false;  // r = M^-1 b
   if (d.cd.nc && !team_coarse_add<Team, NS, KT>(team, d.cd, d.b, d.r, n)) return false;
   double acc1[1] = {0.0};
+  acc_t<KT> a1 = 0;
   for (int64_t q = team.rank(); q < n; q += team.size()) {
     const KT rq = d.r[q];
     d.r0[q] = rq; d.x[q] = KT(0); d.p[q] = KT(0); d.v[q] = KT(0);
-    acc1[0] += double(rq) * double(rq);
+    a1 += acc_t<KT>(rq) * acc_t<KT>(rq);
   }
+  acc1[0] = double(a1);
   double red1[1];
   if (!team.template reduce<1>(acc1, 0u, red1)) return false;
   double rho = red1[0];
@@ -621,11 +629,13 @@ __device__ bool team_bicgstab_bilu(Team& team, const KrylovData<NS, KT>& d, cons
   bilu_apply_ell<NS, KT>(sd, d, il, d.b, d.r);  // r = M^-1 b (subdomain-local)
   if (d.cd.nc && !team_coarse_add_range<Team, NS, KT>(team, d.cd, d.b, d.r, q0, q1)) return false;
   double acc1[1] = {0.0};
+  acc_t<KT> a1 = 0;
   for (int64_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
     const KT rq = d.r[q];
     d.r0[q] = rq; d.x[q] = KT(0); d.p[q] = KT(0); d.v[q] = KT(0);
-    acc1[0] += double(rq) * double(rq);
+    a1 += acc_t<KT>(rq) * acc_t<KT>(rq);
   }
+  acc1[0] = double(a1);
   double red1[1];
   if (!team.template reduce<1>(acc1, 0u, red1)) return false;
   double rho = red1[0];

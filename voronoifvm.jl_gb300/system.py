@@ -141,6 +141,11 @@ class SolverControl:
     # coarse-grid correction stage of the preconditioner: about this many coarse
     # unknowns (aggregates of nodes x species, at most 208); 0 = one-level only
     coarse: int = 0
+    # time / embedding step control of solve(times=...) / solve(embed=...):
+    # "device" runs the whole step loop as one CUDA graph launch (the step
+    # decisions made on the device, graph engine with BiCGStab); "host" decides
+    # each step on the host around device Newton solves (any engine)
+    step_control: str = "device"
 
     def to_c(self, is_linear: bool = False) -> L.Control_t:
         c = L.Control_t()
@@ -441,9 +446,20 @@ def solve(sys: System, inival=0.0, control: Optional[SolverControl] = None, time
         store = np.zeros((max_store, sys.ndofs))
         tst = np.zeros(max_store)
         nst = ctypes.c_int32(0)
-        rc = lib.vfvm_evolve(h, ctypes.byref(c), L.ptr(U0), L.ptr(lambdas), lambdas.size, int(transient), t0,
-                             L.ptr(store), L.ptr(tst), max_store, ctypes.byref(nst), ctypes.byref(hist))
-        _raise(rc, "vfvm_evolve")
+        on_device = (control.step_control == "device" and control.method_linear == "bicgstab"
+                     and bool(np.all(np.diff(lambdas) > 0)))
+        if on_device:
+            syncs = ctypes.c_int32(0)
+            rc = lib.vfvm_evolve_device(h, ctypes.byref(c), L.ptr(U0), L.ptr(lambdas), lambdas.size, int(transient),
+                                        t0, L.ptr(store), L.ptr(tst), max_store, ctypes.byref(nst), ctypes.byref(hist),
+                                        ctypes.byref(syncs))
+            solve.last_host_syncs = int(syncs.value)
+            _raise(rc, "vfvm_evolve_device")
+        else:
+            rc = lib.vfvm_evolve(h, ctypes.byref(c), L.ptr(U0), L.ptr(lambdas), lambdas.size, int(transient), t0,
+                                 L.ptr(store), L.ptr(tst), max_store, ctypes.byref(nst), ctypes.byref(hist))
+            solve.last_host_syncs = None
+            _raise(rc, "vfvm_evolve")
         n = nst.value
         return TransientSolution(tst[:n].tolist(), [_shape(store[i].copy(), sys) for i in range(n)],
                                  NewtonSolverHistory.from_c(hist))
@@ -456,3 +472,4 @@ def solve(sys: System, inival=0.0, control: Optional[SolverControl] = None, time
 
 
 solve.last_history = None
+solve.last_host_syncs = None  # host synchronisations of the last device-controlled evolution
