@@ -198,7 +198,8 @@ int vfvm_evolve(vfvm_ctx* ctx, const vfvm_control* control, const double* inival
  * change, accept / reject / grow (src/vfvm_solver.jl:350-513) -- runs as one
  * launch of a CUDA graph whose controller kernel decides every step on the
  * device; stored solutions are copied to the host once, at the end.  Uses the
- * graph engine with BiCGStab (GMRES: VFVM_ERR_INPUT).  *host_syncs (optional)
+ * graph engine with BiCGStab (GMRES: VFVM_ERR_INPUT); at most 262144 tentative
+ * steps per call (then VFVM_ERR_EMBEDDING).  *host_syncs (optional)
  * receives the number of host synchronisations of the call (independent of the
  * number of steps). */
 int vfvm_evolve_device(vfvm_ctx* ctx, const vfvm_control* control, const double* inival, const double* lambdas,

@@ -364,6 +364,10 @@ extern "C" int vfvm_evolve(vfvm_ctx* c, const vfvm_control* ctl, const double* i
   return final_status;
 }
 
+// tentative steps (accepted or rejected) of one vfvm_evolve_device call at most;
+// beyond them the call returns VFVM_ERR_EMBEDDING
+constexpr int kMaxDeviceSteps = 1 << 18;
+
 // solve_transient! with the step control on the device: the whole step loop is
 // one launch of the step graph (graph kind 2), with no host round trip per step;
 // the stored solutions stay on the device until the loop ends.  Same decisions
@@ -407,7 +411,7 @@ extern "C" int vfvm_evolve_device(vfvm_ctx* c, const vfvm_control* ctl, const do
   h.lambdas = dlam.p; h.Ustore = ustore.p; h.tstore = tstore.p; h.oldsol = w->Uinit.p; h.n = (int64_t)n;
   h.nlam = nlambdas; h.transient = transient ? 1 : 0; h.num_final_steps = ctl->num_final_steps;
   h.force_first_step = ctl->force_first_step; h.handle_exceptions = ctl->handle_exceptions;
-  h.store_all = ctl->store_all; h.max_store = max_store; h.max_tries = 1 << 22;
+  h.store_all = ctl->store_all; h.max_store = max_store; h.max_tries = kMaxDeviceSteps;
   h.status = VFVM_OK; h.store_slot = -1;
 
   // the start value: u_old of the first step (after a first solve at lambdas[0] when embedding)
