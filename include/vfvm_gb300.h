@@ -63,6 +63,9 @@ extern "C" {
 #define VFVM_PHYS_BIPOLAR 13          /* bipolar drift-diffusion (psi,n,p);  params: lambda2,mu_n,mu_p,tau_n,tau_p,doping,V */
 #define VFVM_PHYS_RD2 14              /* two-species reaction-diffusion;    params: D1, D2, k */
 #define VFVM_PHYS_KAPPA_EXP 15        /* -div kappa grad u + exp(u) = f;     params: f; node data: kappa */
+#define VFVM_PHYS_SURFACE_HEAT 16     /* heat equation + conducting surface layer (bflux, bstorage, bsource,
+                                         breaction on boundary region breg; cf. Example311);
+                                         params: eps, eps_s, c_s, k, q0, breg */
 
 /* linear solver / preconditioner / precision selectors */
 #define VFVM_KRYLOV_BICGSTAB 0

@@ -41,7 +41,7 @@ _lib = None
 PHYS = {
     "ex105": 1, "ex106": 2, "ex110": 3, "ex160": 4, "ex207": 5, "ex301": 6, "ex440": 7,
     "laplace_dirichlet": 8, "nlpoisson": 11, "porous": 12, "bipolar": 13, "rd2": 14,
-    "kappa_exp": 15,
+    "kappa_exp": 15, "surface_heat": 16,
 }
 
 
@@ -64,6 +64,7 @@ def lib():
         L.oracle_create.argtypes = [i32, i32, P(d), i32, P(i32), P(i32), i32, P(i32), P(i32), i32,
                                     P(d), i32, P(d), i32, P(d), P(d), i32]
         L.oracle_destroy.argtypes = [ctypes.c_void_p]
+        L.oracle_set_cellwise.argtypes = [ctypes.c_void_p, i32]
         L.oracle_nspec.argtypes = [ctypes.c_void_p]
         L.oracle_nedges.argtypes = [ctypes.c_void_p]
         L.oracle_ncandidates.argtypes = [ctypes.c_void_p]
@@ -138,7 +139,7 @@ def fixed_timesteps(control: Control, dt: float, grow: float = 1.0) -> Control:
 class OracleSystem:
     """Grid tables + physics id + parameters, evaluated by the C++ restatement."""
 
-    def __init__(self, grid, physics, params=(), nodedata=None, bfactors=None, bvalues=None):
+    def __init__(self, grid, physics, params=(), nodedata=None, bfactors=None, bvalues=None, assembly="edgewise"):
         L = lib()
         self.physics_id = PHYS[physics] if isinstance(physics, str) else int(physics)
         self.grid = grid
@@ -170,6 +171,9 @@ class OracleSystem:
             _p(self._bv, ctypes.c_double) if self._bv is not None else None, nbreg)
         if not self.h:
             raise ValueError("oracle_create failed (unknown physics or bad dimension)")
+        if assembly not in ("edgewise", "cellwise"):
+            raise ValueError("assembly must be edgewise or cellwise")
+        L.oracle_set_cellwise(self.h, int(assembly == "cellwise"))
         self.nspec = L.oracle_nspec(self.h)
         self.nnodes = g.nnodes
         self.n = self.nspec * self.nnodes

@@ -11,7 +11,9 @@
 //   Dirichlet constant 1e30                            src/vfvm_system.jl:329
 //   _initialize_dirichlet!                             src/vfvm_system.jl:947-1003
 //   eval_and_assemble (single partition)               src/vfvm_assembly.jl:520-570
-//   assemble_nodes / assemble_edges / assemble_bnodes  src/vfvm_assembly.jl:38-126,128-200,318-407
+//   assemble_nodes / assemble_edges / assemble_bnodes  src/vfvm_assembly.jl:38-126,128-200,318-442
+//   assemble_bedges (bflux on boundary-face edges)     src/vfvm_assembly.jl:444-510
+//   cellwise assembly data (per-cell node/edge factors) src/vfvm_assemblydata.jl:126-208
 //   _addnz (skip exact zeros, NaN is an error)         src/vfvm_assembly.jl:21-28
 //   assemble_res_jac (Node, BNode, Edge)               src/vfvm_assemblydata.jl:245-302,350-382
 //   ResJacEvaluator: forward-mode AD, full chunk       src/vfvm_physics.jl:421-452
@@ -116,6 +118,7 @@ inline double ramp(double t, double t0, double t1, double u0, double u1) {
 struct NodeInfo { int index, region; const double* x; double time, lambda; const double* ndata; };
 struct EdgeInfo { int K, L, region; const double* xK; const double* xL; double time, lambda; const double* ndataK; const double* ndataL; };
 struct BNodeInfo { int index, region; const double* x; double time, lambda, fac, Dirichlet; double* dirichlet_value; };
+struct BEdgeInfo { int K, L, region; const double* xK; const double* xL; double time, lambda; };
 
 // boundary_dirichlet!(y,u,bnode,ispec,ireg,val), src/vfvm_physics.jl:487-494
 template <class T> inline void boundary_dirichlet(T* y, const T* u, BNodeInfo& b, int ispec, int ireg, double v) {
@@ -129,8 +132,17 @@ template <class T> inline void boundary_dirichlet(T* y, const T* u, BNodeInfo& b
 // Physics ids follow include/vfvm_gb300.h (VFVM_PHYS_*).
 struct PhysParams { const double* p; int np; };
 
+// Boundary callbacks beyond breaction (bflux, bstorage, bsource): absent unless a
+// physics defines them.
+struct OBase {
+  static const bool has_bflux = false, has_bstorage = false, has_bsource = false;
+  template <class T> void bflux(T*, const T*, const T*, const BEdgeInfo&) const {}
+  template <class T> void bstorage(T*, const T*, BNodeInfo&) const {}
+  void bsource(double*, BNodeInfo&) const {}
+};
+
 // Each physics: NS, has_* flags, templated callbacks.
-struct PhysEx105 {  // examples/Example105_NonlinearPoisson1D.jl:41-60
+struct PhysEx105 : OBase {  // examples/Example105_NonlinearPoisson1D.jl:41-60
   static const int NS = 1; double eps;
   static const bool has_reaction = true, has_storage = false, has_source = true, has_breaction = false;
   template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = eps * (uK[0] - uL[0]); }
@@ -139,7 +151,7 @@ struct PhysEx105 {  // examples/Example105_NonlinearPoisson1D.jl:41-60
   void source(double* f, const NodeInfo& n) const { f[0] = (n.x[0] <= 0.5) ? 1.0 : -1.0; }
   template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
 };
-struct PhysEx106 {  // examples/Example106_NonlinearDiffusion1D.jl:58-68
+struct PhysEx106 : OBase {  // examples/Example106_NonlinearDiffusion1D.jl:58-68
   static const int NS = 1; double m;
   static const bool has_reaction = false, has_storage = true, has_source = false, has_breaction = false;
   template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = pow(uK[0], m) - pow(uL[0], m); }
@@ -148,7 +160,7 @@ struct PhysEx106 {  // examples/Example106_NonlinearDiffusion1D.jl:58-68
   void source(double*, const NodeInfo&) const {}
   template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
 };
-struct PhysEx110 {  // examples/Example110_ReactionDiffusion1D_TwoSpecies.jl:40-64
+struct PhysEx110 : OBase {  // examples/Example110_ReactionDiffusion1D_TwoSpecies.jl:40-64
   static const int NS = 2; double eps1, eps2;
   static const bool has_reaction = true, has_storage = true, has_source = true, has_breaction = false;
   template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
@@ -160,7 +172,7 @@ struct PhysEx110 {  // examples/Example110_ReactionDiffusion1D_TwoSpecies.jl:40-
   void source(double* f, const NodeInfo& n) const { f[0] = 1.0e-4 * (0.01 + n.x[0]); f[1] = 1.0e-4 * (0.01 + 1.0 - n.x[0]); }
   template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
 };
-struct PhysEx160 {  // examples/Example160_UnipolarDriftDiffusion1D.jl:52-84 (sedan flux; iphi=1, ic=2)
+struct PhysEx160 : OBase {  // examples/Example160_UnipolarDriftDiffusion1D.jl:52-84 (sedan flux; iphi=1, ic=2)
   static const int NS = 2; double eps, z, V;
   static const bool has_reaction = true, has_storage = true, has_source = false, has_breaction = true;
   template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
@@ -182,7 +194,7 @@ struct PhysEx160 {  // examples/Example160_UnipolarDriftDiffusion1D.jl:52-84 (se
     boundary_dirichlet(f, u, b, 1, 2, 0.5);
   }
 };
-struct PhysEx207 {  // examples/Example207_NonlinearPoisson2D.jl:36-50
+struct PhysEx207 : OBase {  // examples/Example207_NonlinearPoisson2D.jl:36-50
   static const int NS = 1; double eps;
   static const bool has_reaction = true, has_storage = true, has_source = true, has_breaction = false;
   template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = eps * (sq(uK[0]) - sq(uL[0])); }
@@ -191,7 +203,7 @@ struct PhysEx207 {  // examples/Example207_NonlinearPoisson2D.jl:36-50
   void source(double* f, const NodeInfo& n) const { double x1 = n.x[0] - 0.5, x2 = n.x[1] - 0.5; f[0] = std::exp(-20.0 * (x1 * x1 + x2 * x2)); }
   template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
 };
-struct PhysEx301 {  // examples/Example301_Laplace3D.jl:15-24
+struct PhysEx301 : OBase {  // examples/Example301_Laplace3D.jl:15-24
   static const int NS = 1;
   static const bool has_reaction = false, has_storage = false, has_source = true, has_breaction = false;
   template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = uK[0] - uL[0]; }
@@ -200,7 +212,7 @@ struct PhysEx301 {  // examples/Example301_Laplace3D.jl:15-24
   void source(double* f, const NodeInfo& n) const { f[0] = n.x[0] * std::sin(5.0 * n.x[1]) * std::exp(n.x[2]); }
   template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
 };
-struct PhysEx440 {  // examples/Example440_ParallelState.jl:16-25
+struct PhysEx440 : OBase {  // examples/Example440_ParallelState.jl:16-25
   static const int NS = 1; double influx;
   static const bool has_reaction = false, has_storage = false, has_source = false, has_breaction = true;
   template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = sq(uK[0]) - sq(uL[0]); }
@@ -212,7 +224,7 @@ struct PhysEx440 {  // examples/Example440_ParallelState.jl:16-25
     if (b.region == 2) f[0] = f[0] - influx;  // boundary_neumann!, src/vfvm_physics.jl:533
   }
 };
-struct PhysLaplaceDir {  // test/test030_cachesol.jl:10-18
+struct PhysLaplaceDir : OBase {  // test/test030_cachesol.jl:10-18
   static const int NS = 1;
   static const bool has_reaction = false, has_storage = false, has_source = false, has_breaction = true;
   template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = uK[0] - uL[0]; }
@@ -225,7 +237,7 @@ struct PhysLaplaceDir {  // test/test030_cachesol.jl:10-18
   }
 };
 // Benchmark workload 1: -div(grad u) + u^3 = 1, u = 0 on every boundary region.
-struct PhysNLPoisson {
+struct PhysNLPoisson : OBase {
   static const int NS = 1;
   static const bool has_reaction = true, has_storage = false, has_source = false, has_breaction = true;
   template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = uK[0] - uL[0]; }
@@ -235,7 +247,7 @@ struct PhysNLPoisson {
   template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const { boundary_dirichlet(f, u, b, 0, b.region, 0.0); }
 };
 // Benchmark workload 2: porous medium u_t - div(grad u^2) = 0, homogeneous Neumann.
-struct PhysPorous {
+struct PhysPorous : OBase {
   static const int NS = 1;
   static const bool has_reaction = false, has_storage = true, has_source = false, has_breaction = false;
   template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = sq(uK[0]) - sq(uL[0]); }
@@ -254,7 +266,7 @@ struct PhysPorous {
 //   C = +doping for x < 0.5, -doping otherwise
 //   ohmic contacts: region 4 (x = 0) at bias 0, region 2 (x = 1) at bias V*lambda_embed
 // params: lambda2, mu_n, mu_p, tau_n, tau_p, doping, V
-struct PhysBipolar {
+struct PhysBipolar : OBase {
   static const int NS = 3; double lambda2, mun, mup, taun, taup, doping, V;
   static const bool has_reaction = true, has_storage = false, has_source = false, has_breaction = true;
   double C(const double* x) const { return x[0] < 0.5 ? doping : -doping; }
@@ -288,7 +300,7 @@ struct PhysBipolar {
 //   flux_i = D_i (u_i,K - u_i,L);  f1 = k (u1 - u2^2), f2 = -k (u1 - u2^2)
 //   Dirichlet: region 4 (x = 0): u1 = 1, u2 = 0;  region 2 (x = 1): u1 = 0, u2 = 1
 // params: D1, D2, k
-struct PhysRD2 {
+struct PhysRD2 : OBase {
   static const int NS = 2; double D1, D2, k;
   static const bool has_reaction = true, has_storage = false, has_source = false, has_breaction = true;
   template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
@@ -311,7 +323,7 @@ struct PhysRD2 {
 // Benchmark workload 5: -div(kappa grad u) + exp(u) = f, u = 0 on every boundary;
 // node data: kappa; edge coefficient = arithmetic mean of the two node values.
 // params: f
-struct PhysKappaExp {
+struct PhysKappaExp : OBase {
   static const int NS = 1; double fsrc;
   static const bool has_reaction = true, has_storage = false, has_source = true, has_breaction = true;
   template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo& e) const {
@@ -322,6 +334,33 @@ struct PhysKappaExp {
   template <class T> void storage(T*, const T*, const NodeInfo&) const {}
   void source(double* f, const NodeInfo&) const { f[0] = fsrc; }
   template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const { boundary_dirichlet(f, u, b, 0, b.region, 0.0); }
+};
+
+// Heat equation with a conducting surface layer on boundary region breg, the
+// single-species form of examples/Example311_HeatEquation_BoundaryDiffusion.jl
+// (flux, bflux, breaction, bsource, bstorage, storage at :40-76 there):
+// storage u, flux eps (uK - uL); on breg: bflux eps_s (uK - uL), bstorage c_s u,
+// breaction k u^3, bsource q0 exp(-20 ((x-1/2)^2 + (y-1/2)^2)).
+struct PhysSurfaceHeat : OBase {
+  static const int NS = 1;
+  static const bool has_reaction = false, has_storage = true, has_source = false, has_breaction = true;
+  static const bool has_bflux = true, has_bstorage = true, has_bsource = true;
+  double eps, eps_s, c_s, k, q0; int breg;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = eps * (uK[0] - uL[0]); }
+  template <class T> void reaction(T*, const T*, const NodeInfo&) const {}
+  template <class T> void storage(T* f, const T* u, const NodeInfo&) const { f[0] = u[0]; }
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const { if (b.region == breg) f[0] = k * cube(u[0]); }
+  template <class T> void bflux(T* f, const T* uK, const T* uL, const BEdgeInfo& e) const {
+    if (e.region == breg) f[0] = eps_s * (uK[0] - uL[0]);
+  }
+  template <class T> void bstorage(T* f, const T* u, BNodeInfo& b) const { if (b.region == breg) f[0] = c_s * u[0]; }
+  void bsource(double* f, BNodeInfo& b) const {
+    if (b.region == breg) {
+      double x1 = b.x[0] - 0.5, x2 = b.x[1] - 0.5;
+      f[0] = q0 * std::exp(-20.0 * (x1 * x1 + x2 * x2));
+    }
+  }
 };
 
 // ---------------------------------------------------------------- system
@@ -345,6 +384,9 @@ struct Oracle {
   std::vector<double> vals;
   std::vector<uint8_t> present;
   int nerr = 0;
+  // assembly = :cellwise (the reference's default, src/vfvm_system.jl:220):
+  // node and edge terms per cell with the cell's own factors
+  bool cellwise = false;
 };
 
 inline int nn_bface(int dim) { return dim; }  // nodes per boundary face: Vertex0D 1, Edge1D 2, Triangle2D 3
@@ -530,53 +572,76 @@ int assemble_t(Oracle& o, const P& ph, const double* U, const double* Uold, doub
   const double tstepinv = 1.0 / tstep;
   const int d = o.dim;
   const double* nd = o.ndata.empty() ? nullptr : o.ndata.data();
-  // assemble_nodes, src/vfvm_assembly.jl:38-126
-  for (int K = 0; K < o.N; ++K) {
-    for (auto& rf : o.nodefac[K]) {
-      NodeInfo ni{K, rf.first, &o.coord[d * K], time, lambda, nd ? nd + (size_t)o.nnd * K : nullptr};
-      double fac = rf.second;
-      double src[NS] = {0}, oldstor[NS] = {0};
-      Dual<NS> u[NS], rr[NS], rs[NS];
-      for (int i = 0; i < NS; ++i) { u[i] = mk<NS>(U[K * NS + i]); u[i].d[i] = 1.0; rr[i] = mk<NS>(0); rs[i] = mk<NS>(0); }
-      if (P::has_source) ph.source(src, ni);
-      if (P::has_reaction) ph.reaction(rr, u, ni);
-      if (P::has_storage) {
-        ph.storage(rs, u, ni);
-        double uo[NS];
-        for (int i = 0; i < NS; ++i) uo[i] = Uold[K * NS + i];
-        ph.storage(oldstor, uo, ni);
-      }
-      for (int i = 0; i < NS; ++i) {
-        F[K * NS + i] += fac * (rr[i].v - src[i] + (rs[i].v - oldstor[i]) * tstepinv);
-        for (int j = 0; j < NS; ++j) addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + j, rr[i].d[j] + rs[i].d[j] * tstepinv, fac);
+  // one node term: fac * (reaction - source + (storage - old storage) / tstep)
+  auto node_term = [&](int K, int reg, double fac) {
+    NodeInfo ni{K, reg, &o.coord[d * K], time, lambda, nd ? nd + (size_t)o.nnd * K : nullptr};
+    double src[NS] = {0}, oldstor[NS] = {0};
+    Dual<NS> u[NS], rr[NS], rs[NS];
+    for (int i = 0; i < NS; ++i) { u[i] = mk<NS>(U[K * NS + i]); u[i].d[i] = 1.0; rr[i] = mk<NS>(0); rs[i] = mk<NS>(0); }
+    if (P::has_source) ph.source(src, ni);
+    if (P::has_reaction) ph.reaction(rr, u, ni);
+    if (P::has_storage) {
+      ph.storage(rs, u, ni);
+      double uo[NS];
+      for (int i = 0; i < NS; ++i) uo[i] = Uold[K * NS + i];
+      ph.storage(oldstor, uo, ni);
+    }
+    for (int i = 0; i < NS; ++i) {
+      F[K * NS + i] += fac * (rr[i].v - src[i] + (rs[i].v - oldstor[i]) * tstepinv);
+      for (int j = 0; j < NS; ++j) addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + j, rr[i].d[j] + rs[i].d[j] * tstepinv, fac);
+    }
+  };
+  // one edge term: flux (bflux on boundary edges) between K (first) and L, scattered 4-way
+  auto edge_term = [&](int K, int L, int reg, double fac, bool boundary) {
+    Dual<2 * NS> uK[NS], uL[NS], f[NS];
+    for (int i = 0; i < NS; ++i) {
+      uK[i] = mk<2 * NS>(U[K * NS + i]); uK[i].d[i] = 1.0;
+      uL[i] = mk<2 * NS>(U[L * NS + i]); uL[i].d[NS + i] = 1.0;
+      f[i] = mk<2 * NS>(0);
+    }
+    if (boundary) {
+      BEdgeInfo be{K, L, reg, &o.coord[d * K], &o.coord[d * L], time, lambda};
+      ph.bflux(f, uK, uL, be);
+    } else {
+      EdgeInfo ei{K, L, reg, &o.coord[d * K], &o.coord[d * L], time, lambda,
+                  nd ? nd + (size_t)o.nnd * K : nullptr, nd ? nd + (size_t)o.nnd * L : nullptr};
+      ph.flux(f, uK, uL, ei);
+    }
+    for (int i = 0; i < NS; ++i) {
+      double v = fac * f[i].v;
+      F[K * NS + i] += v;
+      F[L * NS + i] += -v;
+      for (int j = 0; j < NS; ++j) {
+        int64_t iK = (int64_t)K * NS + i, iL = (int64_t)L * NS + i, jK = (int64_t)K * NS + j, jL = (int64_t)L * NS + j;
+        addnz(o, iK, jK, +f[i].d[j], fac);
+        addnz(o, iL, jK, -f[i].d[j], fac);
+        addnz(o, iK, jL, +f[i].d[NS + j], fac);
+        addnz(o, iL, jL, -f[i].d[NS + j], fac);
       }
     }
-  }
-  // assemble_edges, src/vfvm_assembly.jl:128-200
-  for (int e = 0; e < o.E; ++e) {
-    int K = o.edgenodes[2 * e], L = o.edgenodes[2 * e + 1];
-    for (auto& rf : o.edgefac[e]) {
-      EdgeInfo ei{K, L, rf.first, &o.coord[d * K], &o.coord[d * L], time, lambda,
-                  nd ? nd + (size_t)o.nnd * K : nullptr, nd ? nd + (size_t)o.nnd * L : nullptr};
-      double fac = rf.second;
-      Dual<2 * NS> uK[NS], uL[NS], f[NS];
-      for (int i = 0; i < NS; ++i) {
-        uK[i] = mk<2 * NS>(U[K * NS + i]); uK[i].d[i] = 1.0;
-        uL[i] = mk<2 * NS>(U[L * NS + i]); uL[i].d[NS + i] = 1.0;
-        f[i] = mk<2 * NS>(0);
-      }
-      ph.flux(f, uK, uL, ei);
-      for (int i = 0; i < NS; ++i) {
-        double v = fac * f[i].v;
-        F[K * NS + i] += v;
-        F[L * NS + i] += -v;
-        for (int j = 0; j < NS; ++j) {
-          int64_t iK = (int64_t)K * NS + i, iL = (int64_t)L * NS + i, jK = (int64_t)K * NS + j, jL = (int64_t)L * NS + j;
-          addnz(o, iK, jK, +f[i].d[j], fac);
-          addnz(o, iL, jK, -f[i].d[j], fac);
-          addnz(o, iK, jL, +f[i].d[NS + j], fac);
-          addnz(o, iL, jL, -f[i].d[NS + j], fac);
-        }
+  };
+  if (!o.cellwise) {
+    // assemble_nodes, src/vfvm_assembly.jl:38-126 (edgewise: per node and region)
+    for (int K = 0; K < o.N; ++K)
+      for (auto& rf : o.nodefac[K]) node_term(K, rf.first, rf.second);
+    // assemble_edges, src/vfvm_assembly.jl:128-200 (edgewise: per edge and region)
+    for (int e = 0; e < o.E; ++e)
+      for (auto& rf : o.edgefac[e]) edge_term(o.edgenodes[2 * e], o.edgenodes[2 * e + 1], rf.first, rf.second, false);
+  } else {
+    // the same loops over the cells (CellwiseAssemblyData, src/vfvm_assemblydata.jl:126-136,181-208):
+    // every cell node and every cell edge with the cell's own factor; edge
+    // orientation from the global edge (low -> high node index)
+    const int nnc = d + 1, nen = d == 1 ? 1 : (d == 2 ? 3 : 6);
+    double npar[4], epar[6];
+    for (int c = 0; c < o.ncells; ++c) {
+      cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+      for (int i = 0; i < nnc; ++i) node_term(o.cellnodes[i + nnc * c], o.cellregions[c], npar[i]);
+    }
+    for (int c = 0; c < o.ncells; ++c) {
+      cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+      for (int i = 0; i < nen; ++i) {
+        const int e = o.celledges[i + nen * c];
+        edge_term(o.edgenodes[2 * e], o.edgenodes[2 * e + 1], o.cellregions[c], epar[i], false);
       }
     }
   }
@@ -604,11 +669,41 @@ int assemble_t(Oracle& o, const P& ph, const double* U, const double* Uold, doub
       }
       BNodeInfo bi{K, reg, &o.coord[d * K], time, lambda, fac, Dir, dval};
       Dual<NS> u[NS], y[NS];
+      double bsrc[NS] = {0};
       for (int i = 0; i < NS; ++i) { u[i] = mk<NS>(U[K * NS + i]); u[i].d[i] = 1.0; y[i] = mk<NS>(0); }
+      if (P::has_bsource) ph.bsource(bsrc, bi);
       if (P::has_breaction) ph.breaction(y, u, bi);
       for (int i = 0; i < NS; ++i) {
-        F[K * NS + i] += fac * (y[i].v - 0.0);
+        F[K * NS + i] += fac * (y[i].v - bsrc[i]);
         for (int j = 0; j < NS; ++j) addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + j, y[i].d[j], fac);
+      }
+      // bstorage, src/vfvm_assembly.jl:409-440
+      if (P::has_bstorage) {
+        Dual<NS> sb[NS];
+        double uo[NS], so[NS] = {0};
+        for (int i = 0; i < NS; ++i) { sb[i] = mk<NS>(0); uo[i] = Uold[K * NS + i]; }
+        ph.bstorage(sb, u, bi);
+        ph.bstorage(so, uo, bi);
+        for (int i = 0; i < NS; ++i) {
+          F[K * NS + i] += fac * (sb[i].v - so[i]) * tstepinv;
+          for (int j = 0; j < NS; ++j) addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + j, sb[i].d[j], fac * tstepinv);
+        }
+      }
+    }
+  }
+  // assemble_bedges, src/vfvm_assembly.jl:444-510: the edges of every boundary
+  // face with the face's edge factors (boundary data are always per face),
+  // oriented low -> high node index
+  if (P::has_bflux && d >= 2) {
+    double npar[3], epar[3];
+    const int nle = d == 2 ? 1 : 3;
+    for (int b = 0; b < o.nbf; ++b) {
+      const int* bn = &o.bfacenodes[nbn * b];
+      bfacefactors(d, o.coord.data(), bn, npar, epar);
+      for (int i = 0; i < nle; ++i) {
+        int K = d == 2 ? bn[0] : bn[tri_en[i][0]], L = d == 2 ? bn[1] : bn[tri_en[i][1]];
+        if (K > L) std::swap(K, L);
+        edge_term(K, L, o.bfaceregions[b], epar[i], true);
       }
     }
   }
@@ -659,6 +754,7 @@ int dispatch(const Oracle& o, F&& fn) {
     case 13: { PhysBipolar ph; ph.lambda2 = P(0); ph.mun = P(1); ph.mup = P(2); ph.taun = P(3); ph.taup = P(4); ph.doping = P(5); ph.V = P(6); return fn(ph); }
     case 14: { PhysRD2 ph; ph.D1 = P(0); ph.D2 = P(1); ph.k = P(2); return fn(ph); }
     case 15: { PhysKappaExp ph; ph.fsrc = P(0); return fn(ph); }
+    case 16: { PhysSurfaceHeat ph; ph.eps = P(0); ph.eps_s = P(1); ph.c_s = P(2); ph.k = P(3); ph.q0 = P(4); ph.breg = (int)P(5); return fn(ph); }
   }
   return -1;
 }
@@ -667,7 +763,7 @@ int nspec_of(int phys) {
   switch (phys) {
     case 3: case 4: case 14: return 2;
     case 13: return 3;
-    case 1: case 2: case 5: case 6: case 7: case 8: case 11: case 12: case 15: return 1;
+    case 1: case 2: case 5: case 6: case 7: case 8: case 11: case 12: case 15: case 16: return 1;
   }
   return 0;
 }
@@ -704,6 +800,9 @@ void* oracle_create(int dim, int nnodes, const double* coord, int ncells, const 
 }
 
 void oracle_destroy(void* h) { delete static_cast<Oracle*>(h); }
+
+// assembly = :cellwise (1) or :edgewise (0, the default here)
+void oracle_set_cellwise(void* h, int cellwise) { static_cast<Oracle*>(h)->cellwise = cellwise != 0; }
 
 int oracle_nspec(void* h) { return static_cast<Oracle*>(h)->ns; }
 int oracle_nedges(void* h) { return static_cast<Oracle*>(h)->E; }

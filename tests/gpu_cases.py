@@ -58,6 +58,10 @@ def case(vfvm, name, seed=0):
         g = sg(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "jittered_square.sg"))
         kind, params = "kappa_exp", [0.3]
         nodedata = np.exp(rng.normal(size=g.nnodes))
+    elif name == "surface_heat2d":  # conducting surface layer on the right side (region 2)
+        g, kind, params, tstep = sg(lin(8), lin(8)), "surface_heat", [1.0, 0.3, 0.5, 2.0, 10.0, 2], 1e-2
+    elif name == "surface_heat3d":  # conducting surface layer on the bottom face (region 5)
+        g, kind, params, tstep = sg(lin(4), lin(4), lin(4)), "surface_heat", [1.0, 0.3, 0.5, 2.0, 10.0, 5], 1e-2
     elif name == "laplace_dirichlet":
         g, kind, params = sg(lin(9)), "laplace_dirichlet", []
     else:
@@ -79,4 +83,4 @@ def random_state(c, nspec, rng):
 
 
 NAMES = ["nlpoisson", "porous", "bipolar", "rd2", "kappa_exp", "ex105", "ex106", "ex110", "ex160", "ex207",
-         "ex301", "ex440", "laplace_dirichlet", "kappa_unstructured"]
+         "ex301", "ex440", "laplace_dirichlet", "kappa_unstructured", "surface_heat2d", "surface_heat3d"]

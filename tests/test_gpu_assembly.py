@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-12
 
 
-def make_pair(vfvm, oracle, c):
+def make_pair(vfvm, oracle, c, assembly="edgewise"):
     sys = vfvm.System(c["grid"], vfvm.Physics(c["kind"], c["params"], c["nodedata"]))
     bf = bv = None
     if c["legacy"] is not None:
@@ -25,19 +25,23 @@ def make_pair(vfvm, oracle, c):
             for ireg in range(bf.shape[1]):
                 if bf[ispec, ireg] == 1e30:
                     vfvm.boundary_dirichlet(sys, ispec + 1, ireg + 1, bv[ispec, ireg])
-    osys = oracle.OracleSystem(c["grid"], c["kind"], c["params"], nodedata=c["nodedata"], bfactors=bf, bvalues=bv)
+    osys = oracle.OracleSystem(c["grid"], c["kind"], c["params"], nodedata=c["nodedata"], bfactors=bf, bvalues=bv,
+                               assembly=assembly)
     return sys, osys
 
 
-@pytest.mark.parametrize("kernel", ["tile", "node"])
+@pytest.mark.parametrize("kernel", ["tile", "node", "cellwise"])
 @pytest.mark.parametrize("name", NAMES)
 def test_assembly_parity(vfvm, oracle, name, kernel, monkeypatch):
     # tile: the edge-once kernel over shared-memory node tiles (the default);
-    # node: the node-centric kernel (multi-region grids; selectable for comparison)
+    # node: the node-centric kernel (multi-region grids, physics with boundary
+    # fluxes; selectable for comparison); cellwise: the default kernel against
+    # the oracle's cellwise assembly (the reference's default mode: the same
+    # operator summed cell by cell)
     if kernel == "node":
         monkeypatch.setenv("VFVM_ASSEMBLY_KERNEL", "node")
     c = case(vfvm, name)
-    sys, osys = make_pair(vfvm, oracle, c)
+    sys, osys = make_pair(vfvm, oracle, c, assembly="cellwise" if kernel == "cellwise" else "edgewise")
     rng = np.random.default_rng(42)
     ns = sys.nspec
     # structural pattern in the oracle: union over states (ExtendableSparse keeps entries)

@@ -151,13 +151,19 @@ def test_learned_gain_over_plain_newton(vfvm, oracle, trained):
     err_pred = np.linalg.norm(pred - up, axis=1)
     err_inival = np.linalg.norm(up, axis=1)
     assert np.median(err_pred / err_inival) < 0.2
-    # ... Newton from it succeeds for (nearly) every instance, and costs no more
-    # Newton steps than from inival (this problem's weak nonlinearity leaves plain
-    # Newton little to save: about three steps to max|F| <= 1e-10 either way)
+    # ... Newton from it succeeds for (nearly) every instance, and the held-out set
+    # costs fewer Krylov iterations and no more Newton steps than from inival
+    # (the work of inexact Newton grows with log(initial error / tolerance), so a
+    # start several times closer saves a share of it; this problem's weak
+    # nonlinearity leaves about three Newton steps either way)
     assert from_guess.sum() >= S - 2
-    assert learned_newton <= 1.15 * plain_newton
+    plain_lin = sum(h.nlin for h in hp)
+    learned_lin = sum(h.nlin for h in hl)
     print(f"held-out: prediction error / inival error median {np.median(err_pred / err_inival):.3f}, "
-          f"Newton steps plain {plain_newton / S:.2f}, learned {learned_newton / S:.2f}")
+          f"Newton steps plain {plain_newton / S:.2f}, learned {learned_newton / S:.2f}, "
+          f"Krylov iterations plain {plain_lin / S:.1f}, learned {learned_lin / S:.1f}")
+    assert learned_newton <= plain_newton
+    assert learned_lin < plain_lin
     # both are solutions of the same problems: agree with each other and with the oracle
     # (max|F| <= 1e-10 fixes the solution of this 33 x 33 problem to about 1e-9)
     assert np.max(np.abs(up - ul)) <= 1e-8 * np.max(np.abs(up))

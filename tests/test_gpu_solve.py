@@ -253,6 +253,25 @@ def test_bipolar_fixed_ramp_block_jacobi_vs_oracle(vfvm, oracle, precision, relt
     assert rel_err(tsol.u[-1], osols[-1]) <= SOL_TOL
 
 
+@pytest.mark.parametrize("dim,breg", [(2, 2), (3, 5)])
+def test_surface_heat_steps_vs_oracle(vfvm, oracle, dim, breg):
+    """Boundary fluxes, boundary storage and boundary sources through implicit
+    Euler steps (device step control) against the oracle's fixed steps."""
+    X = lin(16) if dim == 2 else lin(6)
+    g = vfvm.simplexgrid(*([X] * dim))
+    params = [1.0, 0.3, 0.5, 2.0, 10.0, breg]
+    sys = vfvm.System(g, vfvm.Physics("surface_heat", params))
+    u0 = np.full(g.nnodes, 0.2)
+    control = vfvm.fixed_timesteps(vfvm.SolverControl(maxiters_linear=400, reltol_linear=1e-8), 0.02)
+    tsol = vfvm.solve(sys, inival=u0.reshape(1, -1), times=[0.0, 0.1], control=control)
+    osys = oracle.OracleSystem(g, "surface_heat", params)
+    oc = oracle.fixed_timesteps(oracle.Control(), 0.02)
+    _, osols, _ = oracle.solve_transient(osys, u0, [0.0, 0.1], oc)
+    assert len(tsol.u) == len(osols) == 6
+    assert rel_err(tsol.u[-1], osols[-1]) <= SOL_TOL
+    assert np.max(tsol.u[-1]) > 0.3  # the surface source heated the layer
+
+
 @pytest.mark.parametrize("coarse", [0, 40])
 def test_unstructured_grid_vs_oracle(vfvm, oracle, coarse):
     # Delaunay grid of a jittered lattice, read from a SimplexGrid text file

@@ -32,7 +32,8 @@ def _nvcc():
 # object, so these heavy instantiations compile in parallel.
 INST_SOURCE = "vfvm_persist_inst.cu"
 INST_PHYSICS = ["PhysEx105", "PhysEx106", "PhysEx110", "PhysEx160", "PhysEx207", "PhysEx301", "PhysEx440",
-                "PhysLaplaceDir", "PhysNLPoisson", "PhysPorous", "PhysBipolar", "PhysRD2", "PhysKappaExp"]
+                "PhysLaplaceDir", "PhysNLPoisson", "PhysPorous", "PhysBipolar", "PhysRD2", "PhysKappaExp",
+                "PhysSurfaceHeat"]
 
 
 def sources():

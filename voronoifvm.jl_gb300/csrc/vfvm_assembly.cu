@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(256) assemble_tile_kernel(const AsmTables t, c
         }
       }
     }
-    bnode_terms<Ph, P>(t, ph, K, uK, uKs, time, lambda, fK, jd);
+    bnode_terms<Ph, P>(t, ph, K, uK, uKs, Uold, time, tstepinv, lambda, fK, jd);
 #pragma unroll
     for (int i = 0; i < NS; ++i) {
       F[(size_t)K * NS + i] = fK[i];
@@ -241,7 +241,8 @@ int launch_assemble(vfvm_ctx* c, const double* U, const double* Uold, const doub
   const int blocks = (c->N + threads - 1) / threads;
   return dispatch_physics(c->phys, [&](auto ph) {
     using Ph = decltype(ph);
-    if (!c->multireg && c->ntiles > 0 && !use_node_kernel()) {
+    // the tiled kernel has no boundary-edge terms: physics with bflux use the node kernel
+    if (!Ph::has_bflux && !c->multireg && c->ntiles > 0 && !use_node_kernel()) {
       const TileTables tt = c->tile_tables();
       const size_t b = Jf ? tile_smem_bytes<Ph, float>(c) : tile_smem_bytes<Ph, double>(c);
       if (b) {

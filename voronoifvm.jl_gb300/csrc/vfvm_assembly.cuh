@@ -59,10 +59,12 @@ __device__ __forceinline__ void node_terms(const AsmTables& t, const Ph& ph, int
 }
 
 // Boundary-face items of K in bface order: legacy Dirichlet/Robin data
-// (src/vfvm_assembly.jl:355-387) and breaction (src/vfvm_assembly.jl:388-407).
+// (src/vfvm_assembly.jl:355-387), breaction - bsource (:388-407) and
+// (bstorage - old bstorage) / tstep (:409-440).
 template <class Ph, typename P>
 __device__ __forceinline__ void bnode_terms(const AsmTables& t, const Ph& ph, int K, const double* uK, const P* uKs,
-                                            double time, double lambda, double* fK, P* jd) {
+                                            const double* __restrict__ Uold, double time, double tstepinv,
+                                            double lambda, double* fK, P* jd) {
   constexpr int NS = Ph::NS;
   const double* xK = t.coord + (size_t)K * t.dim;
   const int bbeg = t.bn_ptr[K], bend = t.bn_ptr[K + 1];
@@ -84,18 +86,75 @@ __device__ __forceinline__ void bnode_terms(const AsmTables& t, const Ph& ph, in
         }
       }
     }
-    if (Ph::has_breaction) {
-      BNodeItem bi{K, reg, xK, time, lambda, fac, Dir, nullptr};
+    BNodeItem bi{K, reg, xK, time, lambda, fac, Dir, nullptr};
+    if (Ph::has_breaction || Ph::has_bsource) {
       Dual<NS, P> u[NS], y[NS];
+      double bsrc[NS];
 #pragma unroll
-      for (int i = 0; i < NS; ++i) { u[i] = dseed<NS, P>(uK[i], uKs[i], i); y[i] = dconst<NS, P>(0.0); }
-      ph.breaction(y, u, bi);
+      for (int i = 0; i < NS; ++i) { u[i] = dseed<NS, P>(uK[i], uKs[i], i); y[i] = dconst<NS, P>(0.0); bsrc[i] = 0.0; }
+      if (Ph::has_breaction) ph.breaction(y, u, bi);
+      if (Ph::has_bsource) ph.bsource(bsrc, bi);
       const P facp = P(fac);
 #pragma unroll
       for (int i = 0; i < NS; ++i) {
-        fK[i] += fac * y[i].v;
+        fK[i] += fac * (y[i].v - bsrc[i]);
 #pragma unroll
         for (int j = 0; j < NS; ++j) jd[i * NS + j] += y[i].d[j] * facp;
+      }
+    }
+    if (Ph::has_bstorage) {
+      Dual<NS, P> u[NS], s[NS];
+      double uo[NS], so[NS];
+#pragma unroll
+      for (int i = 0; i < NS; ++i) {
+        u[i] = dseed<NS, P>(uK[i], uKs[i], i);
+        s[i] = dconst<NS, P>(0.0);
+        uo[i] = Uold[(size_t)K * NS + i];
+        so[i] = 0.0;
+      }
+      ph.bstorage(s, u, bi);
+      ph.bstorage(so, uo, bi);
+      const P ft = P(fac * tstepinv);
+#pragma unroll
+      for (int i = 0; i < NS; ++i) {
+        fK[i] += fac * (s[i].v - so[i]) * tstepinv;
+#pragma unroll
+        for (int j = 0; j < NS; ++j) jd[i * NS + j] += s[i].d[j] * ft;
+      }
+    }
+  }
+}
+
+// Boundary-edge items of Jacobian slot s (edge A-B, A < B), evaluated from
+// node K's end: assemble_bedges (src/vfvm_assembly.jl:444-510), the same sign
+// and factor placement as a bulk edge (first node +f, second -f).
+template <class Ph, typename P>
+__device__ __forceinline__ void bedge_terms(const AsmTables& t, const Ph& ph, int s, int A, int B, bool kfirst,
+                                            const double* uA, const P* uAs, const double* uB, const P* uBs,
+                                            double time, double lambda, double* fK, P* jd, P* jo) {
+  constexpr int NS = Ph::NS;
+  for (int it = t.sbe_ptr[s]; it < t.sbe_ptr[s + 1]; ++it) {
+    const double fac = t.sbe_fac[it];
+    BEdgeItem be{A, B, t.sbe_reg[it], t.coord + (size_t)A * t.dim, t.coord + (size_t)B * t.dim, time, lambda};
+    Dual<2 * NS, P> ua[NS], ub[NS], f[NS];
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+      ua[i] = dseed<2 * NS, P>(uA[i], uAs[i], i);
+      ub[i] = dseed<2 * NS, P>(uB[i], uBs[i], NS + i);
+      f[i] = dconst<2 * NS, P>(0.0);
+    }
+    ph.bflux(f, ua, ub, be);
+    const P facp = P(fac);
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+      if (kfirst) {
+        fK[i] += fac * f[i].v;
+#pragma unroll
+        for (int j = 0; j < NS; ++j) { jd[i * NS + j] += f[i].d[j] * facp; jo[i * NS + j] += f[i].d[NS + j] * facp; }
+      } else {
+        fK[i] += -(fac * f[i].v);
+#pragma unroll
+        for (int j = 0; j < NS; ++j) { jd[i * NS + j] += (-f[i].d[NS + j]) * facp; jo[i * NS + j] += (-f[i].d[j]) * facp; }
       }
     }
   }
@@ -173,6 +232,12 @@ __device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, 
         }
       }
     }
+    if constexpr (Ph::has_bflux) {
+      if (t.sbe_ptr) {
+        if (kfirst) bedge_terms<Ph, P>(t, ph, s, K, M, true, uK, uKs, uM, uMs, time, lambda, fK, jd, jo);
+        else bedge_terms<Ph, P>(t, ph, s, M, K, false, uM, uMs, uK, uKs, time, lambda, fK, jd, jo);
+      }
+    }
     if (J) {
       P* Js = J + (size_t)s * NS * NS;
 #pragma unroll
@@ -180,7 +245,7 @@ __device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, 
     }
   }
 
-  bnode_terms<Ph, P>(t, ph, K, uK, uKs, time, lambda, fK, jd);
+  bnode_terms<Ph, P>(t, ph, K, uK, uKs, Uold, time, tstepinv, lambda, fK, jd);
 
   bool bad = false;
 #pragma unroll

@@ -238,6 +238,13 @@ struct EdgeItem {
   double time, lambda;
   const double* dataK; const double* dataL;
 };
+// boundary edge: an edge of a boundary face (the reference's BEdge,
+// src/vfvm_geometryitems.jl:504-578), K = first node, L = second node
+struct BEdgeItem {
+  int K, L, region;      // region: the boundary region of the face
+  const double* xK; const double* xL;
+  double time, lambda;
+};
 struct BNodeItem {
   int index, region;
   const double* x;

@@ -111,6 +111,24 @@ void bface_factors(int dim, const double* const* x, double* nodef) {
   }
 }
 
+// Edge factors of the edges of a boundary face (the bfacefactors! edge
+// parameters, src/vfvm_formfactors.jl:263-274 for a segment, :293-332 for a
+// triangle): 1 / length for a segment; half the cotangent of the opposite angle
+// for a triangle, local edge e opposite local node e.
+void bface_edge_factors(int dim, const double* const* x, double* edgef) {
+  if (dim == 2) {
+    edgef[0] = 1.0 / std::sqrt(dist2(x[0], x[1], 2));
+    return;
+  }
+  double l2[3];
+  for (int e = 0; e < 3; ++e) l2[e] = dist2(x[kTriEdges[e][0]], x[kTriEdges[e][1]], 3);
+  double g[3];
+  for (int e = 0; e < 3; ++e) g[e] = (l2[(e + 1) % 3] + l2[(e + 2) % 3] - l2[e]) * l2[e];
+  double area = 0.25 * std::sqrt(g[0] + g[1] + g[2]);
+  double s = 1.0 / (8.0 * area);
+  for (int e = 0; e < 3; ++e) edgef[e] = g[e] * s / l2[e];
+}
+
 struct RegFac { int reg; double fac; };
 
 inline void add_regfac(std::vector<RegFac>& v, int reg, double f) {
@@ -157,13 +175,45 @@ void probe_t(const Ph& ph0, const double* params, int dim, const std::vector<int
     for (int reg : bregs) {
       double dv[NS];
       BNodeItem bi{0, reg, x, 0.5, 0.5, 1.0, kDirichlet, dv};
-      Dual<NS> u[NS], yb[NS];
-      for (int i = 0; i < NS; ++i) { u[i] = dseed<NS, double>(U(rng), i); yb[i] = dconst<NS, double>(0); }
+      Dual<NS> u[NS], yb[NS], sb[NS];
+      for (int i = 0; i < NS; ++i) {
+        u[i] = dseed<NS, double>(U(rng), i);
+        yb[i] = dconst<NS, double>(0);
+        sb[i] = dconst<NS, double>(0);
+      }
       if (Ph::has_breaction) ph.breaction(yb, u, bi);
+      if (Ph::has_bstorage) ph.bstorage(sb, u, bi);
       for (int i = 0; i < NS; ++i)
         for (int j = 0; j < NS; ++j)
-          if (yb[i].d[j] != 0.0) bm[i * NS + j] = 1;
+          if (yb[i].d[j] != 0.0 || sb[i].d[j] != 0.0) bm[i * NS + j] = 1;
     }
+  }
+}
+
+// Structural mask of bflux on boundary region reg: which partials d f_i /
+// d u_first,j and d f_i / d u_second,j can be nonzero (NS x 2NS).
+template <class Ph>
+void probe_bflux_t(const Ph& ph0, const double* params, int reg, std::vector<uint8_t>& out) {
+  constexpr int NS = Ph::NS;
+  Ph ph = ph0;
+  ph.load(params);
+  out.assign(NS * 2 * NS, 0);
+  if (!Ph::has_bflux) return;
+  std::mt19937_64 rng(4321);
+  std::uniform_real_distribution<double> U(0.1, 1.1), X(0.0, 1.0);
+  for (int sample = 0; sample < 6; ++sample) {
+    double x[3] = {X(rng), X(rng), X(rng)}, y[3] = {X(rng), X(rng), X(rng)};
+    BEdgeItem be{0, 1, reg, x, y, 0.5, 0.5};
+    Dual<2 * NS> uk[NS], ul[NS], f[NS];
+    for (int i = 0; i < NS; ++i) {
+      uk[i] = dseed<2 * NS, double>(U(rng), i);
+      ul[i] = dseed<2 * NS, double>(U(rng), NS + i);
+      f[i] = dconst<2 * NS, double>(0);
+    }
+    ph.bflux(f, uk, ul, be);
+    for (int i = 0; i < NS; ++i)
+      for (int j = 0; j < 2 * NS; ++j)
+        if (f[i].d[j] != 0.0) out[i * 2 * NS + j] = 1;
   }
 }
 
@@ -192,6 +242,7 @@ AsmTables vfvm_ctx::tables() const {
   t.nitem_ptr = multireg ? nitem_ptr.p : nullptr; t.nitem_reg = nitem_reg.p; t.nitem_fac = nitem_fac.p;
   t.sitem_ptr = multireg ? sitem_ptr.p : nullptr; t.sitem_reg = sitem_reg.p; t.sitem_fac = sitem_fac.p;
   t.bn_ptr = bn_ptr.p; t.bn_reg = bn_reg.p; t.bn_fac = bn_fac.p;
+  t.sbe_ptr = sbe_ptr.n ? sbe_ptr.p : nullptr; t.sbe_reg = sbe_reg.p; t.sbe_fac = sbe_fac.p;
   t.params = params.p; t.nodedata = nodedata.p; t.nnd = nnd;
   t.bfactors = bfactors.p; t.bvalues = bvalues.p; t.nbregions = nbregions; t.has_legacy = has_legacy ? 1 : 0;
   return t;
@@ -382,6 +433,58 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
     c->nbregions = std::max(maxbreg, ph->nbregions);
   }
 
+  // --- boundary-edge items (physics with bflux): the edges of the boundary
+  // faces with their face edge factors, summed per (edge, boundary region) and
+  // listed under both Jacobian slots of the edge (assemble_bedges,
+  // src/vfvm_assembly.jl:444-510; factors src/vfvm_formfactors.jl:263-332)
+  const bool has_bflux = dispatch_physics(c->phys, [](auto phy) { return decltype(phy)::has_bflux ? 1 : 0; }) == 1;
+  std::vector<int> sbe_ptr, sbe_reg;
+  std::vector<double> sbe_fac;
+  std::map<int, std::vector<uint8_t>> bem_of_reg;  // structural bflux mask per boundary region
+  if (has_bflux && dim >= 2 && nbf > 0) {
+    std::map<int64_t, std::vector<RegFac>> be;  // key: lo * N + hi
+    const double* xs[3];
+    double ef[3];
+    const int nle_b = dim == 2 ? 1 : 3;
+    for (int b = 0; b < nbf; ++b) {
+      for (int v = 0; v < nbn; ++v) xs[v] = &c->h_coord[(size_t)g->bfacenodes[v + (size_t)nbn * b] * dim];
+      bface_edge_factors(dim, xs, ef);
+      for (int e = 0; e < nle_b; ++e) {
+        int a = g->bfacenodes[(dim == 2 ? 0 : kTriEdges[e][0]) + (size_t)nbn * b];
+        int bb = g->bfacenodes[(dim == 2 ? 1 : kTriEdges[e][1]) + (size_t)nbn * b];
+        if (a > bb) std::swap(a, bb);
+        add_regfac(be[(int64_t)a * N + bb], g->bfaceregions[b], ef[e]);
+      }
+    }
+    sbe_ptr.assign(c->nnzb + 1, 0);
+    int64_t found = 0;
+    for (int k = 0; k < N; ++k)
+      for (int s = c->h_browptr[k]; s < c->h_browptr[k + 1]; ++s) {
+        const int m = c->h_bcol[s];
+        if (m != k) {
+          auto it = be.find((int64_t)std::min(k, m) * N + std::max(k, m));
+          if (it != be.end()) {
+            ++found;
+            for (auto& r : it->second) { sbe_reg.push_back(r.reg); sbe_fac.push_back(r.fac); }
+          }
+        }
+        sbe_ptr[s + 1] = (int)sbe_reg.size();
+      }
+    if (found != 2 * (int64_t)be.size()) {  // every boundary-face edge is an edge of the cells
+      fprintf(stderr, "vfvm_create: boundary-face edges that are not cell edges\n");
+      *status = VFVM_ERR_INPUT;
+      delete c;
+      return nullptr;
+    }
+    std::vector<double> p(ph->params, ph->params + ph->nparams);
+    p.resize(16, 0.0);
+    for (int b = 0; b < nbf; ++b) {
+      const int reg = g->bfaceregions[b];
+      if (!bem_of_reg.count(reg))
+        dispatch_physics(c->phys, [&](auto phy) { probe_bflux_t(phy, p.data(), reg, bem_of_reg[reg]); return 0; });
+    }
+  }
+
   // --- legacy boundary data (boundary_dirichlet!(sys, ispec, ireg, val) etc.)
   std::vector<double> bfac_h((size_t)ns * c->nbregions, 0.0), bval_h((size_t)ns * c->nbregions, 0.0);
   if (ph->nbregions > 0 && ph->bfactors && ph->bvalues) {
@@ -439,6 +542,15 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
         for (int it = bn_ptr[k]; it < bn_ptr[k + 1]; ++it)
           for (int i = 0; i < ns; ++i)
             if (bn_reg[it] - 1 < c->nbregions && bfac_h[i + (size_t)ns * (bn_reg[it] - 1)] != 0.0) legdiag[i] = 1;
+      // boundary-edge (bflux) partials of this row: per slot, and summed into the diagonal
+      auto bflux_on = [&](int s, bool first_col, int i, int j) {
+        if (sbe_ptr.empty()) return false;
+        for (int it = sbe_ptr[s]; it < sbe_ptr[s + 1]; ++it) {
+          const auto& mk = bem_of_reg[sbe_reg[it]];
+          if (mk[i * 2 * ns + (first_col ? 0 : ns) + j]) return true;
+        }
+        return false;
+      };
       for (int i = 0; i < ns; ++i) {
         for (int s = c->h_browptr[k]; s < c->h_browptr[k + 1]; ++s) {
           int m = c->h_bcol[s];
@@ -450,10 +562,14 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
                 on = on || bm[i * ns + j];
                 if (i == j && legdiag[i]) on = true;
               }
+              for (int s2 = c->h_browptr[k]; !on && s2 < c->h_browptr[k + 1]; ++s2) {
+                const int m2 = c->h_bcol[s2];
+                if (m2 != k) on = bflux_on(s2, k < m2, i, j);  // d f / d u_K of K's boundary edges
+              }
             } else if (k < m) {
-              on = em[i * 2 * ns + ns + j];  // k is the first node: d f / d u_second
+              on = em[i * 2 * ns + ns + j] || bflux_on(s, false, i, j);  // k first: d f / d u_second
             } else {
-              on = em[i * 2 * ns + j];       // k is the second node: d f / d u_first
+              on = em[i * 2 * ns + j] || bflux_on(s, true, i, j);        // k second: d f / d u_first
             }
             if (on) {
               c->h_colind.push_back(m * ns + j);
@@ -583,6 +699,11 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
   SETUP_CUDA(c->bfactors.upload(bfac_h));
   SETUP_CUDA(c->bvalues.upload(bval_h));
   SETUP_CUDA(c->dirichlet_dof.upload(dir_dof));
+  if (!sbe_ptr.empty()) {
+    SETUP_CUDA(c->sbe_ptr.upload(sbe_ptr));
+    SETUP_CUDA(c->sbe_reg.upload(sbe_reg));
+    SETUP_CUDA(c->sbe_fac.upload(sbe_fac));
+  }
   const size_t n = (size_t)N * ns;
   SETUP_CUDA(c->U.alloc(n));
   SETUP_CUDA(c->Uold.alloc(n));

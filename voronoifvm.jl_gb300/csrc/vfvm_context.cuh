@@ -50,6 +50,10 @@ struct AsmTables {
   const int* sitem_ptr; const int* sitem_reg; const double* sitem_fac;
   // boundary-node items grouped by node (bface order within a node)
   const int* bn_ptr; const int* bn_reg; const double* bn_fac;
+  // boundary-edge items (edges of boundary faces, per boundary region) grouped by
+  // Jacobian slot: both slots of an edge list its items; nullptr when the
+  // physics has no bflux
+  const int* sbe_ptr; const int* sbe_reg; const double* sbe_fac;
   // physics data
   const double* params;
   const double* nodedata; int nnd;
@@ -130,6 +134,8 @@ struct vfvm_ctx {
   vfvm::DBuf<float> slot_facf;
   vfvm::DBuf<int> browptr, bcol, diag, nitem_ptr, nitem_reg, sitem_ptr, sitem_reg, bn_ptr, bn_reg;
   vfvm::DBuf<uint8_t> dirichlet_dof;       // 1 where a Dirichlet penalty acts on the dof
+  vfvm::DBuf<int> sbe_ptr, sbe_reg;         // boundary-edge items per slot (physics with bflux)
+  vfvm::DBuf<double> sbe_fac;
 
   // scalar (reference) pattern
   int64_t nnz = 0;

@@ -38,6 +38,7 @@ vfvm_ctx* clone_context(const vfvm_ctx* b, const vfvm_physics_desc* ph, int* sta
   c->nitem_ptr.view(b->nitem_ptr); c->nitem_reg.view(b->nitem_reg); c->sitem_ptr.view(b->sitem_ptr);
   c->sitem_reg.view(b->sitem_reg); c->bn_ptr.view(b->bn_ptr); c->bn_reg.view(b->bn_reg);
   c->dirichlet_dof.view(b->dirichlet_dof); c->pmap.view(b->pmap);
+  c->sbe_ptr.view(b->sbe_ptr); c->sbe_reg.view(b->sbe_reg); c->sbe_fac.view(b->sbe_fac);
   c->color_nodes.view(b->color_nodes); c->color_ptr.view(b->color_ptr);
   c->lower_ptr.view(b->lower_ptr); c->lower_slots.view(b->lower_slots);
   c->ell_w = b->ell_w; c->lo_w = b->lo_w; c->up_w = b->up_w;

@@ -18,10 +18,16 @@ namespace vfvm {
 
 struct PhysBase {
   static constexpr bool has_reaction = false, has_storage = false, has_source = false, has_breaction = false;
+  // boundary callbacks beyond breaction: bflux (boundary edges), bstorage, bsource
+  // (src/vfvm_physics.jl:82-180)
+  static constexpr bool has_bflux = false, has_bstorage = false, has_bsource = false;
   template <class T> VFVM_HD void reaction(T*, const T*, const NodeItem&) const {}
   template <class T> VFVM_HD void storage(T*, const T*, const NodeItem&) const {}
   VFVM_HD void source(double*, const NodeItem&) const {}
   template <class T> VFVM_HD void breaction(T*, const T*, const BNodeItem&) const {}
+  template <class T> VFVM_HD void bflux(T*, const T*, const T*, const BEdgeItem&) const {}
+  template <class T> VFVM_HD void bstorage(T*, const T*, const BNodeItem&) const {}
+  VFVM_HD void bsource(double*, const BNodeItem&) const {}
 };
 
 // examples/Example105_NonlinearPoisson1D.jl:41-60;  params: eps
@@ -235,11 +241,45 @@ struct PhysKappaExp : PhysBase {
   template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const { boundary_dirichlet(f, u, b, 0, b.region, 0.0); }
 };
 
+// Heat equation with a conducting surface layer on boundary region breg (the
+// single-species form of examples/Example311_HeatEquation_BoundaryDiffusion.jl):
+//   u_t - div(eps grad u) = 0 in the domain (storage u, flux eps (u_K - u_L));
+//   on region breg: surface diffusion along the boundary edges (bflux
+//   eps_s (u_K - u_L)), surface capacity (bstorage c_s u), heat loss k u^3
+//   (breaction) and a heat source q0 exp(-20 ((x-1/2)^2 + (y-1/2)^2)) (bsource);
+//   the other boundary regions are insulated.  Grids of dimension 2 or 3.
+// params: eps, eps_s, c_s, k, q0, breg
+struct PhysSurfaceHeat : PhysBase {
+  static constexpr int NS = 1;
+  static constexpr bool has_storage = true, has_breaction = true, has_bflux = true, has_bstorage = true,
+                        has_bsource = true;
+  double eps, eps_s, c_s, k, q0;
+  int breg;
+  VFVM_HD void load(const double* p) { eps = p[0]; eps_s = p[1]; c_s = p[2]; k = p[3]; q0 = p[4]; breg = (int)p[5]; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const { f[0] = (uK[0] - uL[0]) * eps; }
+  template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const { f[0] = u[0]; }
+  template <class T> VFVM_HD void bflux(T* f, const T* uK, const T* uL, const BEdgeItem& e) const {
+    if (e.region == breg) f[0] = (uK[0] - uL[0]) * eps_s;
+  }
+  template <class T> VFVM_HD void bstorage(T* f, const T* u, const BNodeItem& b) const {
+    if (b.region == breg) f[0] = u[0] * c_s;
+  }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const {
+    if (b.region == breg) f[0] = cube(u[0]) * k;
+  }
+  VFVM_HD void bsource(double* f, const BNodeItem& b) const {
+    if (b.region == breg) {
+      const double x1 = b.x[0] - 0.5, x2 = b.x[1] - 0.5;
+      f[0] = q0 * ::exp(-20.0 * (x1 * x1 + x2 * x2));
+    }
+  }
+};
+
 inline int physics_nspec(int id) {
   switch (id) {
     case VFVM_PHYS_EX105: case VFVM_PHYS_EX106: case VFVM_PHYS_EX207: case VFVM_PHYS_EX301:
     case VFVM_PHYS_EX440: case VFVM_PHYS_LAPLACE_DIRICHLET: case VFVM_PHYS_NLPOISSON:
-    case VFVM_PHYS_POROUS: case VFVM_PHYS_KAPPA_EXP: return 1;
+    case VFVM_PHYS_POROUS: case VFVM_PHYS_KAPPA_EXP: case VFVM_PHYS_SURFACE_HEAT: return 1;
     case VFVM_PHYS_EX110: case VFVM_PHYS_EX160: case VFVM_PHYS_RD2: return 2;
     case VFVM_PHYS_BIPOLAR: return 3;
   }
@@ -252,6 +292,7 @@ inline int physics_nparams(int id) {
     case VFVM_PHYS_EX110: return 2;
     case VFVM_PHYS_EX160: case VFVM_PHYS_RD2: return 3;
     case VFVM_PHYS_BIPOLAR: return 7;
+    case VFVM_PHYS_SURFACE_HEAT: return 6;
   }
   return 0;
 }
@@ -274,6 +315,7 @@ int dispatch_physics(int id, Fn&& fn) {
     case VFVM_PHYS_BIPOLAR: return fn(PhysBipolar{});
     case VFVM_PHYS_RD2: return fn(PhysRD2{});
     case VFVM_PHYS_KAPPA_EXP: return fn(PhysKappaExp{});
+    case VFVM_PHYS_SURFACE_HEAT: return fn(PhysSurfaceHeat{});
   }
   return VFVM_ERR_INPUT;
 }

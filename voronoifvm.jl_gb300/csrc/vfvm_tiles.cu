@@ -165,7 +165,7 @@ int build_assembly_tiles(vfvm_ctx* c, const std::vector<double>& slot_fac) {
   }
   c->ntiles = P.ntiles;
   c->tile_nodes = P.tile_nodes;
-  c->tile_threads = std::max(P.tile_nodes, 128);
+  c->tile_threads = 256;  // all threads evaluate edges; the first tile_nodes also gather nodes
   c->tile_maxloc = P.maxloc;
   c->tile_maxedges = P.maxedges;
   c->tile_edge_evals = (int64_t)P.edge_ab.size();

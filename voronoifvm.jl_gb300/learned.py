@@ -34,7 +34,8 @@ from .batch import BatchSolver
 from .grid import simplexgrid
 from .system import NewtonSolverHistory, Physics, SolverControl, System, _raise
 
-__all__ = ["grf_logkappa", "kappa_instance", "kappa_scale", "Network", "KappaSweep", "LearnedInitialIterate"]
+__all__ = ["grf_logkappa", "kappa_instance", "kappa_scale", "mesh_symmetries", "Network", "KappaSweep",
+           "LearnedInitialIterate"]
 
 
 def grf_logkappa(n: int, seed: int, ell: float = 0.1, sigma: float = 1.0, modes: int = 20,
@@ -77,6 +78,20 @@ def kappa_instance(n: int, seed: int, ell: float = 0.1, sigma: float = 1.0):
     G = grf_logkappa(n, seed, ell, sigma)
     f = float(np.random.default_rng([int(seed), 0x66]).uniform(-1.0, 1.0))
     return G, f
+
+
+def mesh_symmetries(a: np.ndarray, m: int):
+    """The four images of node fields on an m x m square grid (rows of ``a``,
+    node order ix + m*iy) under the symmetries of the triangulation: identity,
+    rotation by 180 degrees, reflection across the diagonal x = y and across
+    x = 1 - y.  simplexgrid splits every square along its (0,0)-(1,1)
+    diagonal, which these four maps (and not the rotations by 90 degrees)
+    preserve, so the discrete kappa_exp problem -- u = 0 on the whole boundary,
+    isotropic kappa -- maps each solution onto the solution of the mapped
+    coefficient field exactly.  Returns an array of shape (4, S, m*m)."""
+    A = np.asarray(a).reshape(-1, m, m)  # [s, iy, ix]
+    T = A.transpose(0, 2, 1)
+    return np.stack([A, A[:, ::-1, ::-1], T, T[:, ::-1, ::-1]]).reshape(4, A.shape[0], m * m)
 
 
 class Network:
@@ -220,6 +235,18 @@ class LearnedInitialIterate:
         """Values at the coarse subgrid nodes of (S, n*n) fine node arrays."""
         F = np.asarray(fine).reshape(-1, self.n, self.n)  # [iy, ix]
         return F[:, ::self.r, ::self.r].reshape(F.shape[0], -1)
+
+    def augment(self, X: np.ndarray, T: np.ndarray, scale=None):
+        """Training pairs under the mesh symmetries (mesh_symmetries): features X
+        (S, nc*nc + 1: coarse field, then f) and coarse targets T (S, nc*nc)
+        become 4 S pairs; `scale` (S,) is repeated alongside."""
+        nc2 = self.nc * self.nc
+        Xs = mesh_symmetries(X[:, :nc2], self.nc)
+        fcol = np.broadcast_to(X[:, nc2:], (4,) + X[:, nc2:].shape)
+        Xa = np.concatenate([Xs, fcol], axis=2).reshape(-1, X.shape[1]).astype(X.dtype)
+        Ta = mesh_symmetries(T, self.nc).reshape(-1, nc2)
+        Sa = None if scale is None else np.tile(np.asarray(scale), 4)
+        return Xa, Ta, Sa
 
     def features(self, logk: np.ndarray, f: np.ndarray) -> np.ndarray:
         return np.concatenate([self.coarse(logk), np.asarray(f).reshape(-1, 1)], axis=1).astype(np.float32)

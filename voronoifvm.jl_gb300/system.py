@@ -218,7 +218,15 @@ class System:
     """A finite-volume system on a grid with a registered device physics.
 
     The device context (tables, form factors, matrix pattern) is created on the
-    first call that needs it and rebuilt when the legacy boundary data change."""
+    first call that needs it and rebuilt when the legacy boundary data change.
+
+    ``assembly``: the reference's :cellwise (its default) and :edgewise modes
+    assemble the same operator -- the sum over cells of the cell-local terms --
+    and differ only in summation order.  The device assembles both from
+    edgewise tables (each edge's factors summed over its cells once, on the
+    host), so every edge flux is evaluated once per edge instead of once per
+    cell sharing it; the result agrees with the reference's cellwise summation
+    to rounding."""
 
     def __init__(self, grid: Grid, physics: Physics, species: Sequence[int] = (1,), is_linear: bool = False,
                  assembly: str = "edgewise", unknown_storage: str = "dense"):
