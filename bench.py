@@ -356,9 +356,11 @@ METRIC_L = ("Newton solves/s at ||F||<=1e-10 (stationary -div(kappa grad u) + ex
 
 
 # DRAM bytes (read + write) of one BiCGStab iteration of the sweep engine per
-# system, from an ncu capture of every kernel of one iteration with all 512
-# systems active (kappa-exp 257 x 257, mixed form); None until measured.
-SWEEP_DRAM_BYTES_PER_SYSTEM_ITERATION = None
+# system: ncu's dram__bytes_read.sum + dram__bytes_write.sum over the 27 kernels
+# of one iteration with all 256 systems of a 256-instance batch active
+# (kappa-exp 257 x 257, mixed form), divided by 256: 5051 MB for the
+# iteration (VFVM_SWEEP_EAGER=1 bench.py --mode batch --batch-n 256 under ncu).
+SWEEP_DRAM_BYTES_PER_SYSTEM_ITERATION = 19.73e6
 
 
 def heldout_seeds(rank):
@@ -696,9 +698,10 @@ def run_learned(args, rank, world):
                            sample=args.single_sample)
     # --- e2e through the public API with host buffers: the user's inputs are the
     # node data kappa = exp(G), the sources f and inival in pinned host memory;
-    # per step: features (log kappa at the coarse subgrid nodes) on the host,
-    # H2D copies, load of all instances on the device, prediction, guarded
-    # solve, D2H of the solutions
+    # per step: the per-instance output factors (f - 1) on the host, H2D copies,
+    # load of all instances on the device, the network features on the device
+    # (log kappa around the coarse subgrid nodes), prediction, guarded solve,
+    # D2H of the solutions
     kappa_h = torch.from_numpy(np.exp(logk_e)).pin_memory()
     f_h = torch.from_numpy(np.ascontiguousarray(f_e, dtype=np.float64)).pin_memory()
     inival_h = torch.zeros(NEVAL * N, dtype=torch.float64).pin_memory()
@@ -711,15 +714,15 @@ def run_learned(args, rank, world):
         flush.fill_(float(it))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        Xh = torch.from_numpy(model.features_from_kappa(kappa_np, f_np)).pin_memory()
         Sh = torch.from_numpy(lk.kappa_scale(f_np)).pin_memory()
         ta = time.perf_counter()
         kappa_d.copy_(kappa_h, non_blocking=True)
         f_d.copy_(f_h, non_blocking=True)
         ini_d.copy_(inival_h, non_blocking=True)
-        Xd, Sd = Xh.to(cuda, non_blocking=True), Sh.to(cuda, non_blocking=True)
+        Sd = Sh.to(cuda, non_blocking=True)
         sweep.load_device(kappa_d, f_d)  # returns once the copies before it are complete
         tb = time.perf_counter()
+        Xd = model.features_device(kappa_d.view(NEVAL, N), f_d)
         g = model.predict_device(Xd, scale=Sd)
         sweep.solve_device(ini_d.data_ptr(), U.data_ptr(), ctl_l, guess_dev=g.data_ptr())
         tc = time.perf_counter()
@@ -729,10 +732,10 @@ def run_learned(args, rank, world):
             e2e.append(t1 - t0)
             phases.append([ta - t0, tb - ta, tc - tb, t1 - tc])
     e2e_value = replica_throughput(NEVAL, float(np.mean(e2e)), world)
-    e2e_phases = dict(zip(("features_ms", "h2d_and_load_ms", "predict_and_solve_ms", "d2h_ms"),
+    e2e_phases = dict(zip(("host_prep_ms", "h2d_and_load_ms", "features_predict_and_solve_ms", "d2h_ms"),
                           (1e3 * np.mean(phases, axis=0)).tolist()))
     e2e_vs_device = float(np.max(np.abs(U_h.numpy().reshape(NEVAL, N) - U_learned)))
-    h2d = int(kappa_h.numel() * 8 + f_h.numel() * 8 + Xh.numel() * 4 + Sh.numel() * 8 + inival_h.numel() * 8)
+    h2d = int(kappa_h.numel() * 8 + f_h.numel() * 8 + Sh.numel() * 8 + inival_h.numel() * 8)
     d2h = int(U_h.numel() * 8)
     # --- roofline of the dominant kernel (the batched Newton launch)
     peak, peak_kind = peaks()

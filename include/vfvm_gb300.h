@@ -358,6 +358,16 @@ int vfvm_prolong_bilinear(int32_t batch, int32_t nc, int32_t ratio, const float*
                           double scale, double shift, const double* inst_scale, double* fine, int64_t fine_stride,
                           void* stream);
 
+/* Network input features on the device: for batch positive node fields on
+ * nested square grids ((nc-1)*ratio+1 nodes per side, FP64, the node order of
+ * simplexgrid), X[b] = the mean of log(field) over the (2*half+1)^2 fine nodes
+ * around each node of the nc x nc coarse subgrid (clipped at the boundary;
+ * half = 0: the node's own value), then extra[b] (NULL: 0).  X is FP32, batch
+ * rows of nc*nc + 1 values.  Device pointers, enqueued on stream (NULL: the
+ * legacy default stream). */
+int vfvm_coarse_log_features(int32_t batch, int32_t nc, int32_t ratio, int32_t half, const double* field,
+                             int64_t field_stride, const double* extra, float* X, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -196,3 +196,20 @@ def test_guarded_start_falls_back(vfvm, trained):
     assert np.array_equal(up[:2], ug[:2])  # the fallback is plain Newton from inival
     assert np.max(np.abs(up - ug)) <= 1e-8 * np.max(np.abs(up))
     sweep.close()
+
+
+@pytest.mark.parametrize("half", [0, 2])
+def test_device_features_match_host(vfvm, half):
+    """vfvm_coarse_log_features (log of the node data, window means around the
+    coarse subgrid nodes, the source f last) equals the host features."""
+    import torch
+    lk = vfvm.learned
+    model = lk.LearnedInitialIterate(N_FINE, N_COARSE, hidden=32, layers=2, max_batch=8, seed=0, half=half)
+    inst = [lk.kappa_instance(N_FINE, 500 + s) for s in range(5)]
+    logk = np.array([a for a, _ in inst])
+    f = np.array([b for _, b in inst])
+    Xh = model.features(logk, f)
+    Xd = model.features_device(torch.from_numpy(np.exp(logk)).cuda(), torch.from_numpy(f).cuda()).cpu().numpy()
+    assert Xd.shape == Xh.shape
+    np.testing.assert_allclose(Xd, Xh, rtol=1e-6, atol=1e-6)
+    model.close()

@@ -269,7 +269,7 @@ def test_surface_heat_steps_vs_oracle(vfvm, oracle, dim, breg):
     _, osols, _ = oracle.solve_transient(osys, u0, [0.0, 0.1], oc)
     assert len(tsol.u) == len(osols) == 6
     assert rel_err(tsol.u[-1], osols[-1]) <= SOL_TOL
-    assert np.max(tsol.u[-1]) > 0.3  # the surface source heated the layer
+    assert np.max(tsol.u[-1]) > 0.2 + 1e-3  # the surface source warmed the layer above its start
 
 
 @pytest.mark.parametrize("coarse", [0, 40])

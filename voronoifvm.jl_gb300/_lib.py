@@ -109,6 +109,7 @@ SIGNATURES = {
     "vfvm_mlp_train_step": (ctypes.c_int, [c_vp, c_i32, c_vp, c_vp, ctypes.c_float, P(ctypes.c_float)]),
     "vfvm_prolong_bilinear": (ctypes.c_int, [c_i32, c_i32, c_i32, c_vp, c_i64, c_d, c_d, c_vp, c_vp, c_i64, c_vp]),
     "vfvm_check_bounded_wait": (ctypes.c_int, [c_i32, P(c_i32), P(ctypes.c_float)]),
+    "vfvm_coarse_log_features": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_vp, c_i64, c_vp, c_vp, c_vp]),
 }
 
 _lib = None

@@ -482,3 +482,49 @@ extern "C" int vfvm_prolong_bilinear(int32_t batch, int32_t nc, int32_t ratio, c
   VFVM_CUDA(cudaGetLastError());
   return VFVM_OK;
 }
+
+namespace vfvm {
+
+// X[b][c] = mean of log(field[b][k]) over the fine nodes k of the window of
+// half-width `half` around coarse node c (clipped at the boundary; half = 0:
+// the node itself), c = cx + nc*cy at fine node (cx*r, cy*r); X[b][nc*nc] = extra[b]
+__global__ void coarse_log_features_kernel(int batch, int nc, int r, int half, const double* __restrict__ field,
+                                           int64_t fstride, const double* __restrict__ extra, float* __restrict__ X) {
+  const int nf = (nc - 1) * r + 1;
+  const int nin = nc * nc + 1;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)batch * nin) return;
+  const int b = (int)(i / nin), c = (int)(i % nin);
+  if (c == nc * nc) {
+    X[i] = extra ? (float)extra[b] : 0.0f;
+    return;
+  }
+  const int cx = c % nc, cy = c / nc;
+  const int x0 = max(cx * r - half, 0), x1 = min(cx * r + half, nf - 1);
+  const int y0 = max(cy * r - half, 0), y1 = min(cy * r + half, nf - 1);
+  const double* F = field + b * fstride;
+  double s = 0.0;
+  for (int y = y0; y <= y1; ++y)
+    for (int x = x0; x <= x1; ++x) s += ::log(F[x + (int64_t)nf * y]);
+  X[i] = (float)(s / ((x1 - x0 + 1) * (y1 - y0 + 1)));
+}
+
+}  // namespace vfvm
+
+// Network input features of a batch of positive node fields (e.g. the kappa of
+// the kappa_exp instances) on nested square grids: the mean of log(field) over
+// a (2 half + 1)^2 window around each node of the nc x nc coarse subgrid (every
+// ratio-th fine node; half = 0 takes the node's own value), then one extra
+// scalar per instance (e.g. the source f).  Device pointers; X is FP32, batch
+// rows of nc*nc + 1 values; enqueued on stream (NULL: the legacy default stream).
+extern "C" int vfvm_coarse_log_features(int32_t batch, int32_t nc, int32_t ratio, int32_t half, const double* field,
+                                        int64_t field_stride, const double* extra, float* X, void* stream) {
+  if (batch < 1 || nc < 2 || ratio < 1 || half < 0 || half > ratio || !field || !X) return VFVM_ERR_INPUT;
+  const int64_t nf = (int64_t)(nc - 1) * ratio + 1;
+  if (field_stride < nf * nf) return VFVM_ERR_INPUT;
+  const int64_t total = (int64_t)batch * (nc * nc + 1);
+  coarse_log_features_kernel<<<nb(total), 256, 0, (cudaStream_t)stream>>>(batch, nc, ratio, half, field, field_stride,
+                                                                         extra, X);
+  VFVM_CUDA(cudaGetLastError());
+  return VFVM_OK;
+}

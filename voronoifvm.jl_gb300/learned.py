@@ -219,14 +219,19 @@ class LearnedInitialIterate:
     """Coarse-grid surrogate of the kappa_exp solution map (G, f) -> u.
 
     Features: G at the nodes of the nc x nc subgrid (every r-th fine node,
-    n = (nc-1) r + 1) and f; targets: u at the same nodes, standardised with the
-    training mean and standard deviation.  ``layers`` linear layers of width
-    ``hidden`` (ReLU between)."""
+    n = (nc-1) r + 1), or with ``half`` > 0 its mean over the (2 half + 1)^2
+    fine nodes around each of them, and f; targets: u at the subgrid nodes,
+    standardised with the training mean and standard deviation.  ``layers``
+    linear layers of width ``hidden`` (ReLU between)."""
 
-    def __init__(self, n: int, nc: int, hidden: int = 512, layers: int = 4, max_batch: int = 512, seed: int = 0):
+    def __init__(self, n: int, nc: int, hidden: int = 512, layers: int = 4, max_batch: int = 512, seed: int = 0,
+                 half: int = 0):
         if (n - 1) % (nc - 1):
             raise ValueError("the coarse grid must nest in the fine grid: (n-1) % (nc-1) == 0")
         self.n, self.nc, self.r = n, nc, (n - 1) // (nc - 1)
+        if not 0 <= half <= self.r:
+            raise ValueError("the feature window half-width must lie in [0, (n-1)/(nc-1)]")
+        self.half = int(half)
         self.sizes = [nc * nc + 1] + [hidden] * (layers - 1) + [nc * nc]
         self.net = Network(self.sizes, max_batch, seed)
         self.mean, self.std = 0.0, 1.0
@@ -248,13 +253,41 @@ class LearnedInitialIterate:
         Sa = None if scale is None else np.tile(np.asarray(scale), 4)
         return Xa, Ta, Sa
 
+    def coarse_mean(self, fine: np.ndarray) -> np.ndarray:
+        """Means of (S, n*n) fine node arrays over the (2 half + 1)^2 window
+        around each coarse subgrid node (clipped at the boundary)."""
+        n, h = self.n, self.half
+        F = np.asarray(fine, dtype=np.float64).reshape(-1, n, n)
+        C = np.zeros((F.shape[0], n + 1, n + 1))
+        C[:, 1:, 1:] = F.cumsum(1).cumsum(2)
+        c = np.arange(self.nc) * self.r
+        lo, hi = np.clip(c - h, 0, n - 1), np.clip(c + h, 0, n - 1) + 1
+        S = C[:, hi][:, :, hi] - C[:, lo][:, :, hi] - C[:, hi][:, :, lo] + C[:, lo][:, :, lo]
+        return (S / ((hi - lo)[:, None] * (hi - lo)[None, :])).reshape(F.shape[0], -1)
+
     def features(self, logk: np.ndarray, f: np.ndarray) -> np.ndarray:
-        return np.concatenate([self.coarse(logk), np.asarray(f).reshape(-1, 1)], axis=1).astype(np.float32)
+        G = self.coarse(logk) if self.half == 0 else self.coarse_mean(logk)
+        return np.concatenate([G, np.asarray(f).reshape(-1, 1)], axis=1).astype(np.float32)
 
     def features_from_kappa(self, kappa: np.ndarray, f: np.ndarray) -> np.ndarray:
-        """The same features from the node data kappa = exp(G) (logarithms at the
-        coarse subgrid nodes only)."""
-        return np.concatenate([np.log(self.coarse(kappa)), np.asarray(f).reshape(-1, 1)], axis=1).astype(np.float32)
+        """The same features from the node data kappa = exp(G), on the host."""
+        G = np.log(self.coarse(kappa)) if self.half == 0 else self.coarse_mean(np.log(kappa))
+        return np.concatenate([G, np.asarray(f).reshape(-1, 1)], axis=1).astype(np.float32)
+
+    def features_device(self, kappa_d, f_d, out=None):
+        """The same features on the device from kappa = exp(G) (CUDA float64,
+        S x n*n) and f (CUDA float64, S values): CUDA float32, S x (nc*nc + 1)."""
+        import torch
+        S = f_d.numel()
+        if not (kappa_d.is_cuda and kappa_d.dtype == torch.float64 and kappa_d.is_contiguous()
+                and kappa_d.numel() == S * self.n * self.n and f_d.dtype == torch.float64 and f_d.is_contiguous()):
+            raise ValueError("kappa: contiguous CUDA float64 S x n*n; f: contiguous CUDA float64, S values")
+        nin = self.nc * self.nc + 1
+        if out is None:
+            out = torch.empty((S, nin), dtype=torch.float32, device=kappa_d.device)
+        _raise(L.load().vfvm_coarse_log_features(S, self.nc, self.r, self.half, kappa_d.data_ptr(), self.n * self.n,
+                                                 f_d.data_ptr(), out.data_ptr(), None), "vfvm_coarse_log_features")
+        return out
 
     def fit(self, X: np.ndarray, U: np.ndarray, scale=None, epochs: int = 200, batch: int = 256, lr: float = 1e-3,
             lr_final: float = 1e-5, seed: int = 0, log_every: int = 0):
