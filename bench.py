@@ -341,6 +341,8 @@ def run_ours(args, rank, world):
 # ----------------------------------------------------------------------------- learned workload
 LN = 257               # fine grid points per side
 LNC = 33               # coarse subgrid (every 8th node) seen and predicted by the network
+LEARN_HALF = 0         # feature window half-width around each coarse node (0: the node's own value)
+LEARN_HIDDEN = 512     # hidden layer width
 NTRAIN = 4096
 NEVAL = 512
 EVAL_SEED0 = 1_000_000
@@ -587,7 +589,7 @@ def run_learned(args, rank, world):
     N = sweep.nnodes
     zeros = torch.zeros(NEVAL * N, dtype=torch.float64, device=cuda)
     U = torch.empty_like(zeros)
-    model = lk.LearnedInitialIterate(LN, LNC, hidden=512, layers=4, max_batch=NEVAL, seed=0)
+    model = lk.LearnedInitialIterate(LN, LNC, hidden=LEARN_HIDDEN, layers=4, max_batch=NEVAL, seed=0, half=LEARN_HALF)
     # the plain (FP64) solver generates the training data (a generous cap: no training solve may fail)
     ctl_train = learned_control(vfvm, "batched_fp64", maxiters_linear=300)
     Xtr, Ttr = [], []
@@ -604,15 +606,17 @@ def run_learned(args, rank, world):
     t_data = time.perf_counter() - t_data
     t_train = time.perf_counter()
     Xtr = np.concatenate(Xtr)
-    losses = model.fit(Xtr, np.concatenate(Ttr), scale=lk.kappa_scale(Xtr[:, -1]), epochs=args.epochs, batch=256,
-                       lr=1e-3)
+    # each solve gives four training pairs: the symmetries of the triangulation
+    Xa, Ta, Sa = model.augment(Xtr, np.concatenate(Ttr), lk.kappa_scale(Xtr[:, -1]))
+    losses = model.fit(Xa, Ta, scale=Sa, epochs=args.epochs, batch=256, lr=1e-3)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t_train
     # --- held-out set
     eval_seeds = heldout_seeds(rank)
     logk_e, f_e = kappa_instances(lk, LN, eval_seeds)
     sweep.load(logk_e, f_e)
-    Xe = torch.from_numpy(model.features(logk_e, f_e)).to(cuda)
+    kappa_e = torch.from_numpy(np.exp(logk_e)).to(cuda)  # the instances' node data, resident on the device
+    f_e_d = torch.from_numpy(np.ascontiguousarray(f_e, dtype=np.float64)).to(cuda)
     Se = torch.from_numpy(lk.kappa_scale(f_e)).to(cuda)
     guess = torch.empty((NEVAL, N), dtype=torch.float64, device=cuda)
     flush = torch.empty(int(512 * 2 ** 20 // 4), dtype=torch.float32, device=cuda)  # > L2 (129 MB)
@@ -638,7 +642,7 @@ def run_learned(args, rank, world):
                                           candidates=(8, 16, 32, 64))
 
     def learned_step():
-        model.predict_device(Xe, scale=Se, out=guess)
+        model.predict_device(model.features_device(kappa_e, f_e_d), scale=Se, out=guess)
         try:
             return sweep.solve_device(zeros.data_ptr(), U.data_ptr(), ctl_l, guess_dev=guess.data_ptr())
         except vfvm.ConvergenceError:  # counted below from the per-system status
@@ -657,7 +661,7 @@ def run_learned(args, rank, world):
         torch.distributed.barrier()
     with ClockSampler(dev) as clk:
         ms_l, (hist_l, from_guess) = timed(learned_step, args.steps, args.warmup)
-    launches_per_step = sweep.solver.launches + (len(model.sizes) - 1 + 3)  # solve graph + network + prolongation
+    launches_per_step = sweep.solver.launches + (len(model.sizes) - 1 + 3) + 1  # solve graph + network + prolongation + features
     clocks = clk.summary()
     U_learned = U.view(NEVAL, N).cpu().numpy()
     ok_l = [h for h in hist_l if h.status == 0]

@@ -267,12 +267,12 @@ class LearnedInitialIterate:
 
     def features(self, logk: np.ndarray, f: np.ndarray) -> np.ndarray:
         G = self.coarse(logk) if self.half == 0 else self.coarse_mean(logk)
-        return np.concatenate([G, np.asarray(f).reshape(-1, 1)], axis=1).astype(np.float32)
+        return np.ascontiguousarray(np.concatenate([G, np.asarray(f).reshape(-1, 1)], axis=1), dtype=np.float32)
 
     def features_from_kappa(self, kappa: np.ndarray, f: np.ndarray) -> np.ndarray:
         """The same features from the node data kappa = exp(G), on the host."""
         G = np.log(self.coarse(kappa)) if self.half == 0 else self.coarse_mean(np.log(kappa))
-        return np.concatenate([G, np.asarray(f).reshape(-1, 1)], axis=1).astype(np.float32)
+        return np.ascontiguousarray(np.concatenate([G, np.asarray(f).reshape(-1, 1)], axis=1), dtype=np.float32)
 
     def features_device(self, kappa_d, f_d, out=None):
         """The same features on the device from kappa = exp(G) (CUDA float64,
