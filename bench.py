@@ -372,6 +372,7 @@ def heldout_seeds(rank):
 
 
 MAXITERS_LINEAR = 50   # BiCGStab iterations per Newton step in the batched forms (inexact Newton)
+BATCH_TAIL = 0         # batched forms: end a Newton step's BiCGStab loop once at most this many systems iterate
 MAXITERS_SINGLE = 300  # one system at a time: the faster cap for those forms
 
 
@@ -396,7 +397,7 @@ def learned_control(vfvm, form, maxiters_linear=None):
     whose BiCGStab stops at the cap takes another (inexact) Newton step; the cap
     bounds the tail of the batched loop, where the slowest systems iterate alone."""
     base = dict(updatecontrol=False, abstol=FTOL_L, reltol=0.0, reltol_linear=1e-4,
-                maxiters_linear=maxiters_linear or MAXITERS_LINEAR)
+                maxiters_linear=maxiters_linear or MAXITERS_LINEAR, batch_krylov_tail=BATCH_TAIL)
     if form in ("plain", "single_coarse"):
         base["maxiters_linear"] = maxiters_linear or MAXITERS_SINGLE
     if form == "plain":            # the plain GPU form: one system at a time, FP64, ILU0
@@ -758,7 +759,9 @@ def run_learned(args, rank, world):
                                f"(network trained on {args.ntrain} plain solves), stopping rule max|F|<=1e-13 (implies the metric's 1e-10)",
                    "form": "network start (guarded) + FP64 residual/update, FP32 Jacobian + FP32 BiCGStab with "
                            f"multicolour ILU0 and a {COARSE}-unknown Galerkin coarse stage (at most {MAXITERS_LINEAR} "
-                           "iterations per Newton step), all instances solved together (one CUDA graph)",
+                           "iterations per Newton step" + (f"; a Newton step's BiCGStab loop ends once at most "
+                                                           f"{BATCH_TAIL} instances still iterate" if BATCH_TAIL else "")
+                           + "), all instances solved together (one CUDA graph)",
                    "l2": "flushed (512 MB write) between timed steps; the per-step working set (~3 GB) exceeds L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "forms": forms,
@@ -1077,15 +1080,21 @@ def main():
     ap.add_argument("--precon", choices=["ilu0", "jacobi", "block_ilu0"], default=PRECON)
     ap.add_argument("--workload", choices=["learned", "porous", "bipolar", "rd2batch"], default="learned")
     ap.add_argument("--ntrain", type=int, default=NTRAIN)
-    ap.add_argument("--epochs", type=int, default=600)
+    ap.add_argument("--epochs", type=int, default=150)
     ap.add_argument("--maxiters-linear", type=int, default=MAXITERS_LINEAR)
+    ap.add_argument("--batch-tail", type=int, default=BATCH_TAIL)
     ap.add_argument("--single-sample", type=int, default=16)
     args = ap.parse_args()
     globals()["ENGINE"] = args.engine
     globals()["PRECON"] = args.precon
     globals()["MAXITERS_LINEAR"] = args.maxiters_linear
+    globals()["BATCH_TAIL"] = args.batch_tail
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.gpus != world:
+        # one process per GPU: --gpus N > 1 runs under torchrun with N ranks
+        sys.exit(f"bench.py: --gpus {args.gpus} but {world} rank(s); launch N > 1 GPUs as "
+                 f"python -m torch.distributed.run --nproc-per-node {args.gpus} bench.py --gpus {args.gpus}")
     if args.mode == "assembly":
         run_assembly_only(args)
         return

@@ -128,6 +128,11 @@ typedef struct vfvm_control {
   int32_t team_ctas;           /* batched solves: CTAs per system (0 = default) */
   int32_t coarse;              /* coarse-grid correction stage of the preconditioner: about this many
                                   coarse unknowns (aggregates x nspec, at most VFVM_COARSE_MAX); 0 = off */
+  int32_t batch_krylov_tail;   /* batched solves on the sweep engine: a Newton step's BiCGStab loop ends
+                                  for all systems once at most this many are still iterating; those take
+                                  their current iterate as the (inexact) Newton update, judged by the same
+                                  FP64 residual.  0 = off (each system iterates to its own tolerance or
+                                  maxiters_linear) */
 } vfvm_control;
 
 #define VFVM_COARSE_MAX 208

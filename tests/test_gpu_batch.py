@@ -124,3 +124,35 @@ def test_load_device_matches_set_instance(vfvm, engine):
     assert np.max(np.abs(runs[0] - runs[1])) > 0  # the second load changed the problems
     with pytest.raises(ValueError):
         batch.load_device(params=torch.zeros((S, 2), dtype=torch.float64, device="cuda"))
+
+
+@pytest.mark.parametrize("tail", [0, 6])
+def test_sweep_batch_krylov_tail_rule(vfvm, oracle, tail):
+    """The batch-level inexact Newton rule of the sweep engine: a Newton step's
+    BiCGStab loop ends for all systems once at most `tail` still iterate; those
+    continue from their current iterate, and every system still meets the FP64
+    residual test and the oracle's solution (1e-8)."""
+    torch = pytest.importorskip("torch")
+    lk = vfvm.learned
+    S, n = 24, 33
+    inst = [lk.kappa_instance(n, 2000 + s) for s in range(S)]
+    logk = np.array([a for a, _ in inst])
+    f = np.array([b for _, b in inst])
+    sweep = lk.KappaSweep(n, S)
+    sweep.load(logk, f)
+    N = sweep.nnodes
+    z = torch.zeros(S * N, dtype=torch.float64, device="cuda")
+    U = torch.empty_like(z)
+    control = vfvm.SolverControl(precision="mixed", coarse=40, updatecontrol=False, abstol=1e-12, reltol=0.0,
+                                 maxiters_linear=50, batch_krylov_tail=tail)
+    hist, _ = sweep.solve_device(z.data_ptr(), U.data_ptr(), control)
+    assert sweep.solver.engine == "sweep"
+    assert all(h.status == 0 for h in hist)
+    Uh = U.view(S, N).cpu().numpy()
+    oc = oracle.Control(abstol=1e-12, reltol=0.0)
+    oc.updatecontrol = False
+    for i in (0, 7, 23):
+        osys = oracle.OracleSystem(sweep.grid, "kappa_exp", [f[i]], nodedata=np.exp(logk[i]))
+        uo, _ = oracle.solve_step(osys, np.zeros(N), oc)
+        assert np.max(np.abs(Uh[i] - uo)) <= 1e-8 * np.max(np.abs(uo))
+    sweep.close()

@@ -55,7 +55,7 @@ class Control_t(ctypes.Structure):
                 ("du_opt", c_d), ("du_max_factor", c_d),
                 ("num_final_steps", c_i32), ("force_first_step", c_i32), ("handle_exceptions", c_i32),
                 ("store_all", c_i32), ("engine", c_i32), ("team_ctas", c_i32),
-                ("coarse", c_i32)]
+                ("coarse", c_i32), ("batch_krylov_tail", c_i32)]
 
 
 class History_t(ctypes.Structure):

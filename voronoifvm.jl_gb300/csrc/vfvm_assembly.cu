@@ -35,14 +35,16 @@ __global__ void __launch_bounds__(128) assemble_kernel(const AsmTables t, const 
 //   stage    the unknowns of the tile's owned and halo nodes into shared memory
 //            (FP64 values and, in the mixed form, their FP32 shadows, each
 //            converted once);
-//   edges    every edge of the tile once: flux(u_first, u_second) on duals,
+//   items    every edge of the tile once: flux(u_first, u_second) on duals,
 //            storing fac * f (FP64) and the two partial blocks d/du_first,
-//            d/du_second (times fac) in shared memory;
-//   nodes    every owned node gathers its edges' results in the reference's
-//            edge order (its block row's columns are sorted by node index):
-//            F[K] += +-fac f, the diagonal block accumulates d/du_K, and each
-//            off-diagonal block is written once; node and boundary terms as in
-//            the node-centric kernel.
+//            d/du_second (times fac) in shared memory; and, as further work
+//            items of the same loop, every owned node's node terms (reaction,
+//            source, storage), stored alongside;
+//   nodes    every owned node starts from its node terms and gathers its
+//            edges' results in the reference's edge order (its block row's
+//            columns are sorted by node index): F[K] += +-fac f, the diagonal
+//            block accumulates d/du_K, and each off-diagonal block is written
+//            once; then its boundary terms.
 // Signs and factor placement follow assemble_edges (src/vfvm_assembly.jl:169-192):
 // the first node gets +f, the second -f.  No atomics; one writer per output.
 template <class Ph, typename P>
@@ -61,6 +63,8 @@ __global__ void __launch_bounds__(256) assemble_tile_kernel(const AsmTables t, c
   double* ef = reinterpret_cast<double*>(smem + L.ef);
   P* ja = reinterpret_cast<P*>(smem + L.ja);
   P* jb = reinterpret_cast<P*>(smem + L.jb);
+  double* nf = reinterpret_cast<double*>(smem + L.nf);
+  P* nj = reinterpret_cast<P*>(smem + L.nj);
 
   const int tile = blockIdx.x;
   const int lbeg = tt.tile_ptr[tile], nloc = tt.tile_ptr[tile + 1] - lbeg, nown = tt.tile_nown[tile];
@@ -82,8 +86,30 @@ __global__ void __launch_bounds__(256) assemble_tile_kernel(const AsmTables t, c
   }
   __syncthreads();
 
-  // ---- every edge of the tile once
-  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+  // ---- work items: every edge of the tile once, then the owned nodes' node terms
+  for (int item = threadIdx.x; item < ne + nown; item += blockDim.x) {
+    if (item >= ne) {
+      const int l = item - ne;
+      const int K = sl[l];
+      double uK[NS], fK[NS];
+      P uKs[NS], jd[NS * NS];
+#pragma unroll
+      for (int i = 0; i < NS; ++i) {
+        uK[i] = uv[l * NS + i];
+        if constexpr (kSh) uKs[i] = us[l * NS + i];
+        else uKs[i] = uK[i];
+        fK[i] = 0.0;
+      }
+#pragma unroll
+      for (int i = 0; i < NS * NS; ++i) jd[i] = P(0);
+      node_terms<Ph, P, false>(t, ph, K, uK, uKs, Uold, time, tstepinv, lambda, fK, jd);
+#pragma unroll
+      for (int i = 0; i < NS; ++i) nf[l * NS + i] = fK[i];
+#pragma unroll
+      for (int i = 0; i < NS * NS; ++i) nj[l * NS * NS + i] = jd[i];
+      continue;
+    }
+    const int e = item;
     const unsigned ab = tt.edge_ab[ebeg + e];
     const int la = (int)(ab & 0xffffu), lb = (int)(ab >> 16);
     const int A = sl[la], B = sl[lb];
@@ -130,11 +156,10 @@ __global__ void __launch_bounds__(256) assemble_tile_kernel(const AsmTables t, c
       uK[i] = uv[l * NS + i];
       if constexpr (kSh) uKs[i] = us[l * NS + i];
       else uKs[i] = uK[i];
-      fK[i] = 0.0;
+      fK[i] = nf[l * NS + i];
     }
 #pragma unroll
-    for (int i = 0; i < NS * NS; ++i) jd[i] = P(0);
-    node_terms<Ph, P, false>(t, ph, K, uK, uKs, Uold, time, tstepinv, lambda, fK, jd);
+    for (int i = 0; i < NS * NS; ++i) jd[i] = nj[l * NS * NS + i];
     const int sbeg = t.browptr[K], send = t.browptr[K + 1], dg = t.diag[K];
     for (int s = sbeg; s < send; ++s) {
       if (s == dg) continue;

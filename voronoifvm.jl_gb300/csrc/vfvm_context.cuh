@@ -82,7 +82,7 @@ struct TileTables {
 
 // Shared-memory layout of one tile (byte offsets), identical on host and device.
 struct TileSmem {
-  size_t lnodes, uv, us, ef, ja, jb, total;
+  size_t lnodes, uv, us, ef, ja, jb, nf, nj, total;
 };
 template <int NS, typename P>
 VFVM_HD TileSmem tile_smem_layout(int maxloc, int maxedges) {
@@ -95,7 +95,9 @@ VFVM_HD TileSmem tile_smem_layout(int maxloc, int maxedges) {
   L.ef = up(L.us + us_bytes);
   L.ja = up(L.ef + (size_t)maxedges * NS * 8);
   L.jb = up(L.ja + (size_t)maxedges * NS * NS * sizeof(P));
-  L.total = up(L.jb + (size_t)maxedges * NS * NS * sizeof(P));
+  L.nf = up(L.jb + (size_t)maxedges * NS * NS * sizeof(P));  // node terms of the owned nodes
+  L.nj = up(L.nf + (size_t)maxloc * NS * 8);
+  L.total = up(L.nj + (size_t)maxloc * NS * NS * sizeof(P));
   return L;
 }
 

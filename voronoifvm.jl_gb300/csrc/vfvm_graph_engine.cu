@@ -778,6 +778,7 @@ DevControl make_devcontrol(const vfvm_control& c) {
   d.maxiters = c.maxiters; d.max_round = c.max_round; d.is_linear = c.is_linear;
   d.updatecontrol = c.updatecontrol; d.maxiters_linear = c.maxiters_linear;
   d.krylov = c.krylov; d.gmres_restart = c.gmres_restart;
+  d.batch_tail = c.batch_krylov_tail > 0 ? c.batch_krylov_tail : 0;
   return d;
 }
 

@@ -356,7 +356,7 @@ int sweep_build_graph(SweepHost& h, const SweepArgs<Ph, KT>& a, cudaStream_t s) 
   // prologue: start values, Dirichlet values, state; Newton condition
   VFVM_CUDA(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   sw_init_kernel<Ph, KT><<<grid, kSweepThreads, 0, s>>>(a);
-  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 1, ncond, a.klist, a.kcount, a.runs);
+  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 1, ncond, a.klist, a.kcount, a.runs, a.call);
   VFVM_CUDA(cudaStreamEndCapture(s, &cap));
   cudaGraphNode_t wnode, knode;
   cudaGraph_t body, kbody;
@@ -364,18 +364,18 @@ int sweep_build_graph(SweepHost& h, const SweepArgs<Ph, KT>& a, cudaStream_t s) 
   // Newton body up to the Krylov loop
   VFVM_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   sweep_newton_head<Ph, KT>(a, s);
-  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 0, kcond, a.klist, a.kcount, a.runs);
+  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 0, kcond, a.klist, a.kcount, a.runs, a.call);
   VFVM_CUDA(cudaStreamEndCapture(s, &cap));
   VFVM_CUDA(add_while(body, kcond, &knode, &kbody));
   // one BiCGStab iteration of every active system
   VFVM_CUDA(cudaStreamBeginCaptureToGraph(s, kbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   sweep_krylov_iteration<Ph, KT>(a, s);
-  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 0, kcond, a.klist, a.kcount, a.runs);
+  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 0, kcond, a.klist, a.kcount, a.runs, a.call);
   VFVM_CUDA(cudaStreamEndCapture(s, &cap));
   // Newton update after the Krylov loop, next Newton condition
   VFVM_CUDA(cudaStreamBeginCaptureToGraph(s, body, &knode, nullptr, 1, cudaStreamCaptureModeThreadLocal));
   sw_update_kernel<Ph, KT><<<grid, kSweepThreads, 0, s>>>(a);
-  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 1, ncond, a.klist, a.kcount, a.runs);
+  sw_cond_kernel<<<1, 1024, 0, s>>>(a.st, a.S, 1, ncond, a.klist, a.kcount, a.runs, a.call);
   VFVM_CUDA(cudaStreamEndCapture(s, &cap));
   VFVM_CUDA(cudaGetLastError());
   VFVM_CUDA(cudaGraphInstantiate(&h.exec, g, 0));
@@ -390,6 +390,8 @@ int sweep_eager(const SweepArgs<Ph, KT>& a, cudaStream_t s) {
   const dim3 grid(a.bpi, a.S);
   std::vector<SweepState> st(a.S);
   std::vector<int> list;
+  SweepCall call;
+  VFVM_CUDA(cudaMemcpyAsync(&call, a.call, sizeof(SweepCall), cudaMemcpyDeviceToHost, s));
   auto any = [&](int which, bool& out) -> int {
     VFVM_CUDA(cudaMemcpyAsync(st.data(), a.st, sizeof(SweepState) * a.S, cudaMemcpyDeviceToHost, s));
     VFVM_CUDA(cudaStreamSynchronize(s));
@@ -400,6 +402,7 @@ int sweep_eager(const SweepArgs<Ph, KT>& a, cudaStream_t s) {
       out = out || (which == 0 ? x.kactive != 0 : (x.nactive || x.restart));
       if (x.kactive) list.push_back(i);
     }
+    if (which == 0 && (int)list.size() <= call.ctl.batch_tail) out = false;  // the batch-level inexact Newton rule
     if (which == 0) {  // the compact list the iteration kernels stride over
       const int cnt = (int)list.size();
       VFVM_CUDA(cudaMemcpyAsync(a.kcount, &cnt, sizeof(int), cudaMemcpyHostToDevice, s));

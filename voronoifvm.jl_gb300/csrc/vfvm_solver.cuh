@@ -14,7 +14,7 @@ struct DevControl {
   double reltol_linear, abstol_linear;
   int maxiters, max_round, is_linear, updatecontrol, maxiters_linear;
   int krylov, gmres_restart;  // VFVM_KRYLOV_*; GMRES basis size (persistent engine only)
-  int pad;
+  int batch_tail;              // sweep engine: end the BiCGStab loop once at most this many systems iterate
 };
 
 // Newton (solve_step!, src/vfvm_solver.jl:13-222) and BiCGStab state kept in

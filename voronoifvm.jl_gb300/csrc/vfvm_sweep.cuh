@@ -592,6 +592,9 @@ __global__ void __launch_bounds__(kSweepThreads) sw_update_kernel(SweepArgs<Ph, 
   const SwUnit u = sw_unit2d();
   const int i = u.i;
   SweepState& s = a.st[i];
+  // the BiCGStab loop is over for every system (those cut short by the
+  // batch-level tail rule keep their current iterate)
+  if (u.lb == 0 && threadIdx.x == 0) s.kactive = 0;
   if (!s.nactive || s.restart) return;
   const int64_t o = i * a.n;
   const bool apply = s.status == VFVM_OK && !s.early;
@@ -645,9 +648,13 @@ __global__ void __launch_bounds__(kSweepThreads) sw_update_kernel(SweepArgs<Ph, 
 // Loop conditions: any system with kactive (which 0) / nactive or restart
 // (which 1).  For which 0 also the compact list of systems still in BiCGStab,
 // in system order (one block; each thread takes a contiguous chunk).
+// Loop condition of the sweep graph: which = 1, any system still in Newton;
+// which = 0, any system still in BiCGStab (and the compact list of them) --
+// unless at most call->ctl.batch_tail systems are (the batch-level inexact
+// Newton rule: the loop ends and they keep their current iterate).
 static __global__ void __launch_bounds__(1024) sw_cond_kernel(const SweepState* st, int S, int which,
                                                              cudaGraphConditionalHandle h, int* klist, int* kcount,
-                                                             unsigned* runs) {
+                                                             unsigned* runs, const SweepCall* call) {
   if (threadIdx.x == 0) atomicAdd(&runs[which], 1u);  // loop bodies executed (launch accounting)
   __shared__ int wsum[32];
   __shared__ int total;
@@ -677,7 +684,10 @@ static __global__ void __launch_bounds__(1024) sw_cond_kernel(const SweepState* 
       if (st[i].kactive) klist[pos++] = i;
     if (t == 0) *kcount = total;
   }
-  if (t == 0) cudaGraphSetConditional(h, total > 0 ? 1u : 0u);
+  if (t == 0) {
+    const int tail = which == 0 ? call->ctl.batch_tail : 0;
+    cudaGraphSetConditional(h, total > tail ? 1u : 0u);
+  }
 }
 
 }  // namespace vfvm

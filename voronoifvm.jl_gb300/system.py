@@ -141,6 +141,9 @@ class SolverControl:
     # coarse-grid correction stage of the preconditioner: about this many coarse
     # unknowns (aggregates of nodes x species, at most 208); 0 = one-level only
     coarse: int = 0
+    # batched solves on the sweep engine: end a Newton step's BiCGStab loop once at
+    # most this many systems still iterate (they keep their current iterate; 0: off)
+    batch_krylov_tail: int = 0
     # time / embedding step control of solve(times=...) / solve(embed=...):
     # "device" runs the whole step loop as one CUDA graph launch (the step
     # decisions made on the device, graph engine with BiCGStab); "host" decides
@@ -170,6 +173,7 @@ class SolverControl:
         c.engine = L.ENGINE[self.engine]
         c.team_ctas = int(self.team_ctas)
         c.coarse = int(self.coarse)
+        c.batch_krylov_tail = int(self.batch_krylov_tail)
         return c
 
 
