@@ -66,6 +66,21 @@ extern "C" {
 #define VFVM_PHYS_SURFACE_HEAT 16     /* heat equation + conducting surface layer (bflux, bstorage, bsource,
                                          breaction on boundary region breg; cf. Example311);
                                          params: eps, eps_s, c_s, k, q0, breg */
+#define VFVM_PHYS_BOUNDARY_SPECIES 17 /* bulk species 1 and a boundary species 2 living on boundary region
+                                         breg (examples/Example230_BoundaryFlux.jl): species 1
+                                         -d u'' + k u = c; species 2 -d_b v'' + k_b(s) v = c_b(s) along
+                                         breg (bflux, breaction, bsource) or, enabled as a bulk species
+                                         of a 1D grid, in the bulk; s = the second coordinate on the
+                                         boundary, the first in the bulk; k_b = kmax, c_b = 0 for
+                                         s <= 1/2, else k_b = 0, c_b = cmax;
+                                         params: d, k, c, d_b, kmax, cmax, breg */
+#define VFVM_PHYS_EDGE_REACTION 18    /* u_t - div grad u = 1, u = 0 on boundary regions 1-6, the source as a
+                                         node reaction (mode 0) or an edge reaction -h^2/(2 dim) (mode 1) or
+                                         -(x_K - x_L)^2/2 (mode 2) (examples/DevEx002_EdgeReaction.jl);
+                                         params: mode, dim */
+#define VFVM_PHYS_JOULE_HEAT 19       /* potential phi and temperature T with Joule heating as an edge
+                                         reaction (the callbacks of examples/Example206_JouleHeat.jl);
+                                         params: kappa0, alpha, T0, lambda, c */
 
 /* linear solver / preconditioner / precision selectors */
 #define VFVM_KRYLOV_BICGSTAB 0
@@ -101,6 +116,26 @@ typedef struct vfvm_physics_desc {
   int32_t nbregions;           /* legacy boundary data (boundary_dirichlet!(sys, ...)): */
   const double* bfactors;      /* nspec x nbregions, column-major; 1e30 marks Dirichlet */
   const double* bvalues;       /* nspec x nbregions */
+  /* Species restricted to regions (enable_species!(sys, ispec, regions) and
+   * enable_boundary_species!(sys, ispec, bregions), src/vfvm_system.jl:433-513).
+   * Both counts 0: every species lives on every node (the default here).
+   * Otherwise region_species (nspec x ncellregions_species, column-major) is
+   * nonzero where species ispec is enabled in cell region ireg, bregion_species
+   * (nspec x nbregions_species) where it is enabled on boundary region ibreg.  A
+   * node carries a species when a cell of an enabled region or a boundary face
+   * of an enabled boundary region contains it.  The unknowns stay dense (nspec
+   * per node, the reference's DenseSystem): node, edge, boundary-node and
+   * boundary-edge terms assemble the rows and columns of the species of their
+   * region or node only (src/vfvm_assemblydata.jl:245-470), the other dofs get
+   * F += U - Uold with a unit diagonal (src/vfvm_system.jl:1012-1026) and are
+   * set to 0 before each Newton solve (:1030-1042).  The values on the enabled
+   * dofs are those of the reference's sparse unknown storage as well.  Systems
+   * with restricted species assemble with the node-centric kernel and run on
+   * single-system solves (batched solves return VFVM_ERR_INPUT). */
+  int32_t ncellregions_species;
+  const int32_t* region_species;
+  int32_t nbregions_species;
+  const int32_t* bregion_species;
 } vfvm_physics_desc;
 
 /* SolverControl subset (src/vfvm_solvercontrol.jl:13-270) plus device solver settings. */
@@ -129,9 +164,10 @@ typedef struct vfvm_control {
   int32_t coarse;              /* coarse-grid correction stage of the preconditioner: about this many
                                   coarse unknowns (aggregates x nspec, at most VFVM_COARSE_MAX); 0 = off */
   int32_t batch_krylov_tail;   /* batched solves on the sweep engine: a Newton step's BiCGStab loop ends
-                                  for all systems once at most this many are still iterating; those take
-                                  their current iterate as the (inexact) Newton update, judged by the same
-                                  FP64 residual.  0 = off (each system iterates to its own tolerance or
+                                  for all systems once at most this many are still iterating and they are
+                                  at most a tenth of the systems that entered the loop; those take their
+                                  current iterate as the (inexact) Newton update, judged by the same FP64
+                                  residual.  0 = off (each system iterates to its own tolerance or
                                   maxiters_linear) */
 } vfvm_control;
 

@@ -41,7 +41,7 @@ _lib = None
 PHYS = {
     "ex105": 1, "ex106": 2, "ex110": 3, "ex160": 4, "ex207": 5, "ex301": 6, "ex440": 7,
     "laplace_dirichlet": 8, "nlpoisson": 11, "porous": 12, "bipolar": 13, "rd2": 14,
-    "kappa_exp": 15, "surface_heat": 16,
+    "kappa_exp": 15, "surface_heat": 16, "boundary_species": 17, "edge_reaction": 18, "joule_heat": 19,
 }
 
 
@@ -65,6 +65,8 @@ def lib():
                                     P(d), i32, P(d), i32, P(d), P(d), i32]
         L.oracle_destroy.argtypes = [ctypes.c_void_p]
         L.oracle_set_cellwise.argtypes = [ctypes.c_void_p, i32]
+        L.oracle_set_species.argtypes = [ctypes.c_void_p, i32, P(i32), i32, P(i32)]
+        L.oracle_set_species.restype = i32
         L.oracle_nspec.argtypes = [ctypes.c_void_p]
         L.oracle_nedges.argtypes = [ctypes.c_void_p]
         L.oracle_ncandidates.argtypes = [ctypes.c_void_p]
@@ -139,7 +141,11 @@ def fixed_timesteps(control: Control, dt: float, grow: float = 1.0) -> Control:
 class OracleSystem:
     """Grid tables + physics id + parameters, evaluated by the C++ restatement."""
 
-    def __init__(self, grid, physics, params=(), nodedata=None, bfactors=None, bvalues=None, assembly="edgewise"):
+    def __init__(self, grid, physics, params=(), nodedata=None, bfactors=None, bvalues=None, assembly="edgewise",
+                 region_species=None, bregion_species=None):
+        """region_species (nspec x ncellregions) / bregion_species (nspec x
+        nbregions): nonzero where enable_species! / enable_boundary_species!
+        enabled a species (None for both: every species on every node)."""
         L = lib()
         self.physics_id = PHYS[physics] if isinstance(physics, str) else int(physics)
         self.grid = grid
@@ -175,6 +181,14 @@ class OracleSystem:
             raise ValueError("assembly must be edgewise or cellwise")
         L.oracle_set_cellwise(self.h, int(assembly == "cellwise"))
         self.nspec = L.oracle_nspec(self.h)
+        if region_species is not None or bregion_species is not None:
+            rs = np.asfortranarray(np.zeros((self.nspec, 0)) if region_species is None else region_species,
+                                   dtype=np.int32)
+            bs = np.asfortranarray(np.zeros((self.nspec, 0)) if bregion_species is None else bregion_species,
+                                   dtype=np.int32)
+            self._species = (rs, bs)
+            if L.oracle_set_species(self.h, rs.shape[1], _p(rs, ctypes.c_int), bs.shape[1], _p(bs, ctypes.c_int)):
+                raise ValueError("a species is both a bulk and a boundary species, or no species is enabled")
         self.nnodes = g.nnodes
         self.n = self.nspec * self.nnodes
         self.tasm = 0.0

@@ -135,7 +135,8 @@ struct PhysParams { const double* p; int np; };
 // Boundary callbacks beyond breaction (bflux, bstorage, bsource): absent unless a
 // physics defines them.
 struct OBase {
-  static const bool has_bflux = false, has_bstorage = false, has_bsource = false;
+  static const bool has_bflux = false, has_bstorage = false, has_bsource = false, has_edgereaction = false;
+  template <class T> void edgereaction(T*, const T*, const T*, const EdgeInfo&) const {}
   template <class T> void bflux(T*, const T*, const T*, const BEdgeInfo&) const {}
   template <class T> void bstorage(T*, const T*, BNodeInfo&) const {}
   void bsource(double*, BNodeInfo&) const {}
@@ -363,6 +364,93 @@ struct PhysSurfaceHeat : OBase {
   }
 };
 
+// examples/Example230_BoundaryFlux.jl:58-165: species 1 is the 2D bulk species
+// (flux2D!, reaction2D!, source2D!, :106-121), species 2 the boundary species
+// on region breg (bflux!, breaction!, bsource!, :123-165; the switch at
+// bnode.coord[2] <= 0.5).  The bulk callbacks of species 2 restate the 1D line
+// problem (flux!, reaction!, source!, :58-71); its node-index switch of k1 and
+// c1 at length_x_half is the switch at x <= 1/2 for the example's even n.
+struct PhysBoundarySpecies : OBase {
+  static const int NS = 2;
+  static const bool has_reaction = true, has_storage = false, has_source = true, has_breaction = true;
+  static const bool has_bflux = true, has_bstorage = false, has_bsource = true;
+  double d, k, c, db, kmax, cmax; int breg;
+  double kb(double s) const { return s <= 0.5 ? kmax : 0.0; }
+  double cb(double s) const { return s <= 0.5 ? 0.0 : cmax; }
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
+    f[0] = d * (uK[0] - uL[0]);
+    f[1] = db * (uK[1] - uL[1]);
+  }
+  template <class T> void reaction(T* f, const T* u, const NodeInfo& n) const {
+    f[0] = k * u[0];
+    f[1] = kb(n.x[0]) * u[1];
+  }
+  template <class T> void storage(T*, const T*, const NodeInfo&) const {}
+  void source(double* f, const NodeInfo& n) const { f[0] = c; f[1] = cb(n.x[0]); }
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const { if (b.region == breg) f[1] = kb(b.x[1]) * u[1]; }
+  template <class T> void bflux(T* f, const T* uK, const T* uL, const BEdgeInfo& e) const {
+    if (e.region == breg) f[1] = db * (uK[1] - uL[1]);
+  }
+  void bsource(double* f, BNodeInfo& b) const { if (b.region == breg) f[1] = cb(b.x[1]); }
+};
+
+// examples/DevEx002_EdgeReaction.jl:49-104 (case :compare_max): storage u, flux
+// u_K - u_L, u = 0 on boundary regions 1-6 (bcondition!), and the unit source as
+// reaction! (mode 0: -1), edgereaction! (mode 1: -meas(edge)^2 / (2 dim)) or
+// edgereaction2! (mode 2: -(phi_K - phi_L)^2 / 2, phi the first coordinate).
+struct PhysEdgeReaction : OBase {
+  static const int NS = 1;
+  static const bool has_reaction = true, has_storage = true, has_source = false, has_breaction = true;
+  static const bool has_edgereaction = true;
+  int mode = 0, dim = 1;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = uK[0] - uL[0]; }
+  template <class T> void storage(T* f, const T* u, const NodeInfo&) const { f[0] = u[0]; }
+  template <class T> void reaction(T* f, const T* u, const NodeInfo&) const { if (mode == 0) f[0] = u[0] * 0.0 + (-1.0); }
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void edgereaction(T* f, const T* uK, const T*, const EdgeInfo& e) const {
+    if (mode == 1) {
+      double s = 0.0;
+      for (int k = 0; k < dim; ++k) s += (e.xK[k] - e.xL[k]) * (e.xK[k] - e.xL[k]);
+      double h = std::sqrt(s);
+      f[0] = uK[0] * 0.0 + (-1.0 * (h * h) / (2 * dim));
+    } else if (mode == 2) {
+      double dp = e.xK[0] - e.xL[0];
+      f[0] = uK[0] * 0.0 + (-dp * dp / 2);
+    }
+  }
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const {
+    for (int r = 1; r <= 6; ++r) boundary_dirichlet(f, u, b, 0, r, 0.0);
+  }
+};
+
+// examples/Example206_JouleHeat.jl:63-92: storage!, flux!, jouleheat! (the edge
+// reaction) and bcondition! (boundary_dirichlet! for phi on regions 1, 2;
+// boundary_robin! y += 0.5 T - T0 for T on regions 1-4, src/vfvm_physics.jl:551).
+// kappa is evaluated at y[iT], still 0 where the example reads it.
+struct PhysJouleHeat : OBase {
+  static const int NS = 2;
+  static const bool has_reaction = false, has_storage = true, has_source = false, has_breaction = true;
+  static const bool has_edgereaction = true;
+  double kappa0, alpha, T0, lam, c;
+  template <class T> T kappa(const T& t) const { return kappa0 * exp(alpha * (t - T0)); }
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
+    f[0] = kappa(f[1]) * (uK[0] - uL[0]);
+    f[1] = lam * (uK[1] - uL[1]);
+  }
+  template <class T> void edgereaction(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
+    f[1] = kappa(f[1]) * (-1.0) * (uK[0] - uL[0]) * (uK[0] - uL[0]);  // -kappa * d * d
+  }
+  template <class T> void reaction(T*, const T*, const NodeInfo&) const {}
+  template <class T> void storage(T* f, const T* u, const NodeInfo&) const { f[1] = c * u[1]; }
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const {
+    boundary_dirichlet(f, u, b, 0, 1, -10.0);
+    boundary_dirichlet(f, u, b, 0, 2, 10.0);
+    for (int r = 1; r <= 4; ++r)
+      if (b.region == r) f[1] = f[1] + (0.5 * u[1] - T0);
+  }
+};
+
 // ---------------------------------------------------------------- system
 struct Oracle {
   int dim = 0, N = 0, ncells = 0, nbf = 0, ns = 1, phys = 0, nregions = 1, nbregions = 0, nnd = 0;
@@ -387,6 +475,11 @@ struct Oracle {
   // assembly = :cellwise (the reference's default, src/vfvm_system.jl:220):
   // node and edge terms per cell with the cell's own factors
   bool cellwise = false;
+  // species restricted to regions (enable_species!, enable_boundary_species!,
+  // src/vfvm_system.jl:433-513): species bit masks per cell region and per node
+  // (node_dof); masked = false: every species on every node
+  bool masked = false;
+  std::vector<unsigned> reg_spec, node_spec;
 };
 
 inline int nn_bface(int dim) { return dim; }  // nodes per boundary face: Vertex0D 1, Edge1D 2, Triangle2D 3
@@ -573,7 +666,11 @@ int assemble_t(Oracle& o, const P& ph, const double* U, const double* Uold, doub
   const int d = o.dim;
   const double* nd = o.ndata.empty() ? nullptr : o.ndata.data();
   // one node term: fac * (reaction - source + (storage - old storage) / tstep)
+  // isregionspecies / isnodespecies masks of assemble_res_jac (src/vfvm_assemblydata.jl:245-470)
+  auto region_mask = [&](int reg) { return o.masked ? o.reg_spec[reg - 1] : ~0u; };
+  auto node_mask = [&](int K) { return o.masked ? o.node_spec[K] : ~0u; };
   auto node_term = [&](int K, int reg, double fac) {
+    const unsigned m = region_mask(reg);
     NodeInfo ni{K, reg, &o.coord[d * K], time, lambda, nd ? nd + (size_t)o.nnd * K : nullptr};
     double src[NS] = {0}, oldstor[NS] = {0};
     Dual<NS> u[NS], rr[NS], rs[NS];
@@ -587,12 +684,15 @@ int assemble_t(Oracle& o, const P& ph, const double* U, const double* Uold, doub
       ph.storage(oldstor, uo, ni);
     }
     for (int i = 0; i < NS; ++i) {
+      if (!((m >> i) & 1u)) continue;
       F[K * NS + i] += fac * (rr[i].v - src[i] + (rs[i].v - oldstor[i]) * tstepinv);
-      for (int j = 0; j < NS; ++j) addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + j, rr[i].d[j] + rs[i].d[j] * tstepinv, fac);
+      for (int j = 0; j < NS; ++j)
+        if ((m >> j) & 1u) addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + j, rr[i].d[j] + rs[i].d[j] * tstepinv, fac);
     }
   };
   // one edge term: flux (bflux on boundary edges) between K (first) and L, scattered 4-way
   auto edge_term = [&](int K, int L, int reg, double fac, bool boundary) {
+    const unsigned m = boundary ? node_mask(K) : region_mask(reg);
     Dual<2 * NS> uK[NS], uL[NS], f[NS];
     for (int i = 0; i < NS; ++i) {
       uK[i] = mk<2 * NS>(U[K * NS + i]); uK[i].d[i] = 1.0;
@@ -608,15 +708,40 @@ int assemble_t(Oracle& o, const P& ph, const double* U, const double* Uold, doub
       ph.flux(f, uK, uL, ei);
     }
     for (int i = 0; i < NS; ++i) {
+      if (!((m >> i) & 1u)) continue;
       double v = fac * f[i].v;
       F[K * NS + i] += v;
       F[L * NS + i] += -v;
       for (int j = 0; j < NS; ++j) {
+        if (!((m >> j) & 1u)) continue;
         int64_t iK = (int64_t)K * NS + i, iL = (int64_t)L * NS + i, jK = (int64_t)K * NS + j, jL = (int64_t)L * NS + j;
         addnz(o, iK, jK, +f[i].d[j], fac);
         addnz(o, iL, jK, -f[i].d[j], fac);
         addnz(o, iK, jL, +f[i].d[NS + j], fac);
         addnz(o, iL, jL, -f[i].d[NS + j], fac);
+      }
+    }
+    // edgereaction, src/vfvm_assembly.jl:202-238: fac * r to both end nodes,
+    // Jacobian entries with the signs placed there
+    if (P::has_edgereaction && !boundary) {
+      Dual<2 * NS> r[NS];
+      for (int i = 0; i < NS; ++i) r[i] = mk<2 * NS>(0);
+      EdgeInfo ei{K, L, reg, &o.coord[d * K], &o.coord[d * L], time, lambda,
+                  nd ? nd + (size_t)o.nnd * K : nullptr, nd ? nd + (size_t)o.nnd * L : nullptr};
+      ph.edgereaction(r, uK, uL, ei);
+      for (int i = 0; i < NS; ++i) {
+        if (!((m >> i) & 1u)) continue;
+        double v = fac * r[i].v;
+        F[K * NS + i] += v;
+        F[L * NS + i] += v;
+        for (int j = 0; j < NS; ++j) {
+          if (!((m >> j) & 1u)) continue;
+          int64_t iK = (int64_t)K * NS + i, iL = (int64_t)L * NS + i, jK = (int64_t)K * NS + j, jL = (int64_t)L * NS + j;
+          addnz(o, iK, jK, +r[i].d[j], fac);
+          addnz(o, iL, jK, -r[i].d[j], fac);
+          addnz(o, iK, jL, -r[i].d[NS + j], fac);
+          addnz(o, iL, jL, +r[i].d[NS + j], fac);
+        }
       }
     }
   };
@@ -673,9 +798,12 @@ int assemble_t(Oracle& o, const P& ph, const double* U, const double* Uold, doub
       for (int i = 0; i < NS; ++i) { u[i] = mk<NS>(U[K * NS + i]); u[i].d[i] = 1.0; y[i] = mk<NS>(0); }
       if (P::has_bsource) ph.bsource(bsrc, bi);
       if (P::has_breaction) ph.breaction(y, u, bi);
+      const unsigned nm = node_mask(K);
       for (int i = 0; i < NS; ++i) {
+        if (!((nm >> i) & 1u)) continue;
         F[K * NS + i] += fac * (y[i].v - bsrc[i]);
-        for (int j = 0; j < NS; ++j) addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + j, y[i].d[j], fac);
+        for (int j = 0; j < NS; ++j)
+          if ((nm >> j) & 1u) addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + j, y[i].d[j], fac);
       }
       // bstorage, src/vfvm_assembly.jl:409-440
       if (P::has_bstorage) {
@@ -685,8 +813,10 @@ int assemble_t(Oracle& o, const P& ph, const double* U, const double* Uold, doub
         ph.bstorage(sb, u, bi);
         ph.bstorage(so, uo, bi);
         for (int i = 0; i < NS; ++i) {
+          if (!((nm >> i) & 1u)) continue;
           F[K * NS + i] += fac * (sb[i].v - so[i]) * tstepinv;
-          for (int j = 0; j < NS; ++j) addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + j, sb[i].d[j], fac * tstepinv);
+          for (int j = 0; j < NS; ++j)
+            if ((nm >> j) & 1u) addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + j, sb[i].d[j], fac * tstepinv);
         }
       }
     }
@@ -707,6 +837,15 @@ int assemble_t(Oracle& o, const P& ph, const double* U, const double* Uold, doub
       }
     }
   }
+  // _eval_and_assemble_inactive_species, src/vfvm_system.jl:1012-1026: the
+  // species a node does not carry get F += U - Uold and a unit diagonal
+  if (o.masked)
+    for (int K = 0; K < o.N; ++K)
+      for (int i = 0; i < NS; ++i)
+        if (!((o.node_spec[K] >> i) & 1u)) {
+          F[K * NS + i] += U[K * NS + i] - Uold[K * NS + i];
+          addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + i, 1.0, 1.0);
+        }
   return o.nerr ? 2 : 0;
 }
 
@@ -734,6 +873,11 @@ void init_dirichlet_t(Oracle& o, const P& ph, double* U, double time, double lam
         }
       }
     }
+  // _initialize_inactive_dof!, src/vfvm_system.jl:1030-1042
+  if (o.masked)
+    for (int K = 0; K < o.N; ++K)
+      for (int i = 0; i < NS; ++i)
+        if (!((o.node_spec[K] >> i) & 1u)) U[K * NS + i] = 0.0;
 }
 
 template <class F>
@@ -755,15 +899,18 @@ int dispatch(const Oracle& o, F&& fn) {
     case 14: { PhysRD2 ph; ph.D1 = P(0); ph.D2 = P(1); ph.k = P(2); return fn(ph); }
     case 15: { PhysKappaExp ph; ph.fsrc = P(0); return fn(ph); }
     case 16: { PhysSurfaceHeat ph; ph.eps = P(0); ph.eps_s = P(1); ph.c_s = P(2); ph.k = P(3); ph.q0 = P(4); ph.breg = (int)P(5); return fn(ph); }
+    case 18: { PhysEdgeReaction ph; ph.mode = (int)P(0); ph.dim = (int)P(1); return fn(ph); }
+    case 19: { PhysJouleHeat ph; ph.kappa0 = P(0); ph.alpha = P(1); ph.T0 = P(2); ph.lam = P(3); ph.c = P(4); return fn(ph); }
+    case 17: { PhysBoundarySpecies ph; ph.d = P(0); ph.k = P(1); ph.c = P(2); ph.db = P(3); ph.kmax = P(4); ph.cmax = P(5); ph.breg = (int)P(6); return fn(ph); }
   }
   return -1;
 }
 
 int nspec_of(int phys) {
   switch (phys) {
-    case 3: case 4: case 14: return 2;
+    case 3: case 4: case 14: case 17: case 19: return 2;
     case 13: return 3;
-    case 1: case 2: case 5: case 6: case 7: case 8: case 11: case 12: case 15: case 16: return 1;
+    case 1: case 2: case 5: case 6: case 7: case 8: case 11: case 12: case 15: case 16: case 18: return 1;
   }
   return 0;
 }
@@ -803,6 +950,40 @@ void oracle_destroy(void* h) { delete static_cast<Oracle*>(h); }
 
 // assembly = :cellwise (1) or :edgewise (0, the default here)
 void oracle_set_cellwise(void* h, int cellwise) { static_cast<Oracle*>(h)->cellwise = cellwise != 0; }
+
+// enable_species!(sys, ispec, regions) / enable_boundary_species!(sys, ispec,
+// bregions) (src/vfvm_system.jl:433-513): region_species (ns x ncreg,
+// column-major) and bregion_species (ns x nbreg) nonzero where enabled; a node
+// carries the species of the cells and boundary faces containing it.  Returns
+// 0, or -1 for a species that is both a bulk and a boundary species, or for no
+// species at all (the reference's DomainError and "No species enabled").
+int oracle_set_species(void* h, int ncreg, const int* region_species, int nbreg, const int* bregion_species) {
+  Oracle* o = static_cast<Oracle*>(h);
+  const int ns = o->ns, d = o->dim;
+  int maxreg = 1;
+  for (int c = 0; c < o->ncells; ++c) maxreg = std::max(maxreg, o->cellregions[c]);
+  auto mask = [&](const int* tab, int ncols, int reg) {
+    unsigned m = 0;
+    if (reg >= 1 && reg <= ncols)
+      for (int i = 0; i < ns; ++i)
+        if (tab[i + ns * (reg - 1)]) m |= 1u << i;
+    return m;
+  };
+  unsigned bulk = 0, bnd = 0;
+  for (int r = 1; r <= ncreg; ++r) bulk |= mask(region_species, ncreg, r);
+  for (int r = 1; r <= nbreg; ++r) bnd |= mask(bregion_species, nbreg, r);
+  o->reg_spec.assign(maxreg, 0u);
+  for (int r = 1; r <= maxreg; ++r) o->reg_spec[r - 1] = mask(region_species, ncreg, r);
+  o->node_spec.assign(o->N, 0u);
+  for (int c = 0; c < o->ncells; ++c)
+    for (int v = 0; v <= d; ++v) o->node_spec[o->cellnodes[v + (d + 1) * c]] |= o->reg_spec[o->cellregions[c] - 1];
+  for (int b = 0; b < o->nbf; ++b)
+    for (int v = 0; v < d; ++v) o->node_spec[o->bfacenodes[v + d * b]] |= mask(bregion_species, nbreg, o->bfaceregions[b]);
+  bool any = false;
+  for (int K = 0; K < o->N; ++K) any = any || o->node_spec[K] != 0;
+  o->masked = true;
+  return ((bulk & bnd) != 0 || !any) ? -1 : 0;
+}
 
 int oracle_nspec(void* h) { return static_cast<Oracle*>(h)->ns; }
 int oracle_nedges(void* h) { return static_cast<Oracle*>(h)->E; }

@@ -62,6 +62,12 @@ def case(vfvm, name, seed=0):
         g, kind, params, tstep = sg(lin(8), lin(8)), "surface_heat", [1.0, 0.3, 0.5, 2.0, 10.0, 2], 1e-2
     elif name == "surface_heat3d":  # conducting surface layer on the bottom face (region 5)
         g, kind, params, tstep = sg(lin(4), lin(4), lin(4)), "surface_heat", [1.0, 0.3, 0.5, 2.0, 10.0, 5], 1e-2
+    elif name == "edge_reaction2d":  # DevEx002: the unit source as an edge reaction -h^2/4
+        g, kind, params = sg(lin(8), lin(8)), "edge_reaction", [1, 2]
+    elif name == "edge_reaction3d":  # the edge reaction -(x_K - x_L)^2 / 2
+        g, kind, params = sg(lin(3), lin(3), lin(3)), "edge_reaction", [2, 3]
+    elif name == "joule_heat":  # Example206's callbacks on a 3 x 1 rectangle
+        g, kind, params = sg(3 * lin(12), lin(4)), "joule_heat", [1.0, 1.0, 0.5, 1.0, 1.0]
     elif name == "laplace_dirichlet":
         g, kind, params = sg(lin(9)), "laplace_dirichlet", []
     else:
@@ -83,4 +89,5 @@ def random_state(c, nspec, rng):
 
 
 NAMES = ["nlpoisson", "porous", "bipolar", "rd2", "kappa_exp", "ex105", "ex106", "ex110", "ex160", "ex207",
-         "ex301", "ex440", "laplace_dirichlet", "kappa_unstructured", "surface_heat2d", "surface_heat3d"]
+         "ex301", "ex440", "laplace_dirichlet", "kappa_unstructured", "surface_heat2d", "surface_heat3d",
+         "edge_reaction2d", "edge_reaction3d", "joule_heat"]

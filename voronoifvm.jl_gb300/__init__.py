@@ -7,8 +7,8 @@ reference's ``System``/``Physics``/``solve``/``SolverControl`` interface.
 from .grid import Grid, read_sg, simplexgrid, write_sg
 from .system import (AssemblyError, ConvergenceError, EmbeddingError, LinearSolverError, NewtonSolverHistory,
                      Physics, SolverControl, System, TransientSolution, boundary_dirichlet, edgefactors,
-                     evaluate_residual_and_jacobian, fixed_timesteps, integrate, nodevolumes, num_species, solve,
-                     unknowns)
+                     enable_boundary_species, enable_species, evaluate_residual_and_jacobian, fixed_timesteps,
+                     integrate, node_species, nodevolumes, num_species, solve, unknowns)
 from . import _lib
 from .batch import BatchSolver
 from . import learned
@@ -16,5 +16,6 @@ from .build import build_library
 
 __all__ = ["Grid", "simplexgrid", "read_sg", "write_sg", "Physics", "System", "SolverControl", "NewtonSolverHistory", "TransientSolution",
            "AssemblyError", "ConvergenceError", "EmbeddingError", "LinearSolverError", "boundary_dirichlet",
+           "enable_species", "enable_boundary_species", "node_species",
            "edgefactors", "evaluate_residual_and_jacobian", "fixed_timesteps", "integrate", "nodevolumes",
            "num_species", "solve", "unknowns", "build_library"]

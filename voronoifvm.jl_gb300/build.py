@@ -33,7 +33,7 @@ def _nvcc():
 INST_SOURCE = "vfvm_persist_inst.cu"
 INST_PHYSICS = ["PhysEx105", "PhysEx106", "PhysEx110", "PhysEx160", "PhysEx207", "PhysEx301", "PhysEx440",
                 "PhysLaplaceDir", "PhysNLPoisson", "PhysPorous", "PhysBipolar", "PhysRD2", "PhysKappaExp",
-                "PhysSurfaceHeat"]
+                "PhysSurfaceHeat", "PhysBoundarySpecies", "PhysEdgeReaction", "PhysJouleHeat"]
 
 
 def sources():

@@ -20,7 +20,9 @@ __device__ __forceinline__ bool nan_bits(double x) {
 __device__ __forceinline__ bool nan_bits(float x) { return (__float_as_uint(x) & 0x7fffffffu) > 0x7f800000u; }
 
 // Node terms of K: reaction - source + (storage - oldstorage)/tstep
-// (src/vfvm_assembly.jl:38-126), added to fK and the diagonal block jd.
+// (src/vfvm_assembly.jl:38-126), added to fK and the diagonal block jd.  With
+// species restricted to regions (MR and t.reg_spec) only the rows and columns
+// of the species of the item's region (src/vfvm_assemblydata.jl:245-269).
 template <class Ph, typename P, bool MR>
 __device__ __forceinline__ void node_terms(const AsmTables& t, const Ph& ph, int K, const double* uK, const P* uKs,
                                            const double* __restrict__ Uold, double time, double tstepinv,
@@ -32,6 +34,7 @@ __device__ __forceinline__ void node_terms(const AsmTables& t, const Ph& ph, int
   for (int it = nbeg; it < nend; ++it) {
     const int reg = MR ? t.nitem_reg[it] : t.region;
     const double fac = MR ? t.nitem_fac[it] : t.node_fac[K];
+    const unsigned rm = (MR && t.reg_spec) ? t.reg_spec[reg - 1] : ~0u;
     NodeItem ni{K, reg, xK, time, lambda, dK};
     Dual<NS, P> u[NS], r[NS], s[NS];
 #pragma unroll
@@ -51,20 +54,24 @@ __device__ __forceinline__ void node_terms(const AsmTables& t, const Ph& ph, int
     const P facp = P(fac), tip = P(tstepinv);
 #pragma unroll
     for (int i = 0; i < NS; ++i) {
+      if (!((rm >> i) & 1u)) continue;
       fK[i] += fac * (r[i].v - src[i] + (s[i].v - ostor[i]) * tstepinv);
 #pragma unroll
-      for (int j = 0; j < NS; ++j) jd[i * NS + j] += (r[i].d[j] + s[i].d[j] * tip) * facp;
+      for (int j = 0; j < NS; ++j)
+        if ((rm >> j) & 1u) jd[i * NS + j] += (r[i].d[j] + s[i].d[j] * tip) * facp;
     }
   }
 }
 
 // Boundary-face items of K in bface order: legacy Dirichlet/Robin data
-// (src/vfvm_assembly.jl:355-387), breaction - bsource (:388-407) and
-// (bstorage - old bstorage) / tstep (:409-440).
+// (src/vfvm_assembly.jl:355-387, every species of the dense layout),
+// breaction - bsource (:388-407) and (bstorage - old bstorage) / tstep
+// (:409-440) in the rows and columns of the node's species nm
+// (src/vfvm_assemblydata.jl:278-301).
 template <class Ph, typename P>
 __device__ __forceinline__ void bnode_terms(const AsmTables& t, const Ph& ph, int K, const double* uK, const P* uKs,
                                             const double* __restrict__ Uold, double time, double tstepinv,
-                                            double lambda, double* fK, P* jd) {
+                                            double lambda, double* fK, P* jd, unsigned nm = ~0u) {
   constexpr int NS = Ph::NS;
   const double* xK = t.coord + (size_t)K * t.dim;
   const int bbeg = t.bn_ptr[K], bend = t.bn_ptr[K + 1];
@@ -97,9 +104,11 @@ __device__ __forceinline__ void bnode_terms(const AsmTables& t, const Ph& ph, in
       const P facp = P(fac);
 #pragma unroll
       for (int i = 0; i < NS; ++i) {
+        if (!((nm >> i) & 1u)) continue;
         fK[i] += fac * (y[i].v - bsrc[i]);
 #pragma unroll
-        for (int j = 0; j < NS; ++j) jd[i * NS + j] += y[i].d[j] * facp;
+        for (int j = 0; j < NS; ++j)
+          if ((nm >> j) & 1u) jd[i * NS + j] += y[i].d[j] * facp;
       }
     }
     if (Ph::has_bstorage) {
@@ -117,9 +126,11 @@ __device__ __forceinline__ void bnode_terms(const AsmTables& t, const Ph& ph, in
       const P ft = P(fac * tstepinv);
 #pragma unroll
       for (int i = 0; i < NS; ++i) {
+        if (!((nm >> i) & 1u)) continue;
         fK[i] += fac * (s[i].v - so[i]) * tstepinv;
 #pragma unroll
-        for (int j = 0; j < NS; ++j) jd[i * NS + j] += s[i].d[j] * ft;
+        for (int j = 0; j < NS; ++j)
+          if ((nm >> j) & 1u) jd[i * NS + j] += s[i].d[j] * ft;
       }
     }
   }
@@ -127,12 +138,15 @@ __device__ __forceinline__ void bnode_terms(const AsmTables& t, const Ph& ph, in
 
 // Boundary-edge items of Jacobian slot s (edge A-B, A < B), evaluated from
 // node K's end: assemble_bedges (src/vfvm_assembly.jl:444-510), the same sign
-// and factor placement as a bulk edge (first node +f, second -f).
+// and factor placement as a bulk edge (first node +f, second -f); with species
+// restricted to regions, the rows and columns of the first node's species
+// (src/vfvm_assemblydata.jl:391-420).
 template <class Ph, typename P>
 __device__ __forceinline__ void bedge_terms(const AsmTables& t, const Ph& ph, int s, int A, int B, bool kfirst,
                                             const double* uA, const P* uAs, const double* uB, const P* uBs,
                                             double time, double lambda, double* fK, P* jd, P* jo) {
   constexpr int NS = Ph::NS;
+  const unsigned m = t.node_spec ? t.node_spec[A] : ~0u;
   for (int it = t.sbe_ptr[s]; it < t.sbe_ptr[s + 1]; ++it) {
     const double fac = t.sbe_fac[it];
     BEdgeItem be{A, B, t.sbe_reg[it], t.coord + (size_t)A * t.dim, t.coord + (size_t)B * t.dim, time, lambda};
@@ -147,14 +161,17 @@ __device__ __forceinline__ void bedge_terms(const AsmTables& t, const Ph& ph, in
     const P facp = P(fac);
 #pragma unroll
     for (int i = 0; i < NS; ++i) {
+      if (!((m >> i) & 1u)) continue;
       if (kfirst) {
         fK[i] += fac * f[i].v;
 #pragma unroll
-        for (int j = 0; j < NS; ++j) { jd[i * NS + j] += f[i].d[j] * facp; jo[i * NS + j] += f[i].d[NS + j] * facp; }
+        for (int j = 0; j < NS; ++j)
+          if ((m >> j) & 1u) { jd[i * NS + j] += f[i].d[j] * facp; jo[i * NS + j] += f[i].d[NS + j] * facp; }
       } else {
         fK[i] += -(fac * f[i].v);
 #pragma unroll
-        for (int j = 0; j < NS; ++j) { jd[i * NS + j] += (-f[i].d[NS + j]) * facp; jo[i * NS + j] += (-f[i].d[j]) * facp; }
+        for (int j = 0; j < NS; ++j)
+          if ((m >> j) & 1u) { jd[i * NS + j] += (-f[i].d[NS + j]) * facp; jo[i * NS + j] += (-f[i].d[j]) * facp; }
       }
     }
   }
@@ -196,6 +213,7 @@ __device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, 
     for (int it = ebeg; it < eend; ++it) {
       const int reg = MR ? t.sitem_reg[it] : t.region;
       const double fac = MR ? t.sitem_fac[it] : t.slot_fac[s];
+      const unsigned rm = (MR && t.reg_spec) ? t.reg_spec[reg - 1] : ~0u;  // src/vfvm_assemblydata.jl:346-381
       EdgeItem ei{A, B, reg, t.coord + (size_t)A * t.dim, t.coord + (size_t)B * t.dim, time, lambda,
                   t.nodedata ? t.nodedata + (size_t)A * t.nnd : nullptr,
                   t.nodedata ? t.nodedata + (size_t)B * t.nnd : nullptr};
@@ -213,9 +231,11 @@ __device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, 
       if (kfirst) {
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
+          if (!((rm >> i) & 1u)) continue;
           fK[i] += fac * f[i].v;
 #pragma unroll
           for (int j = 0; j < NS; ++j) {
+            if (!((rm >> j) & 1u)) continue;
             jd[i * NS + j] += f[i].d[j] * facp;
             jo[i * NS + j] += f[i].d[NS + j] * facp;
           }
@@ -223,11 +243,39 @@ __device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, 
       } else {
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
+          if (!((rm >> i) & 1u)) continue;
           fK[i] += -(fac * f[i].v);
 #pragma unroll
           for (int j = 0; j < NS; ++j) {
+            if (!((rm >> j) & 1u)) continue;
             jd[i * NS + j] += (-f[i].d[NS + j]) * facp;
             jo[i * NS + j] += (-f[i].d[j]) * facp;
+          }
+        }
+      }
+      if constexpr (Ph::has_edgereaction) {
+        // edgereaction (src/vfvm_assembly.jl:202-238): fac * r added to both end
+        // nodes, the Jacobian entries placed as the reference places them (first
+        // node's row: +dr/du_first, -dr/du_second; second node's row:
+        // -dr/du_first, +dr/du_second)
+        Dual<2 * NS, P> r[NS];
+#pragma unroll
+        for (int i = 0; i < NS; ++i) r[i] = dconst<2 * NS, P>(0.0);
+        ph.edgereaction(r, ua, ub, ei);
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+          if (!((rm >> i) & 1u)) continue;
+          fK[i] += fac * r[i].v;
+#pragma unroll
+          for (int j = 0; j < NS; ++j) {
+            if (!((rm >> j) & 1u)) continue;
+            if (kfirst) {
+              jd[i * NS + j] += r[i].d[j] * facp;
+              jo[i * NS + j] += (-r[i].d[NS + j]) * facp;
+            } else {
+              jd[i * NS + j] += r[i].d[NS + j] * facp;
+              jo[i * NS + j] += (-r[i].d[j]) * facp;
+            }
           }
         }
       }
@@ -245,7 +293,18 @@ __device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, 
     }
   }
 
-  bnode_terms<Ph, P>(t, ph, K, uK, uKs, Uold, time, tstepinv, lambda, fK, jd);
+  const unsigned nm = (MR && t.node_spec) ? t.node_spec[K] : ~0u;
+  bnode_terms<Ph, P>(t, ph, K, uK, uKs, Uold, time, tstepinv, lambda, fK, jd, nm);
+  if (MR && t.node_spec) {
+    // the species K does not carry: F += U - Uold, unit diagonal
+    // (_eval_and_assemble_inactive_species, src/vfvm_system.jl:1012-1026)
+#pragma unroll
+    for (int i = 0; i < NS; ++i)
+      if (!((nm >> i) & 1u)) {
+        fK[i] += uK[i] - Uold[(size_t)K * NS + i];
+        jd[i * NS + i] += P(1);
+      }
+  }
 
   bool bad = false;
 #pragma unroll
@@ -270,7 +329,8 @@ __device__ __forceinline__ void init_dirichlet_node(const AsmTables& t, const Ph
                                                     double time, double lambda) {
   constexpr int NS = Ph::NS;
   const int bbeg = t.bn_ptr[K], bend = t.bn_ptr[K + 1];
-  if (bbeg == bend) return;
+  const unsigned nm = t.node_spec ? t.node_spec[K] : ~0u;
+  if (bbeg == bend && !t.node_spec) return;
   const double* xK = t.coord + (size_t)K * t.dim;
   double u[NS];
 #pragma unroll
@@ -291,6 +351,10 @@ __device__ __forceinline__ void init_dirichlet_node(const AsmTables& t, const Ph
       }
     }
   }
+  // species K does not carry start at 0 (_initialize_inactive_dof!, src/vfvm_system.jl:1030-1042)
+#pragma unroll
+  for (int i = 0; i < NS; ++i)
+    if (!((nm >> i) & 1u)) u[i] = 0.0;
 #pragma unroll
   for (int i = 0; i < NS; ++i) U[(size_t)K * NS + i] = u[i];
 }

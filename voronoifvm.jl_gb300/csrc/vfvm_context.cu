@@ -171,6 +171,13 @@ void probe_t(const Ph& ph0, const double* params, int dim, const std::vector<int
       for (int i = 0; i < NS; ++i)
         for (int j = 0; j < 2 * NS; ++j)
           if (f[i].d[j] != 0.0) em[i * 2 * NS + j] = 1;
+      if (Ph::has_edgereaction) {  // the same four entries per species pair as a flux
+        for (int i = 0; i < NS; ++i) f[i] = dconst<2 * NS, double>(0);
+        ph.edgereaction(f, uk, ul, ei);
+        for (int i = 0; i < NS; ++i)
+          for (int j = 0; j < 2 * NS; ++j)
+            if (f[i].d[j] != 0.0) em[i * 2 * NS + j] = 1;
+      }
     }
     for (int reg : bregs) {
       double dv[NS];
@@ -245,6 +252,8 @@ AsmTables vfvm_ctx::tables() const {
   t.sbe_ptr = sbe_ptr.n ? sbe_ptr.p : nullptr; t.sbe_reg = sbe_reg.p; t.sbe_fac = sbe_fac.p;
   t.params = params.p; t.nodedata = nodedata.p; t.nnd = nnd;
   t.bfactors = bfactors.p; t.bvalues = bvalues.p; t.nbregions = nbregions; t.has_legacy = has_legacy ? 1 : 0;
+  t.reg_spec = species_masked ? reg_spec.p : nullptr;
+  t.node_spec = species_masked ? node_spec.p : nullptr;
   return t;
 }
 
@@ -296,6 +305,12 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
   if (ns == 0) return nullptr;
   if (ph->nparams < physics_nparams(ph->physics_id) || (ph->nparams > 0 && !ph->params)) return nullptr;
   if (ph->nnodedata < physics_nnodedata(ph->physics_id) || (ph->nnodedata > 0 && !ph->nodedata)) return nullptr;
+  {
+    std::vector<double> p(ph->params, ph->params + ph->nparams);
+    p.resize(16, 0.0);
+    if (!dispatch_physics(ph->physics_id, [&](auto phy) { return decltype(phy)::valid(g->dim, p.data()) ? 1 : 0; }))
+      return nullptr;
+  }
   const int dim = g->dim, N = g->nnodes, nc = g->ncells, nbf = g->nbfaces, nvc = dim + 1;
   // index validation: every table entry must address an existing node/region
   for (int64_t i = 0; i < (int64_t)nvc * nc; ++i) if (g->cellnodes[i] < 0 || g->cellnodes[i] >= N) return nullptr;
@@ -337,6 +352,56 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
   c->single_region = g->cellregions[0];
   c->multireg = false;
   for (int i = 1; i < nc; ++i) if (g->cellregions[i] != c->single_region) { c->multireg = true; break; }
+
+  // --- species restricted to regions (enable_species! / enable_boundary_species!,
+  // src/vfvm_system.jl:433-513): the species mask of every cell region and, from
+  // the cells and boundary faces containing it, of every node (node_dof)
+  if (ph->ncellregions_species > 0 || ph->nbregions_species > 0) {
+    if (ns > 32 || ph->ncellregions_species < 0 || ph->nbregions_species < 0 ||
+        (ph->ncellregions_species > 0 && !ph->region_species) ||
+        (ph->nbregions_species > 0 && !ph->bregion_species)) {
+      *status = VFVM_ERR_INPUT;
+      delete c;
+      return nullptr;
+    }
+    const unsigned all = ns == 32 ? ~0u : (1u << ns) - 1u;
+    auto mask_of = [&](const int32_t* tab, int ncols, int reg) {
+      unsigned m = 0;
+      if (reg >= 1 && reg <= ncols)
+        for (int i = 0; i < ns; ++i)
+          if (tab[i + (size_t)ns * (reg - 1)]) m |= 1u << i;
+      return m;
+    };
+    c->h_reg_spec.assign(maxreg, 0u);
+    for (int r = 1; r <= maxreg; ++r) c->h_reg_spec[r - 1] = mask_of(ph->region_species, ph->ncellregions_species, r);
+    unsigned bulk = 0, bnd = 0;  // a species is a bulk or a boundary species, not both
+    for (int r = 1; r <= ph->ncellregions_species; ++r) bulk |= mask_of(ph->region_species, ph->ncellregions_species, r);
+    for (int r = 1; r <= ph->nbregions_species; ++r) bnd |= mask_of(ph->bregion_species, ph->nbregions_species, r);
+    c->h_node_spec.assign(N, 0u);
+    for (int cell = 0; cell < nc; ++cell) {
+      const unsigned m = c->h_reg_spec[g->cellregions[cell] - 1];
+      for (int v = 0; v < nvc; ++v) c->h_node_spec[g->cellnodes[v + (size_t)nvc * cell]] |= m;
+    }
+    for (int b = 0; b < nbf; ++b) {
+      const unsigned m = mask_of(ph->bregion_species, ph->nbregions_species, g->bfaceregions[b]);
+      for (int v = 0; v < dim; ++v) c->h_node_spec[g->bfacenodes[v + (size_t)dim * b]] |= m;
+    }
+    bool any = false, masked = false;
+    for (int k = 0; k < N; ++k) { any = any || c->h_node_spec[k] != 0; masked = masked || c->h_node_spec[k] != all; }
+    for (int cell = 0; cell < nc; ++cell) masked = masked || c->h_reg_spec[g->cellregions[cell] - 1] != all;
+    if ((bulk & bnd) != 0 || !any) {  // the reference's DomainError / "No species enabled"
+      *status = VFVM_ERR_INPUT;
+      delete c;
+      return nullptr;
+    }
+    if (masked) {
+      c->species_masked = true;
+      c->multireg = true;  // the node-centric kernel with per-item regions applies the masks
+    } else {
+      c->h_reg_spec.clear();
+      c->h_node_spec.clear();
+    }
+  }
   std::vector<std::vector<RegFac>> nfac(N), efac(E);
   {
     const double* xs[4];
@@ -542,9 +607,34 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
         for (int it = bn_ptr[k]; it < bn_ptr[k + 1]; ++it)
           for (int i = 0; i < ns; ++i)
             if (bn_reg[it] - 1 < c->nbregions && bfac_h[i + (size_t)ns * (bn_reg[it] - 1)] != 0.0) legdiag[i] = 1;
+      // species restricted to regions: entry (i, j) of a term exists only when
+      // both species belong to the term's region (cell terms) or node (boundary
+      // terms; a boundary edge: its first node), src/vfvm_assemblydata.jl:245-470
+      const bool msk = c->species_masked;
+      auto pair_in = [](unsigned m, int i, int j) { return ((m >> i) & 1u) && ((m >> j) & 1u); };
+      auto node_items_allow = [&](int i, int j) {
+        if (!msk) return true;
+        for (int it = nitem_ptr[k]; it < nitem_ptr[k + 1]; ++it)
+          if (pair_in(c->h_reg_spec[nitem_reg[it] - 1], i, j)) return true;
+        return false;
+      };
+      auto slot_items_allow = [&](int s, int i, int j) {
+        if (!msk) return true;
+        for (int it = sitem_ptr[s]; it < sitem_ptr[s + 1]; ++it)
+          if (pair_in(c->h_reg_spec[sitem_reg[it] - 1], i, j)) return true;
+        return false;
+      };
+      auto edges_allow = [&](int i, int j) {  // some incident edge carries (i, j)
+        if (!msk) return true;
+        for (int s2 = c->h_browptr[k]; s2 < c->h_browptr[k + 1]; ++s2)
+          if (c->h_bcol[s2] != k && slot_items_allow(s2, i, j)) return true;
+        return false;
+      };
+      const unsigned kspec = msk ? c->h_node_spec[k] : ~0u;
       // boundary-edge (bflux) partials of this row: per slot, and summed into the diagonal
       auto bflux_on = [&](int s, bool first_col, int i, int j) {
         if (sbe_ptr.empty()) return false;
+        if (msk && !pair_in(c->h_node_spec[std::min(k, c->h_bcol[s])], i, j)) return false;
         for (int it = sbe_ptr[s]; it < sbe_ptr[s + 1]; ++it) {
           const auto& mk = bem_of_reg[sbe_reg[it]];
           if (mk[i * 2 * ns + (first_col ? 0 : ns) + j]) return true;
@@ -557,19 +647,22 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
           for (int j = 0; j < ns; ++j) {
             bool on;
             if (m == k) {
-              on = nm[i * ns + j] || em[i * 2 * ns + j] || em[i * 2 * ns + ns + j];
+              on = (nm[i * ns + j] && node_items_allow(i, j)) ||
+                   ((em[i * 2 * ns + j] || em[i * 2 * ns + ns + j]) && edges_allow(i, j));
               if (bnode) {
-                on = on || bm[i * ns + j];
+                on = on || (bm[i * ns + j] && pair_in(kspec, i, j));
                 if (i == j && legdiag[i]) on = true;
               }
+              // a species the node does not carry: F += U - Uold, unit diagonal
+              if (i == j && msk && !((kspec >> i) & 1u)) on = true;
               for (int s2 = c->h_browptr[k]; !on && s2 < c->h_browptr[k + 1]; ++s2) {
                 const int m2 = c->h_bcol[s2];
                 if (m2 != k) on = bflux_on(s2, k < m2, i, j);  // d f / d u_K of K's boundary edges
               }
-            } else if (k < m) {
-              on = em[i * 2 * ns + ns + j] || bflux_on(s, false, i, j);  // k first: d f / d u_second
-            } else {
-              on = em[i * 2 * ns + j] || bflux_on(s, true, i, j);        // k second: d f / d u_first
+            } else if (k < m) {  // k first: d f / d u_second
+              on = (em[i * 2 * ns + ns + j] && slot_items_allow(s, i, j)) || bflux_on(s, false, i, j);
+            } else {             // k second: d f / d u_first
+              on = (em[i * 2 * ns + j] && slot_items_allow(s, i, j)) || bflux_on(s, true, i, j);
             }
             if (on) {
               c->h_colind.push_back(m * ns + j);
@@ -698,6 +791,10 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
   SETUP_CUDA(c->nodedata.upload(nd));
   SETUP_CUDA(c->bfactors.upload(bfac_h));
   SETUP_CUDA(c->bvalues.upload(bval_h));
+  if (c->species_masked) {
+    SETUP_CUDA(c->reg_spec.upload(c->h_reg_spec));
+    SETUP_CUDA(c->node_spec.upload(c->h_node_spec));
+  }
   SETUP_CUDA(c->dirichlet_dof.upload(dir_dof));
   if (!sbe_ptr.empty()) {
     SETUP_CUDA(c->sbe_ptr.upload(sbe_ptr));

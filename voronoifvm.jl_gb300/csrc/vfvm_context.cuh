@@ -58,6 +58,10 @@ struct AsmTables {
   const double* params;
   const double* nodedata; int nnd;
   const double* bfactors; const double* bvalues; int nbregions; int has_legacy;
+  // species restricted to regions (nullptr: every species on every node):
+  // reg_spec[ireg-1] = bit mask of the species enabled in cell region ireg,
+  // node_spec[K] = bit mask of the species of node K
+  const unsigned* reg_spec; const unsigned* node_spec;
 };
 
 // Node tiles of the edge-once assembly (vfvm_tiles.cu builds them, the tiled
@@ -138,6 +142,11 @@ struct vfvm_ctx {
   vfvm::DBuf<uint8_t> dirichlet_dof;       // 1 where a Dirichlet penalty acts on the dof
   vfvm::DBuf<int> sbe_ptr, sbe_reg;         // boundary-edge items per slot (physics with bflux)
   vfvm::DBuf<double> sbe_fac;
+  // species restricted to regions (enable_species! / enable_boundary_species!);
+  // such contexts take the multi-region paths (multireg is set)
+  bool species_masked = false;
+  std::vector<unsigned> h_reg_spec, h_node_spec;
+  vfvm::DBuf<unsigned> reg_spec, node_spec;
 
   // scalar (reference) pattern
   int64_t nnz = 0;

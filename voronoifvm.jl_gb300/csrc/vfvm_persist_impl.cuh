@@ -390,6 +390,7 @@ int sweep_eager(const SweepArgs<Ph, KT>& a, cudaStream_t s) {
   const dim3 grid(a.bpi, a.S);
   std::vector<SweepState> st(a.S);
   std::vector<int> list;
+  int started = 0;  // systems that entered the current BiCGStab loop
   SweepCall call;
   VFVM_CUDA(cudaMemcpyAsync(&call, a.call, sizeof(SweepCall), cudaMemcpyDeviceToHost, s));
   auto any = [&](int which, bool& out) -> int {
@@ -402,7 +403,12 @@ int sweep_eager(const SweepArgs<Ph, KT>& a, cudaStream_t s) {
       out = out || (which == 0 ? x.kactive != 0 : (x.nactive || x.restart));
       if (x.kactive) list.push_back(i);
     }
-    if (which == 0 && (int)list.size() <= call.ctl.batch_tail) out = false;  // the batch-level inexact Newton rule
+    // the batch-level inexact Newton rule (sw_cond_kernel)
+    if (which == 1) started = 0;
+    if (which == 0) {
+      if (started == 0) started = (int)list.size();
+      if ((int)list.size() <= call.ctl.batch_tail && 10 * (int)list.size() <= started) out = false;
+    }
     if (which == 0) {  // the compact list the iteration kernels stride over
       const int cnt = (int)list.size();
       VFVM_CUDA(cudaMemcpyAsync(a.kcount, &cnt, sizeof(int), cudaMemcpyHostToDevice, s));
@@ -466,7 +472,7 @@ int sweep_run(vfvm_batch* b, const vfvm_control* ctl, int bpi_req, double time, 
     VFVM_CUDA(take(h.tickets, (size_t)S * 4));
     VFVM_CUDA(take(h.call, sizeof(SweepCall)));
     VFVM_CUDA(take(h.klist, (size_t)(S + 1) * 4));
-    VFVM_CUDA(take(h.runs, 2 * sizeof(unsigned)));
+    VFVM_CUDA(take(h.runs, 4 * sizeof(unsigned)));
     VFVM_CUDA(cudaMemset(h.tickets.p, 0, (size_t)S * 4));
     VFVM_CUDA(cudaMemset(h.st.p, 0, (size_t)S * sizeof(SweepState)));
     VFVM_CUDA(cudaMemset(h.vecs.p, 0, (size_t)9 * S * n * kt));
@@ -527,7 +533,7 @@ int sweep_run(vfvm_batch* b, const vfvm_control* ctl, int bpi_req, double time, 
   call.fallback = guess ? fallback : nullptr;
   call.guard = guess ? 1 : 0;
   VFVM_CUDA(cudaMemcpyAsync(h.call.p, &call, sizeof(call), cudaMemcpyHostToDevice, b->stream));
-  VFVM_CUDA(cudaMemsetAsync(h.runs.p, 0, 2 * sizeof(unsigned), b->stream));
+  VFVM_CUDA(cudaMemsetAsync(h.runs.p, 0, 4 * sizeof(unsigned), b->stream));
   VFVM_CUDA(cudaEventRecord(b->e0, b->stream));
   const char* eager = std::getenv("VFVM_SWEEP_EAGER");
   if (eager && eager[0] == '1') {

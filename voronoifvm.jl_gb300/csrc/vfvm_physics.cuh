@@ -21,13 +21,18 @@ struct PhysBase {
   // boundary callbacks beyond breaction: bflux (boundary edges), bstorage, bsource
   // (src/vfvm_physics.jl:82-180)
   static constexpr bool has_bflux = false, has_bstorage = false, has_bsource = false;
+  // edgereaction (src/vfvm_physics.jl:67-182): an edge term added to both end nodes
+  static constexpr bool has_edgereaction = false;
   template <class T> VFVM_HD void reaction(T*, const T*, const NodeItem&) const {}
+  template <class T> VFVM_HD void edgereaction(T*, const T*, const T*, const EdgeItem&) const {}
   template <class T> VFVM_HD void storage(T*, const T*, const NodeItem&) const {}
   VFVM_HD void source(double*, const NodeItem&) const {}
   template <class T> VFVM_HD void breaction(T*, const T*, const BNodeItem&) const {}
   template <class T> VFVM_HD void bflux(T*, const T*, const T*, const BEdgeItem&) const {}
   template <class T> VFVM_HD void bstorage(T*, const T*, const BNodeItem&) const {}
   VFVM_HD void bsource(double*, const BNodeItem&) const {}
+  // whether the parameter block suits grids of this dimension (checked once by vfvm_create)
+  static bool valid(int, const double*) { return true; }
 };
 
 // examples/Example105_NonlinearPoisson1D.jl:41-60;  params: eps
@@ -275,12 +280,119 @@ struct PhysSurfaceHeat : PhysBase {
   }
 };
 
+// A bulk species and a boundary species (examples/Example230_BoundaryFlux.jl):
+// species 1: -d u'' + k u = c (flux, reaction, source); species 2 on boundary
+// region breg: -d_b v'' + k_b(y) v = c_b(y) along the boundary (bflux,
+// breaction, bsource), k_b = kmax, c_b = 0 where y <= 1/2, k_b = 0, c_b = cmax
+// elsewhere.  The bulk callbacks carry the same law for species 2 in the first
+// coordinate, so a 1D grid with species 2 enabled as a bulk species solves the
+// example's reference line problem (the example's node-index switch of k and c
+// at the middle node equals the coordinate switch at 1/2).  Species 2 is
+// meant to be restricted to breg (enable_boundary_species!) on grids of
+// dimension 2, and breg = 0 on the 1D grid.
+// params: d, k, c, d_b, kmax, cmax, breg
+struct PhysBoundarySpecies : PhysBase {
+  static constexpr int NS = 2;
+  static constexpr bool has_reaction = true, has_source = true, has_breaction = true, has_bflux = true,
+                        has_bsource = true;
+  double d, k, c, db, kmax, cmax;
+  int breg;
+  VFVM_HD void load(const double* p) { d = p[0]; k = p[1]; c = p[2]; db = p[3]; kmax = p[4]; cmax = p[5]; breg = (int)p[6]; }
+  // the boundary callbacks read the second coordinate: boundary region breg needs dim >= 2
+  static bool valid(int dim, const double* p) { return dim >= 2 || (int)p[6] == 0; }
+  VFVM_HD double kb(double s) const { return s <= 0.5 ? kmax : 0.0; }
+  VFVM_HD double cb(double s) const { return s <= 0.5 ? 0.0 : cmax; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const {
+    f[0] = (uK[0] - uL[0]) * d;
+    f[1] = (uK[1] - uL[1]) * db;
+  }
+  template <class T> VFVM_HD void reaction(T* f, const T* u, const NodeItem& n) const {
+    f[0] = u[0] * k;
+    f[1] = u[1] * kb(n.x[0]);
+  }
+  VFVM_HD void source(double* f, const NodeItem& n) const { f[0] = c; f[1] = cb(n.x[0]); }
+  template <class T> VFVM_HD void bflux(T* f, const T* uK, const T* uL, const BEdgeItem& e) const {
+    if (e.region == breg) f[1] = (uK[1] - uL[1]) * db;
+  }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const {
+    if (b.region == breg) f[1] = u[1] * kb(b.x[1]);
+  }
+  VFVM_HD void bsource(double* f, const BNodeItem& b) const {
+    if (b.region == breg) f[1] = cb(b.x[1]);
+  }
+};
+
+// examples/DevEx002_EdgeReaction.jl:49-104 (case :compare_max): u_t - div grad u
+// = 1 with u = 0 on every boundary region (1-6), the unit source given as
+// mode 0: a node reaction -1; mode 1: an edge reaction -h^2/(2 dim), h the
+// edge length; mode 2: an edge reaction -(x_K - x_L)^2 / 2.
+// params: mode, dim
+struct PhysEdgeReaction : PhysBase {
+  static constexpr int NS = 1;
+  static constexpr bool has_reaction = true, has_storage = true, has_breaction = true, has_edgereaction = true;
+  int mode, dim;
+  VFVM_HD void load(const double* p) { mode = (int)p[0]; dim = (int)p[1]; }
+  static bool valid(int d, const double* p) { return (int)p[1] == d && p[0] >= 0.0 && p[0] <= 2.0; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const { f[0] = uK[0] - uL[0]; }
+  template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const { f[0] = u[0]; }
+  // constant terms are written as u * 0 + value so that T may be a dual number
+  template <class T> VFVM_HD void reaction(T* f, const T* u, const NodeItem&) const {
+    if (mode == 0) f[0] = u[0] * 0.0 + (-1.0);
+  }
+  template <class T> VFVM_HD void edgereaction(T* f, const T* uK, const T*, const EdgeItem& e) const {
+    if (mode == 1) {
+      double s = 0.0;
+      for (int d = 0; d < dim; ++d) s += (e.xK[d] - e.xL[d]) * (e.xK[d] - e.xL[d]);
+      const double h = sqrt(s);  // meas(edge)
+      f[0] = uK[0] * 0.0 + (-1.0 * (h * h) / (2 * dim));
+    } else if (mode == 2) {
+      const double dp = e.xK[0] - e.xL[0];
+      f[0] = uK[0] * 0.0 + (-dp * dp / 2);
+    }
+  }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const {
+    for (int r = 1; r <= 6; ++r) boundary_dirichlet(f, u, b, 0, r, 0.0);
+  }
+};
+
+// The callbacks of examples/Example206_JouleHeat.jl:63-92 (phi, T): flux
+// kappa(y_T) (phi_K - phi_L), lambda (T_K - T_L); edge reaction (Joule heat)
+// -kappa(y_T) (phi_K - phi_L)^2 on T; storage c T; phi = -10 on boundary
+// region 1, +10 on region 2; Robin 0.5 T - T0 for T on regions 1-4.  kappa(T)
+// = kappa0 exp(alpha (T - T0)) is evaluated at the output value y_T, which is
+// still 0 where the example reads it (the example's own form).
+// params: kappa0, alpha, T0, lambda, c
+struct PhysJouleHeat : PhysBase {
+  static constexpr int NS = 2;
+  static constexpr bool has_storage = true, has_breaction = true, has_edgereaction = true;
+  double kappa0, alpha, T0, lam, c;
+  VFVM_HD void load(const double* p) { kappa0 = p[0]; alpha = p[1]; T0 = p[2]; lam = p[3]; c = p[4]; }
+  template <class T> VFVM_HD T kappa(const T& t) const { return exp((t - T0) * alpha) * kappa0; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const {
+    f[0] = kappa(f[1]) * (uK[0] - uL[0]);
+    f[1] = (uK[1] - uL[1]) * lam;
+  }
+  template <class T> VFVM_HD void edgereaction(T* f, const T* uK, const T* uL, const EdgeItem&) const {
+    const T d = uK[0] - uL[0];
+    f[1] = kappa(f[1]) * (-1.0) * d * d;
+  }
+  template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const { f[1] = u[1] * c; }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const {
+    boundary_dirichlet(f, u, b, 0, 1, -10.0);
+    boundary_dirichlet(f, u, b, 0, 2, 10.0);
+    for (int r = 1; r <= 4; ++r)
+      if (b.region == r) f[1] = f[1] + (u[1] * 0.5 - T0);  // boundary_robin!: y += factor u - value
+  }
+};
+
 inline int physics_nspec(int id) {
   switch (id) {
     case VFVM_PHYS_EX105: case VFVM_PHYS_EX106: case VFVM_PHYS_EX207: case VFVM_PHYS_EX301:
     case VFVM_PHYS_EX440: case VFVM_PHYS_LAPLACE_DIRICHLET: case VFVM_PHYS_NLPOISSON:
-    case VFVM_PHYS_POROUS: case VFVM_PHYS_KAPPA_EXP: case VFVM_PHYS_SURFACE_HEAT: return 1;
-    case VFVM_PHYS_EX110: case VFVM_PHYS_EX160: case VFVM_PHYS_RD2: return 2;
+    case VFVM_PHYS_POROUS: case VFVM_PHYS_KAPPA_EXP: case VFVM_PHYS_SURFACE_HEAT:
+    case VFVM_PHYS_EDGE_REACTION: return 1;
+    case VFVM_PHYS_EX110: case VFVM_PHYS_EX160: case VFVM_PHYS_RD2: case VFVM_PHYS_BOUNDARY_SPECIES:
+    case VFVM_PHYS_JOULE_HEAT: return 2;
     case VFVM_PHYS_BIPOLAR: return 3;
   }
   return 0;
@@ -293,6 +405,9 @@ inline int physics_nparams(int id) {
     case VFVM_PHYS_EX160: case VFVM_PHYS_RD2: return 3;
     case VFVM_PHYS_BIPOLAR: return 7;
     case VFVM_PHYS_SURFACE_HEAT: return 6;
+    case VFVM_PHYS_BOUNDARY_SPECIES: return 7;
+    case VFVM_PHYS_EDGE_REACTION: return 2;
+    case VFVM_PHYS_JOULE_HEAT: return 5;
   }
   return 0;
 }
@@ -316,6 +431,9 @@ int dispatch_physics(int id, Fn&& fn) {
     case VFVM_PHYS_RD2: return fn(PhysRD2{});
     case VFVM_PHYS_KAPPA_EXP: return fn(PhysKappaExp{});
     case VFVM_PHYS_SURFACE_HEAT: return fn(PhysSurfaceHeat{});
+    case VFVM_PHYS_BOUNDARY_SPECIES: return fn(PhysBoundarySpecies{});
+    case VFVM_PHYS_EDGE_REACTION: return fn(PhysEdgeReaction{});
+    case VFVM_PHYS_JOULE_HEAT: return fn(PhysJouleHeat{});
   }
   return VFVM_ERR_INPUT;
 }

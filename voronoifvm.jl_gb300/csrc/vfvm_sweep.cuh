@@ -59,7 +59,8 @@ struct SweepArgs {
   int ncolors;
   int* klist;                  // systems still in BiCGStab (built before each iteration)
   int* kcount;
-  unsigned* runs;              // loop-condition evaluations [BiCGStab, Newton] (launch accounting)
+  unsigned* runs;              // loop-condition evaluations [BiCGStab, Newton] (launch accounting),
+                               // systems that entered the current BiCGStab loop
 };
 
 // The work unit of a block: system i, block lb of the nb blocks serving it.
@@ -650,8 +651,11 @@ __global__ void __launch_bounds__(kSweepThreads) sw_update_kernel(SweepArgs<Ph, 
 // in system order (one block; each thread takes a contiguous chunk).
 // Loop condition of the sweep graph: which = 1, any system still in Newton;
 // which = 0, any system still in BiCGStab (and the compact list of them) --
-// unless at most call->ctl.batch_tail systems are (the batch-level inexact
-// Newton rule: the loop ends and they keep their current iterate).
+// unless at most call->ctl.batch_tail systems are and they are at most a tenth
+// of the systems that entered this BiCGStab loop (the batch-level inexact
+// Newton rule: the loop ends and the stragglers keep their current iterate).
+// runs[0..1]: loop bodies executed; runs[2]: systems that entered the current
+// BiCGStab loop (set by its first evaluation, cleared by the Newton condition).
 static __global__ void __launch_bounds__(1024) sw_cond_kernel(const SweepState* st, int S, int which,
                                                              cudaGraphConditionalHandle h, int* klist, int* kcount,
                                                              unsigned* runs, const SweepCall* call) {
@@ -685,8 +689,14 @@ static __global__ void __launch_bounds__(1024) sw_cond_kernel(const SweepState* 
     if (t == 0) *kcount = total;
   }
   if (t == 0) {
-    const int tail = which == 0 ? call->ctl.batch_tail : 0;
-    cudaGraphSetConditional(h, total > tail ? 1u : 0u);
+    bool go = total > 0;
+    if (which == 1) {
+      runs[2] = 0u;
+    } else {
+      if (runs[2] == 0u) runs[2] = (unsigned)total;
+      if (total <= call->ctl.batch_tail && 10u * (unsigned)total <= runs[2]) go = false;
+    }
+    cudaGraphSetConditional(h, go ? 1u : 0u);
   }
 }
 

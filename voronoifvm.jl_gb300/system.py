@@ -8,6 +8,9 @@ Names, argument meaning and error behaviour follow the reference:
   cannot cross the C ABI
 * ``boundary_dirichlet(sys, ispec, ireg, val)`` -- the system-level (legacy)
   Dirichlet data, src/vfvm_system.jl:329 and src/vfvm_assembly.jl:355-387
+* ``enable_species(sys, ispec, regions)``, ``enable_boundary_species(sys, ispec,
+  bregions)`` -- species restricted to cell or boundary regions,
+  src/vfvm_system.jl:433-513
 * ``SolverControl``, ``fixed_timesteps``   -- src/vfvm_solvercontrol.jl:13-327
 * ``solve(sys; inival, control, times, embed, tstep, time, data)`` --
   src/vfvm_solver.jl:551-668
@@ -35,7 +38,8 @@ from .grid import Grid
 
 __all__ = ["Physics", "System", "SolverControl", "NewtonSolverHistory", "TransientSolution",
            "ConvergenceError", "AssemblyError", "LinearSolverError", "EmbeddingError",
-           "boundary_dirichlet", "solve", "unknowns", "evaluate_residual_and_jacobian",
+           "boundary_dirichlet", "enable_species", "enable_boundary_species", "solve", "unknowns",
+           "evaluate_residual_and_jacobian", "node_species",
            "fixed_timesteps", "nodevolumes", "integrate", "num_species"]
 
 Dirichlet = 1.0e30  # src/vfvm_system.jl:329
@@ -142,7 +146,8 @@ class SolverControl:
     # unknowns (aggregates of nodes x species, at most 208); 0 = one-level only
     coarse: int = 0
     # batched solves on the sweep engine: end a Newton step's BiCGStab loop once at
-    # most this many systems still iterate (they keep their current iterate; 0: off)
+    # most this many systems still iterate and they are at most a tenth of those
+    # that entered the loop (they keep their current iterate; 0: off)
     batch_krylov_tail: int = 0
     # time / embedding step control of solve(times=...) / solve(embed=...):
     # "device" runs the whole step loop as one CUDA graph launch (the step
@@ -230,23 +235,41 @@ class System:
     edgewise tables (each edge's factors summed over its cells once, on the
     host), so every edge flux is evaluated once per edge instead of once per
     cell sharing it; the result agrees with the reference's cellwise summation
-    to rounding."""
+    to rounding.
 
-    def __init__(self, grid: Grid, physics: Physics, species: Sequence[int] = (1,), is_linear: bool = False,
-                 assembly: str = "edgewise", unknown_storage: str = "dense"):
+    ``species``: the species enabled in every cell region (``None``: all of
+    the physics' species).  ``enable_species`` / ``enable_boundary_species``
+    restrict species to regions; the first such call on a system created with
+    ``species=None`` starts from no species.
+
+    ``unknown_storage``: the device keeps the dense layout (nspec unknowns per
+    node) in both modes; a species a node does not carry is decoupled there by
+    a unit row.  With ``:sparse`` the solutions read 0 on those dofs and
+    ``evaluate_residual_and_jacobian`` returns the system of the carried dofs
+    only -- what the reference's sparse storage holds."""
+
+    def __init__(self, grid: Grid, physics: Physics, species: Optional[Sequence[int]] = None,
+                 is_linear: bool = False, assembly: str = "edgewise", unknown_storage: str = "dense"):
         if assembly not in ("edgewise", "cellwise"):
             raise ValueError("assembly must be :edgewise or :cellwise")
-        if unknown_storage != "dense":
-            raise ValueError("only dense unknown storage is offloaded")
+        if unknown_storage not in ("dense", "sparse"):
+            raise ValueError("unknown_storage must be :dense or :sparse")
         self.grid = grid
         self.physics = physics
         self.nspec = L.PHYSICS_NSPEC[physics.physics_id]
-        self.species = list(species)
         self.is_linear = is_linear
         self.assembly = assembly
+        self.unknown_storage = unknown_storage
         nb = max(grid.num_bfaceregions, 1)
         self.boundary_factors = np.zeros((self.nspec, nb), order="F")
         self.boundary_values = np.zeros((self.nspec, nb), order="F")
+        # region_species (nspec x cell regions) / bregion_species (nspec x
+        # boundary regions): None = every species on every node
+        self.region_species = None
+        self.bregion_species = None
+        self.species = list(range(1, self.nspec + 1)) if species is None else list(species)
+        if species is not None:
+            enable_species(self, self.species, None)
         self._ctx = None
         self._ctx_key = None
         self._nodedata_id = None
@@ -282,13 +305,22 @@ class System:
         keep["bv"] = np.asfortranarray(self.boundary_values)
         pt = L.Physics_t(self.physics.physics_id, len(self.physics.data), L.ptr(params), nd, ndp,
                          keep["bf"].shape[1], L.ptr(keep["bf"]), L.ptr(keep["bv"]))
+        if self.region_species is not None:
+            keep["rs"] = np.asfortranarray(self.region_species, dtype=np.int32)
+            keep["bs"] = np.asfortranarray(self.bregion_species, dtype=np.int32)
+            pt.ncellregions_species = keep["rs"].shape[1]
+            pt.region_species = L.ptr(keep["rs"], L.c_i32)
+            pt.nbregions_species = keep["bs"].shape[1]
+            pt.bregion_species = L.ptr(keep["bs"], L.c_i32)
         return gt, pt, keep
 
     @property
     def ctx(self):
         nd = self.physics.nodedata
         key = (self.boundary_factors.tobytes(), self.boundary_values.tobytes(),
-               None if nd is None else np.shape(nd))
+               None if nd is None else np.shape(nd),
+               None if self.region_species is None else (self.region_species.tobytes(),
+                                                         self.bregion_species.tobytes()))
         if self._ctx is None or key != self._ctx_key:
             lib = L.load()
             self.close()
@@ -369,6 +401,79 @@ def boundary_dirichlet(sys: System, ispec: int, ireg: int, val: float):
     sys.boundary_values[ispec - 1, ireg - 1] = val
 
 
+def _species_tables(sys: System):
+    if sys.region_species is None:
+        g = sys.grid
+        nreg = int(np.max(g.cellregions)) if g.ncells else 1
+        nb = max(int(np.max(g.bfaceregions)) if g.nbfaces else 1, 1)
+        sys.region_species = np.zeros((sys.nspec, nreg), dtype=np.int32, order="F")
+        sys.bregion_species = np.zeros((sys.nspec, nb), dtype=np.int32, order="F")
+    return sys.region_species, sys.bregion_species
+
+
+def enable_species(sys: System, ispec, regions=None):
+    """enable_species!(system, ispec, regions) (src/vfvm_system.jl:433-480): add
+    species ``ispec`` (1-based; an int or a list) to the cell regions
+    ``regions`` (1-based; None: all).  A species cannot be both a bulk and a
+    boundary species (the reference's DomainError, raised as ValueError)."""
+    rs, bs = _species_tables(sys)
+    regs = range(1, rs.shape[1] + 1) if regions is None else list(regions)
+    for i in ([ispec] if np.isscalar(ispec) else list(ispec)):
+        i = int(i)
+        if not 1 <= i <= sys.nspec:
+            raise ValueError(f"species {i} outside 1..{sys.nspec} of this physics")
+        if bs[i - 1].any():
+            raise ValueError(f"species {i} is already a boundary species")
+        for r in regs:
+            if not 1 <= int(r) <= rs.shape[1]:
+                raise ValueError(f"cell region {r} outside 1..{rs.shape[1]}")
+            rs[i - 1, int(r) - 1] = 1
+    return sys
+
+
+def enable_boundary_species(sys: System, ispec: int, bregions):
+    """enable_boundary_species!(system, ispec, bregions) (src/vfvm_system.jl:483-513):
+    add species ``ispec`` to the boundary regions ``bregions`` (1-based)."""
+    rs, bs = _species_tables(sys)
+    i = int(ispec)
+    if not 1 <= i <= sys.nspec:
+        raise ValueError(f"species {i} outside 1..{sys.nspec} of this physics")
+    if rs[i - 1].any():
+        raise ValueError(f"species {i} is already a bulk species")
+    for r in bregions:
+        if not 1 <= int(r) <= bs.shape[1]:
+            raise ValueError(f"boundary region {r} outside 1..{bs.shape[1]}")
+        bs[i - 1, int(r) - 1] = 1
+    return sys
+
+
+def node_species(sys: System) -> np.ndarray:
+    """Boolean (nspec, nnodes): whether node K carries species i -- the
+    reference's node_dof (isnodespecies, src/vfvm_system.jl:765)."""
+    g = sys.grid
+    out = np.zeros((sys.nspec, g.nnodes), dtype=bool)
+    if sys.region_species is None:
+        out[...] = True
+        return out
+    rs, bs = sys.region_species != 0, sys.bregion_species != 0
+    for r in range(rs.shape[1]):
+        nodes = np.unique(g.cellnodes[:, g.cellregions == r + 1])
+        out[np.ix_(rs[:, r], nodes)] = True
+    for r in range(bs.shape[1]):
+        nodes = np.unique(g.bfacenodes[:, g.bfaceregions == r + 1])
+        out[np.ix_(bs[:, r], nodes)] = True
+    return out
+
+
+def _sparse_view(sys: System, U: np.ndarray) -> np.ndarray:
+    """A solution as the reference's sparse storage reads it: 0 on the dofs
+    a node does not carry."""
+    if sys.unknown_storage == "sparse" and sys.region_species is not None:
+        U = np.array(U, order="F")
+        U[~node_species(sys)] = 0.0
+    return U
+
+
 def unknowns(sys: System, inival=0.0) -> np.ndarray:
     """Dense solution array (nspec, nnodes), Fortran order."""
     U = np.empty((sys.nspec, sys.nnodes), order="F")
@@ -405,6 +510,10 @@ def evaluate_residual_and_jacobian(sys: System, u, t: float = 0.0, tstep: float 
     vals = np.zeros(ci.size)
     _raise(lib.vfvm_assemble(h, L.ptr(U), L.ptr(Uo), t, tstep, embed, L.ptr(F), L.ptr(vals)))
     J = sp.csr_matrix((vals, ci, rp), shape=(sys.ndofs, sys.ndofs))
+    if sys.unknown_storage == "sparse" and sys.region_species is not None:
+        # the carried dofs only (node-major, species ascending: the sparse dof order)
+        act = np.flatnonzero(node_species(sys).ravel(order="F"))
+        return F[act], J[act][:, act].tocsr()
     return _shape(F, sys), J
 
 
@@ -473,12 +582,13 @@ def solve(sys: System, inival=0.0, control: Optional[SolverControl] = None, time
             solve.last_host_syncs = None
             _raise(rc, "vfvm_evolve")
         n = nst.value
-        return TransientSolution(tst[:n].tolist(), [_shape(store[i].copy(), sys) for i in range(n)],
+        return TransientSolution(tst[:n].tolist(),
+                                 [_sparse_view(sys, _shape(store[i].copy(), sys)) for i in range(n)],
                                  NewtonSolverHistory.from_c(hist))
     U = np.zeros(sys.ndofs)
     rc = lib.vfvm_solve(h, ctypes.byref(c), L.ptr(U0), L.ptr(U), time, tstep, 0.0, ctypes.byref(hist))
     _raise(rc, "vfvm_solve")
-    out = _shape(U, sys)
+    out = _sparse_view(sys, _shape(U, sys))
     solve.last_history = NewtonSolverHistory.from_c(hist)
     return out
 
