@@ -81,6 +81,10 @@ extern "C" {
 #define VFVM_PHYS_JOULE_HEAT 19       /* potential phi and temperature T with Joule heating as an edge
                                          reaction (the callbacks of examples/Example206_JouleHeat.jl);
                                          params: kappa0, alpha, T0, lambda, c */
+#define VFVM_PHYS_EX161 20            /* Example161 bipolar drift-diffusion in quasi-Fermi potentials (phi_n,
+                                         phi_p, psi), doping per cell region 1/2/3, bias ramp in time on
+                                         boundary region 2; params: Cn, Cp, Ca, En, Ep, mu_n, mu_p, lambda,
+                                         tPrecond, tRamp, tExt, Vprecond, VExt, DirichletVal */
 
 /* linear solver / preconditioner / precision selectors */
 #define VFVM_KRYLOV_BICGSTAB 0

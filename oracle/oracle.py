@@ -42,6 +42,7 @@ PHYS = {
     "ex105": 1, "ex106": 2, "ex110": 3, "ex160": 4, "ex207": 5, "ex301": 6, "ex440": 7,
     "laplace_dirichlet": 8, "nlpoisson": 11, "porous": 12, "bipolar": 13, "rd2": 14,
     "kappa_exp": 15, "surface_heat": 16, "boundary_species": 17, "edge_reaction": 18, "joule_heat": 19,
+    "ex161": 20, "testfunction": 21,
 }
 
 
@@ -78,6 +79,7 @@ def lib():
         L.oracle_csr.argtypes = [ctypes.c_void_p, P(i64), P(i32), P(d)]
         L.oracle_csr.restype = i64
         L.oracle_init_dirichlet.argtypes = [ctypes.c_void_p, P(d), d, d]
+        L.oracle_integrate.argtypes = [ctypes.c_void_p, P(d), P(d), P(d), P(d)]
         L.oracle_cellfactors.argtypes = [i32, P(d), P(i32), P(d), P(d)]
         L.oracle_bfacefactors_raw.argtypes = [i32, P(d), P(i32), P(d), P(d)]
         L.oracle_fbernoulli_pm.argtypes = [P(d), P(d), P(d), i64]
@@ -234,6 +236,25 @@ class OracleSystem:
         J = sp.csr_matrix((vv, ci, rp), shape=(self.n, self.n))
         return F, J
 
+    def integrate(self, T, U, Uold=None, tstep=None):
+        """Test-function integrals (src/vfvm_testfunctions.jl:125-380) of the
+        flat solution U with test function T: a dict of per-species arrays
+        flux, react, src, stor, oldstor, erea, and ``steady`` = flux + react -
+        src + erea (integrate(system, T, U)) or, with Uold and tstep, that plus
+        (stor - oldstor) / tstep (the implicit Euler step form)."""
+        U = np.ascontiguousarray(U, dtype=np.float64).ravel()
+        Uo = U if Uold is None else np.ascontiguousarray(Uold, dtype=np.float64).ravel()
+        T = np.ascontiguousarray(T, dtype=np.float64).ravel()
+        out = np.zeros(6 * self.nspec)
+        lib().oracle_integrate(self.h, _p(T, ctypes.c_double), _p(U, ctypes.c_double), _p(Uo, ctypes.c_double),
+                               _p(out, ctypes.c_double))
+        parts = dict(zip(("flux", "react", "src", "stor", "oldstor", "erea"), out.reshape(6, self.nspec)))
+        I = parts["flux"] + parts["react"] - parts["src"]
+        if Uold is not None and tstep is not None:
+            I = I + (parts["stor"] - parts["oldstor"]) / tstep
+        parts["steady" if tstep is None else "step"] = I + parts["erea"]
+        return parts
+
     def init_dirichlet(self, U, time=0.0, embed=0.0):
         lib().oracle_init_dirichlet(self.h, _p(U, ctypes.c_double), time, embed)
         return U
@@ -244,6 +265,23 @@ class OracleSystem:
         x = spla.splu(J.tocsc()).solve(F)
         self.tlin += _time.perf_counter() - t0
         return x
+
+
+def testfunction(grid, bc0, bc1, assembly="edgewise"):
+    """testfunction(TestFunctionFactory(system), bc0, bc1),
+    src/vfvm_testfunctions.jl:38-108: the Laplace system of the factory with
+    Dirichlet value -1 on the regions bc1 and 0 on bc0, its residual and matrix
+    at 0, T = matrix \\ residual (T = 1 on bc1, 0 on bc0)."""
+    nb = int(np.max(grid.bfaceregions))
+    bf = np.zeros((1, nb))
+    bv = np.zeros((1, nb))
+    for r in bc1:
+        bf[0, r - 1], bv[0, r - 1] = 1.0e30, -1.0
+    for r in bc0:
+        bf[0, r - 1], bv[0, r - 1] = 1.0e30, 0.0
+    tsys = OracleSystem(grid, "testfunction", [], bfactors=bf, bvalues=bv, assembly=assembly)
+    F, J = tsys.assemble(np.zeros(grid.nnodes), tstep=math.inf)
+    return spla.splu(J.tocsc()).solve(F)
 
 
 class NewtonHistory:

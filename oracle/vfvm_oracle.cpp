@@ -451,6 +451,73 @@ struct PhysJouleHeat : OBase {
   }
 };
 
+// examples/Example161_BipolarDriftDiffusionCurrent.jl:85-151: quasi-Fermi
+// potentials phi_n, phi_p and the electrostatic potential psi (species 1-3),
+// densities n = exp(zn (phi_n - psi + En)), p = exp(zp (phi_p - psi + Ep)) with
+// zn = -1, zp = 1; doping Cn / Ca / -Cp in cell regions 1 / 2 / 3; Scharfetter-
+// Gummel fluxes through fbernoulli_pm; the bias scanProtocol(t) (:54-66) on
+// boundary region 2.
+// params: Cn, Cp, Ca, En, Ep, mun, mup, lambda, tPrecond, tRamp, tExt, Vprecond, VExt, DirichletVal
+struct PhysEx161 : OBase {
+  static const int NS = 3;
+  static const bool has_reaction = true, has_storage = true, has_source = false, has_breaction = true;
+  double Cn, Cp, Ca, En, Ep, mun, mup, lambda, tPrecond, tRamp, tExt, Vprecond, VExt, DirichletVal;
+  static constexpr double zn = -1.0, zp = 1.0;
+  double scan(double t) const {
+    const double tEnd = tPrecond + tRamp + tExt;
+    if (0.0 <= t && t <= tPrecond) return Vprecond;
+    if (tPrecond <= t && t <= tPrecond + tRamp) return Vprecond - (Vprecond - VExt) / tRamp * (t - tPrecond);
+    if (tPrecond + tRamp <= t && t <= tEnd) return VExt;
+    return 0.0;
+  }
+  template <class T> void reaction(T* f, const T* u, const NodeInfo& n) const {
+    T nn = exp(zn * (u[0] - u[2] + En));
+    T np = exp(zp * (u[1] - u[2] + Ep));
+    double C = n.region == 1 ? Cn : (n.region == 2 ? Ca : (n.region == 3 ? -Cp : 0.0));
+    f[2] = -(C + zn * nn + zp * np);
+    const double r0 = 1.0;
+    T recomb = (r0 + 1.0 / (nn + np)) * (nn * np * (1.0 - exp(u[0] - u[1])));
+    f[0] = zn * recomb;
+    f[1] = zp * recomb;
+  }
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
+    f[2] = -(lambda * lambda) * (uL[2] - uK[2]);
+    T bp, bm;
+    fbernoulli_pm(-(uL[2] - uK[2]), bp, bm);
+    T nn1 = exp(zn * (uK[0] - uK[2] + En)), np1 = exp(zp * (uK[1] - uK[2] + Ep));
+    T nn2 = exp(zn * (uL[0] - uL[2] + En)), np2 = exp(zp * (uL[1] - uL[2] + Ep));
+    f[0] = -zn * mun * (bm * nn2 - bp * nn1);
+    f[1] = -zp * mup * (bp * np2 - bm * np1);
+  }
+  template <class T> void storage(T* f, const T* u, const NodeInfo&) const {
+    f[0] = zn * exp(zn * (u[0] - u[2] + En));
+    f[1] = zp * exp(zp * (u[1] - u[2] + Ep));
+  }
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const {
+    const double s = scan(b.time);
+    boundary_dirichlet(f, u, b, 0, 1, 0.0);
+    boundary_dirichlet(f, u, b, 1, 1, 0.0);
+    boundary_dirichlet(f, u, b, 2, 1, 0.5 * (En + Ep) + std::asinh(Cn / (2 * std::sqrt(std::exp(-(En - Ep))))));
+    boundary_dirichlet(f, u, b, 0, 2, DirichletVal + s);
+    boundary_dirichlet(f, u, b, 1, 2, DirichletVal + s);
+    boundary_dirichlet(f, u, b, 2, 2,
+                       0.5 * (En + Ep) + std::asinh(-Cp / (2 * std::sqrt(std::exp(-(En - Ep))))) + DirichletVal + s);
+  }
+};
+
+// The physics of TestFunctionFactory (src/vfvm_testfunctions.jl:38-50): flux
+// u_K - u_L, storage u; Dirichlet data through the legacy boundary factors.
+struct PhysTestFunction : OBase {
+  static const int NS = 1;
+  static const bool has_reaction = false, has_storage = true, has_source = false, has_breaction = false;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = uK[0] - uL[0]; }
+  template <class T> void storage(T* f, const T* u, const NodeInfo&) const { f[0] = u[0]; }
+  template <class T> void reaction(T*, const T*, const NodeInfo&) const {}
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
+};
+
 // ---------------------------------------------------------------- system
 struct Oracle {
   int dim = 0, N = 0, ncells = 0, nbf = 0, ns = 1, phys = 0, nregions = 1, nbregions = 0, nnd = 0;
@@ -880,6 +947,69 @@ void init_dirichlet_t(Oracle& o, const P& ph, double* U, double time, double lam
         if (!((o.node_spec[K] >> i) & 1u)) U[K * NS + i] = 0.0;
 }
 
+// Test-function integrals (src/vfvm_testfunctions.jl:210-380): per species
+// out[0] I_flux = sum fac flux(U) (T_K - T_L) over edge items, out[1] I_react =
+// sum fac reaction(U) T_K and out[2] I_src = sum fac source T_K over node
+// items, out[3] / out[4] the storage of U / Uold, out[5] the edge reaction
+// with T_K + T_L.  Items as in the assembly mode (edgewise: per node/edge and
+// region; cellwise: per cell).
+template <class P>
+void integrate_t(Oracle& o, const P& ph, const double* T, const double* U, const double* Uold, double* out) {
+  const int NS = P::NS, d = o.dim;
+  for (int k = 0; k < 6 * NS; ++k) out[k] = 0.0;
+  const double* nd = o.ndata.empty() ? nullptr : o.ndata.data();
+  auto node_item = [&](int K, int reg, double fac) {
+    NodeInfo ni{K, reg, &o.coord[d * K], 0.0, 1.0, nd ? nd + (size_t)o.nnd * K : nullptr};
+    double y[NS], u[NS], uo[NS];
+    for (int i = 0; i < NS; ++i) { u[i] = U[K * NS + i]; uo[i] = Uold[K * NS + i]; }
+    for (int i = 0; i < NS; ++i) y[i] = 0.0;
+    if (P::has_reaction) ph.reaction(y, u, ni);
+    for (int i = 0; i < NS; ++i) out[1 * NS + i] += fac * y[i] * T[K];
+    for (int i = 0; i < NS; ++i) y[i] = 0.0;
+    if (P::has_source) ph.source(y, ni);
+    for (int i = 0; i < NS; ++i) out[2 * NS + i] += fac * y[i] * T[K];
+    for (int i = 0; i < NS; ++i) y[i] = 0.0;
+    if (P::has_storage) ph.storage(y, u, ni);
+    for (int i = 0; i < NS; ++i) out[3 * NS + i] += fac * y[i] * T[K];
+    for (int i = 0; i < NS; ++i) y[i] = 0.0;
+    if (P::has_storage) ph.storage(y, uo, ni);
+    for (int i = 0; i < NS; ++i) out[4 * NS + i] += fac * y[i] * T[K];
+  };
+  auto edge_item = [&](int K, int L, int reg, double fac) {
+    EdgeInfo ei{K, L, reg, &o.coord[d * K], &o.coord[d * L], 0.0, 1.0,
+                nd ? nd + (size_t)o.nnd * K : nullptr, nd ? nd + (size_t)o.nnd * L : nullptr};
+    double y[NS], uK[NS], uL[NS];
+    for (int i = 0; i < NS; ++i) { uK[i] = U[K * NS + i]; uL[i] = U[L * NS + i]; y[i] = 0.0; }
+    ph.flux(y, uK, uL, ei);
+    for (int i = 0; i < NS; ++i) out[0 * NS + i] += fac * y[i] * (T[K] - T[L]);
+    if (P::has_edgereaction) {
+      for (int i = 0; i < NS; ++i) y[i] = 0.0;
+      ph.edgereaction(y, uK, uL, ei);
+      for (int i = 0; i < NS; ++i) out[5 * NS + i] += fac * y[i] * (T[K] + T[L]);
+    }
+  };
+  if (!o.cellwise) {
+    for (int K = 0; K < o.N; ++K)
+      for (auto& rf : o.nodefac[K]) node_item(K, rf.first, rf.second);
+    for (int e = 0; e < o.E; ++e)
+      for (auto& rf : o.edgefac[e]) edge_item(o.edgenodes[2 * e], o.edgenodes[2 * e + 1], rf.first, rf.second);
+  } else {
+    const int nnc = d + 1, nen = d == 1 ? 1 : (d == 2 ? 3 : 6);
+    double npar[4], epar[6];
+    for (int c = 0; c < o.ncells; ++c) {
+      cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+      for (int i = 0; i < nnc; ++i) node_item(o.cellnodes[i + nnc * c], o.cellregions[c], npar[i]);
+    }
+    for (int c = 0; c < o.ncells; ++c) {
+      cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+      for (int i = 0; i < nen; ++i) {
+        const int e = o.celledges[i + nen * c];
+        edge_item(o.edgenodes[2 * e], o.edgenodes[2 * e + 1], o.cellregions[c], epar[i]);
+      }
+    }
+  }
+}
+
 template <class F>
 int dispatch(const Oracle& o, F&& fn) {
   const double* p = o.params.data();
@@ -899,6 +1029,14 @@ int dispatch(const Oracle& o, F&& fn) {
     case 14: { PhysRD2 ph; ph.D1 = P(0); ph.D2 = P(1); ph.k = P(2); return fn(ph); }
     case 15: { PhysKappaExp ph; ph.fsrc = P(0); return fn(ph); }
     case 16: { PhysSurfaceHeat ph; ph.eps = P(0); ph.eps_s = P(1); ph.c_s = P(2); ph.k = P(3); ph.q0 = P(4); ph.breg = (int)P(5); return fn(ph); }
+    case 20: {
+      PhysEx161 ph;
+      ph.Cn = P(0); ph.Cp = P(1); ph.Ca = P(2); ph.En = P(3); ph.Ep = P(4); ph.mun = P(5); ph.mup = P(6);
+      ph.lambda = P(7); ph.tPrecond = P(8); ph.tRamp = P(9); ph.tExt = P(10); ph.Vprecond = P(11); ph.VExt = P(12);
+      ph.DirichletVal = P(13);
+      return fn(ph);
+    }
+    case 21: { PhysTestFunction ph; return fn(ph); }
     case 18: { PhysEdgeReaction ph; ph.mode = (int)P(0); ph.dim = (int)P(1); return fn(ph); }
     case 19: { PhysJouleHeat ph; ph.kappa0 = P(0); ph.alpha = P(1); ph.T0 = P(2); ph.lam = P(3); ph.c = P(4); return fn(ph); }
     case 17: { PhysBoundarySpecies ph; ph.d = P(0); ph.k = P(1); ph.c = P(2); ph.db = P(3); ph.kmax = P(4); ph.cmax = P(5); ph.breg = (int)P(6); return fn(ph); }
@@ -909,8 +1047,8 @@ int dispatch(const Oracle& o, F&& fn) {
 int nspec_of(int phys) {
   switch (phys) {
     case 3: case 4: case 14: case 17: case 19: return 2;
-    case 13: return 3;
-    case 1: case 2: case 5: case 6: case 7: case 8: case 11: case 12: case 15: case 16: case 18: return 1;
+    case 13: case 20: return 3;
+    case 1: case 2: case 5: case 6: case 7: case 8: case 11: case 12: case 15: case 16: case 18: case 21: return 1;
   }
   return 0;
 }
@@ -1028,6 +1166,13 @@ int64_t oracle_csr(void* h, int64_t* rowptr, int* colind, double* vals) {
     if (rowptr) rowptr[i + 1] = k;
   }
   return k;
+}
+
+// Test-function integrals of U (Uold for the old storage): out = 6 x nspec,
+// see integrate_t
+void oracle_integrate(void* h, const double* T, const double* U, const double* Uold, double* out) {
+  Oracle* o = static_cast<Oracle*>(h);
+  dispatch(*o, [&](const auto& ph) { integrate_t(*o, ph, T, U, Uold ? Uold : U, out); return 0; });
 }
 
 void oracle_init_dirichlet(void* h, double* U, double time, double lambda) {

@@ -28,6 +28,7 @@ EXAMPLES = {
     "Example106_NonlinearDiffusion1D": r"testval\s*=\s*([-0-9.e]+)",
     "Example110_ReactionDiffusion1D_TwoSpecies": r"testval\s*=\s*([-0-9.e]+)",
     "Example160_UnipolarDriftDiffusion1D": r"evolval\s*=\s*([-0-9.e]+)",
+    "Example161_BipolarDriftDiffusionCurrent": r"testval\s*=\s*([-0-9.e]+)",
     "Example207_NonlinearPoisson2D": r"testval\s*=\s*([-0-9.e]+)",
     "Example301_Laplace3D": r"testval\s*=\s*([-0-9.e]+)",
     "Example440_ParallelState": r"testval\s*=\s*([-0-9.e]+)",

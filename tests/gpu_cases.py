@@ -68,6 +68,10 @@ def case(vfvm, name, seed=0):
         g, kind, params = sg(lin(3), lin(3), lin(3)), "edge_reaction", [2, 3]
     elif name == "joule_heat":  # Example206's callbacks on a 3 x 1 rectangle
         g, kind, params = sg(3 * lin(12), lin(4)), "joule_heat", [1.0, 1.0, 0.5, 1.0, 1.0]
+    elif name == "ex161":  # Example161: three cell regions, bias ramp in time (mid-ramp here)
+        import ex161_case
+        g, kind, params = ex161_case.grid(vfvm), "ex161", ex161_case.PARAMS
+        t, tstep = ex161_case.T_PRECOND + 0.5 * ex161_case.T_RAMP, 1e-6
     elif name == "laplace_dirichlet":
         g, kind, params = sg(lin(9)), "laplace_dirichlet", []
     else:
@@ -90,4 +94,4 @@ def random_state(c, nspec, rng):
 
 NAMES = ["nlpoisson", "porous", "bipolar", "rd2", "kappa_exp", "ex105", "ex106", "ex110", "ex160", "ex207",
          "ex301", "ex440", "laplace_dirichlet", "kappa_unstructured", "surface_heat2d", "surface_heat3d",
-         "edge_reaction2d", "edge_reaction3d", "joule_heat"]
+         "edge_reaction2d", "edge_reaction3d", "joule_heat", "ex161"]

@@ -133,3 +133,27 @@ def test_cachesol_linear_exact(oracle, grid):
     F, J = s.assemble(np.zeros(10))
     x = s.linsolve(J, -F)
     assert np.max(np.abs(x - X)) <= 1e-15
+
+
+@pytest.mark.parametrize("assembly", ["edgewise", "cellwise"])
+def test_example161_current(vfvm, oracle, testvals, assembly):
+    """Example161: bipolar drift-diffusion in three cell regions, three adaptive
+    transient phases, test-function current integrals (runtests :296-303)."""
+    import ex161_case as E
+    g = E.grid(vfvm)
+    osys = oracle.OracleSystem(g, "ex161", E.PARAMS, assembly=assembly)
+    c = oracle.Control()
+    c.Δu_opt = math.inf
+    base, phases = E.control_fields()
+    for k, v in base.items():
+        setattr(c, k, v)
+    u = E.inival(E.coords()).ravel(order="F")
+    for (t0, t1), fields in phases:
+        for k, v in fields.items():
+            setattr(c, k, v)
+        times, sols, _ = oracle.solve_transient(osys, u, [t0, t1], c)
+        u = sols[-1]
+    tf = oracle.testfunction(g, [1], [2], assembly=assembly)
+    assert len(times) == 119
+    ref = testvals["Example161_BipolarDriftDiffusionCurrent"]["value"]
+    assert E.current_sum(osys, tf, times, sols) == pytest.approx(ref, rel=RTOL)

@@ -145,6 +145,15 @@ template <int N, typename P> VFVM_HD Dual<N, P> operator/(const Dual<N, P>& a, d
   for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * ib;
   return r;
 }
+template <int N, typename P> VFVM_HD Dual<N, P> operator/(double a, const Dual<N, P>& b) {
+  Dual<N, P> r; r.v = a / b.v;
+  P ib, q;
+  if constexpr (kShadow<P>) { ib = P(1) / b.s; q = P(a) * ib; r.s = q; }
+  else { ib = 1.0 / b.v; q = r.v; r.s = r.v; }
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = (-q * b.d[i]) * ib;
+  return r;
+}
 // chain rule helper: r = f(a) with FP64 value fv and, in the partials'
 // precision, value fs and derivative dfs
 template <int N, typename P> VFVM_HD Dual<N, P> chain(const Dual<N, P>& a, double fv, P fs, P dfs) {
@@ -189,6 +198,12 @@ template <int N, typename P> VFVM_HD Dual<N, P> dmax(const Dual<N, P>& a, double
 VFVM_HD double sq(double a) { return a * a; }
 VFVM_HD double cube(double a) { return a * a * a; }
 VFVM_HD double dmax(double a, double b) { return a > b ? a : b; }
+// exp for physics callbacks that run on doubles as well as on duals (storage
+// is evaluated at the old values in plain doubles); a name of its own, since
+// plain-double overloads of exp in this namespace would collide with the
+// global ones where the namespace is imported
+VFVM_HD double vexp(double a) { return ::exp(a); }
+template <int N, typename P> VFVM_HD Dual<N, P> vexp(const Dual<N, P>& a) { return exp(a); }
 
 // -----------------------------------------------------------------------------
 // Bernoulli function B(x) = x/(exp(x)-1) and B(-x), with the reference's

@@ -385,6 +385,63 @@ struct PhysJouleHeat : PhysBase {
   }
 };
 
+// examples/Example161_BipolarDriftDiffusionCurrent.jl:85-151: quasi-Fermi
+// potentials phi_n, phi_p and the electrostatic potential psi (species 1-3),
+// densities n = exp(zn (phi_n - psi + En)), p = exp(zp (phi_p - psi + Ep)),
+// zn = -1, zp = 1; doping Cn / Ca / -Cp in cell regions 1 / 2 / 3;
+// Scharfetter-Gummel fluxes through fbernoulli_pm; recombination
+// (1 + 1/(n+p)) n p (1 - exp(phi_n - phi_p)); Dirichlet values on boundary
+// regions 1 and 2, the latter shifted by the bias scanProtocol(t) (:54-66).
+// params: Cn, Cp, Ca, En, Ep, mu_n, mu_p, lambda, tPrecond, tRamp, tExt, Vprecond, VExt, DirichletVal
+struct PhysEx161 : PhysBase {
+  static constexpr int NS = 3;
+  static constexpr bool has_reaction = true, has_storage = true, has_breaction = true;
+  double Cn, Cp, Ca, En, Ep, mun, mup, lambda, tPrecond, tRamp, tExt, Vprecond, VExt, DirichletVal;
+  static constexpr double zn = -1.0, zp = 1.0;
+  VFVM_HD void load(const double* p) {
+    Cn = p[0]; Cp = p[1]; Ca = p[2]; En = p[3]; Ep = p[4]; mun = p[5]; mup = p[6]; lambda = p[7];
+    tPrecond = p[8]; tRamp = p[9]; tExt = p[10]; Vprecond = p[11]; VExt = p[12]; DirichletVal = p[13];
+  }
+  VFVM_HD double scan(double t) const {
+    const double tEnd = tPrecond + tRamp + tExt;
+    if (0.0 <= t && t <= tPrecond) return Vprecond;
+    if (tPrecond <= t && t <= tPrecond + tRamp) return Vprecond - (Vprecond - VExt) / tRamp * (t - tPrecond);
+    if (tPrecond + tRamp <= t && t <= tEnd) return VExt;
+    return 0.0;
+  }
+  template <class T> VFVM_HD void reaction(T* f, const T* u, const NodeItem& n) const {
+    const T nn = vexp(zn * (u[0] - u[2] + En));
+    const T np = vexp(zp * (u[1] - u[2] + Ep));
+    const double C = n.region == 1 ? Cn : (n.region == 2 ? Ca : (n.region == 3 ? -Cp : 0.0));
+    f[2] = -(C + zn * nn + zp * np);
+    const T recomb = (1.0 + 1.0 / (nn + np)) * (nn * np * (1.0 - vexp(u[0] - u[1])));
+    f[0] = zn * recomb;
+    f[1] = zp * recomb;
+  }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const {
+    f[2] = -(lambda * lambda) * (uL[2] - uK[2]);
+    T bp, bm;
+    fbernoulli_pm(-(uL[2] - uK[2]), bp, bm);
+    const T nn1 = vexp(zn * (uK[0] - uK[2] + En)), np1 = vexp(zp * (uK[1] - uK[2] + Ep));
+    const T nn2 = vexp(zn * (uL[0] - uL[2] + En)), np2 = vexp(zp * (uL[1] - uL[2] + Ep));
+    f[0] = -zn * mun * (bm * nn2 - bp * nn1);
+    f[1] = -zp * mup * (bp * np2 - bm * np1);
+  }
+  template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const {
+    f[0] = zn * vexp(zn * (u[0] - u[2] + En));
+    f[1] = zp * vexp(zp * (u[1] - u[2] + Ep));
+  }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const {
+    const double s = scan(b.time);
+    boundary_dirichlet(f, u, b, 0, 1, 0.0);
+    boundary_dirichlet(f, u, b, 1, 1, 0.0);
+    boundary_dirichlet(f, u, b, 2, 1, 0.5 * (En + Ep) + asinh(Cn / (2 * sqrt(::exp(-(En - Ep))))));
+    boundary_dirichlet(f, u, b, 0, 2, DirichletVal + s);
+    boundary_dirichlet(f, u, b, 1, 2, DirichletVal + s);
+    boundary_dirichlet(f, u, b, 2, 2, 0.5 * (En + Ep) + asinh(-Cp / (2 * sqrt(::exp(-(En - Ep))))) + DirichletVal + s);
+  }
+};
+
 inline int physics_nspec(int id) {
   switch (id) {
     case VFVM_PHYS_EX105: case VFVM_PHYS_EX106: case VFVM_PHYS_EX207: case VFVM_PHYS_EX301:
@@ -393,7 +450,7 @@ inline int physics_nspec(int id) {
     case VFVM_PHYS_EDGE_REACTION: return 1;
     case VFVM_PHYS_EX110: case VFVM_PHYS_EX160: case VFVM_PHYS_RD2: case VFVM_PHYS_BOUNDARY_SPECIES:
     case VFVM_PHYS_JOULE_HEAT: return 2;
-    case VFVM_PHYS_BIPOLAR: return 3;
+    case VFVM_PHYS_BIPOLAR: case VFVM_PHYS_EX161: return 3;
   }
   return 0;
 }
@@ -408,6 +465,7 @@ inline int physics_nparams(int id) {
     case VFVM_PHYS_BOUNDARY_SPECIES: return 7;
     case VFVM_PHYS_EDGE_REACTION: return 2;
     case VFVM_PHYS_JOULE_HEAT: return 5;
+    case VFVM_PHYS_EX161: return 14;
   }
   return 0;
 }
@@ -434,6 +492,7 @@ int dispatch_physics(int id, Fn&& fn) {
     case VFVM_PHYS_BOUNDARY_SPECIES: return fn(PhysBoundarySpecies{});
     case VFVM_PHYS_EDGE_REACTION: return fn(PhysEdgeReaction{});
     case VFVM_PHYS_JOULE_HEAT: return fn(PhysJouleHeat{});
+    case VFVM_PHYS_EX161: return fn(PhysEx161{});
   }
   return VFVM_ERR_INPUT;
 }
