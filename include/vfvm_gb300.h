@@ -85,6 +85,8 @@ extern "C" {
                                          phi_p, psi), doping per cell region 1/2/3, bias ramp in time on
                                          boundary region 2; params: Cn, Cp, Ca, En, Ep, mu_n, mu_p, lambda,
                                          tPrecond, tRamp, tExt, Vprecond, VExt, DirichletVal */
+#define VFVM_PHYS_TESTFUNCTION 21     /* the Laplace system of TestFunctionFactory (flux u_K - u_L, storage u);
+                                         Dirichlet values through the legacy boundary data */
 
 /* linear solver / preconditioner / precision selectors */
 #define VFVM_KRYLOV_BICGSTAB 0
@@ -201,6 +203,23 @@ void vfvm_control_default(vfvm_control* c);
  * pattern, work buffers.  Returns NULL on failure with *status set. */
 vfvm_ctx* vfvm_create(const vfvm_grid* grid, const vfvm_physics_desc* phys, int* status);
 void vfvm_destroy(vfvm_ctx* ctx);
+
+/* Test-function integrals (integrate(system, T, U) and its implicit Euler form,
+ * src/vfvm_testfunctions.jl:125-380) of host arrays T (nnodes), U and Uold
+ * (nspec x nnodes; Uold NULL: U), physics evaluated at (time, lambda) (the
+ * reference uses 0 and 1).  out = 6 x nspec, per species: the flux term
+ * sum fac flux (T_K - T_L), the reaction, source, storage(U) and storage(Uold)
+ * terms sum fac f T_K, and the edge-reaction term sum fac r (T_K + T_L).
+ * integrate(system, T, U) = flux + reaction - source + edge reaction; the
+ * implicit Euler form adds (storage - old storage) / tstep. */
+int vfvm_integrate(vfvm_ctx* ctx, const double* T, const double* U, const double* Uold, double time, double lambda,
+                   double* out);
+
+/* The ODE/DAE form (src/vfvm_diffeq_interface.jl:10-112): the right hand side
+ * is -F and its Jacobian -J of vfvm_assemble at tstep = INFINITY; the mass
+ * matrix is the storage Jacobian at U = 0 (storage and bstorage with their
+ * node factors).  vals: its values in the scalar pattern of vfvm_pattern. */
+int vfvm_mass_matrix(vfvm_ctx* ctx, double* vals);
 
 /* sizes: out[0]=nspec, out[1]=nnodes, out[2]=nedges, out[3]=nnz of the scalar
  * pattern, out[4]=number of matrix blocks, out[5]=ncolors of the ILU0 ordering */

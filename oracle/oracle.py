@@ -80,6 +80,7 @@ def lib():
         L.oracle_csr.restype = i64
         L.oracle_init_dirichlet.argtypes = [ctypes.c_void_p, P(d), d, d]
         L.oracle_integrate.argtypes = [ctypes.c_void_p, P(d), P(d), P(d), P(d)]
+        L.oracle_mass_matrix.argtypes = [ctypes.c_void_p]
         L.oracle_cellfactors.argtypes = [i32, P(d), P(i32), P(d), P(d)]
         L.oracle_bfacefactors_raw.argtypes = [i32, P(d), P(i32), P(d), P(d)]
         L.oracle_fbernoulli_pm.argtypes = [P(d), P(d), P(d), i64]
@@ -235,6 +236,17 @@ class OracleSystem:
         self.tasm += _time.perf_counter() - t0
         J = sp.csr_matrix((vv, ci, rp), shape=(self.n, self.n))
         return F, J
+
+    def mass_matrix(self):
+        """mass_matrix(state), src/vfvm_diffeq_interface.jl:60-112, as CSR."""
+        L = lib()
+        L.oracle_mass_matrix(self.h)
+        nnz = L.oracle_csr(self.h, None, None, None)
+        rp = np.zeros(self.n + 1, dtype=np.int64)
+        ci = np.zeros(nnz, dtype=np.int32)
+        vv = np.zeros(nnz)
+        L.oracle_csr(self.h, _p(rp, ctypes.c_int64), _p(ci, ctypes.c_int), _p(vv, ctypes.c_double))
+        return sp.csr_matrix((vv, ci, rp), shape=(self.n, self.n))
 
     def integrate(self, T, U, Uold=None, tstep=None):
         """Test-function integrals (src/vfvm_testfunctions.jl:125-380) of the

@@ -1010,6 +1010,55 @@ void integrate_t(Oracle& o, const P& ph, const double* T, const double* U, const
   }
 }
 
+// mass_matrix, src/vfvm_diffeq_interface.jl:60-112: the storage Jacobian at
+// U = 0 (node items: storage with the node factor; boundary items: bstorage
+// with the boundary factor), with the species masks of assemble_res_jac.
+template <class P>
+void mass_t(Oracle& o, const P& ph) {
+  const int NS = P::NS, d = o.dim;
+  std::fill(o.vals.begin(), o.vals.end(), 0.0);
+  std::fill(o.present.begin(), o.present.end(), 0);
+  Dual<NS> u[NS], s[NS];
+  for (int i = 0; i < NS; ++i) { u[i] = mk<NS>(0.0); u[i].d[i] = 1.0; }
+  const double* nd = o.ndata.empty() ? nullptr : o.ndata.data();
+  auto node_item = [&](int K, int reg, double fac) {
+    if (!P::has_storage) return;
+    const unsigned m = o.masked ? o.reg_spec[reg - 1] : ~0u;
+    NodeInfo ni{K, reg, &o.coord[d * K], 0.0, 0.0, nd ? nd + (size_t)o.nnd * K : nullptr};
+    for (int i = 0; i < NS; ++i) s[i] = mk<NS>(0);
+    ph.storage(s, u, ni);
+    for (int i = 0; i < NS; ++i)
+      for (int j = 0; j < NS; ++j)
+        if (((m >> i) & 1u) && ((m >> j) & 1u)) addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + j, s[i].d[j], fac);
+  };
+  if (!o.cellwise) {
+    for (int K = 0; K < o.N; ++K)
+      for (auto& rf : o.nodefac[K]) node_item(K, rf.first, rf.second);
+  } else {
+    const int nnc = d + 1;
+    double npar[4], epar[6];
+    for (int c = 0; c < o.ncells; ++c) {
+      cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+      for (int i = 0; i < nnc; ++i) node_item(o.cellnodes[i + nnc * c], o.cellregions[c], npar[i]);
+    }
+  }
+  if (P::has_bstorage) {
+    const int nbn = nn_bface(d);
+    for (int b = 0; b < o.nbf; ++b)
+      for (int ib = 0; ib < nbn; ++ib) {
+        const int K = o.bfacenodes[ib + nbn * b];
+        const double fac = o.bfacenodefac[ib + nbn * b];
+        const unsigned m = o.masked ? o.node_spec[K] : ~0u;
+        BNodeInfo bi{K, o.bfaceregions[b], &o.coord[d * K], 0.0, 0.0, fac, kDirichlet, nullptr};
+        for (int i = 0; i < NS; ++i) s[i] = mk<NS>(0);
+        ph.bstorage(s, u, bi);
+        for (int i = 0; i < NS; ++i)
+          for (int j = 0; j < NS; ++j)
+            if (((m >> i) & 1u) && ((m >> j) & 1u)) addnz(o, (int64_t)K * NS + i, (int64_t)K * NS + j, s[i].d[j], fac);
+      }
+  }
+}
+
 template <class F>
 int dispatch(const Oracle& o, F&& fn) {
   const double* p = o.params.data();
@@ -1173,6 +1222,12 @@ int64_t oracle_csr(void* h, int64_t* rowptr, int* colind, double* vals) {
 void oracle_integrate(void* h, const double* T, const double* U, const double* Uold, double* out) {
   Oracle* o = static_cast<Oracle*>(h);
   dispatch(*o, [&](const auto& ph) { integrate_t(*o, ph, T, U, Uold ? Uold : U, out); return 0; });
+}
+
+// the mass matrix into the entry store (read it with oracle_csr)
+void oracle_mass_matrix(void* h) {
+  Oracle* o = static_cast<Oracle*>(h);
+  dispatch(*o, [&](const auto& ph) { mass_t(*o, ph); return 0; });
 }
 
 void oracle_init_dirichlet(void* h, double* U, double time, double lambda) {

@@ -2,8 +2,9 @@
 
 The three adaptive transient phases run through the product API (the step
 loop on the device); the test-function currents of the GPU's solutions are
-taken with the oracle's restatement of src/vfvm_testfunctions.jl (the current
-integral is post-processing outside the offloaded path).  The step times must
+taken twice: with the oracle's restatement of src/vfvm_testfunctions.jl, and
+with the device's own test function and current integrals (the whole example
+through the product API).  The step times must
 equal the oracle's and the current sum the reference's testval within its own
 tolerance (runtests :296-303, Julia's isapprox, rtol = sqrt(eps)).  Each
 Newton step solves with BiCGStab to a relative 1e-12, so the Newton iterates
@@ -54,3 +55,12 @@ def test_example161_current_gpu(vfvm, oracle, step_control):
     assert max(np.max(np.abs(a - b)) for a, b in zip(sols, osols)) <= 1e-8
     tf = oracle.testfunction(g, [1], [2])
     assert E.current_sum(osys, tf, tsol.t, sols) == pytest.approx(ref, rel=RTOL)
+    # the whole example through the product API: the device test function and currents
+    T = vfvm.testfunction(vfvm.TestFunctionFactory(sys), [1], [2])
+    total = 0.0
+    for k in range(1, len(tsol.t)):
+        dt = tsol.t[k] - tsol.t[k - 1]
+        e_new = vfvm.integrate_gradT_flux(sys, T, tsol.u[k])
+        e_old = vfvm.integrate_gradT_flux(sys, T, tsol.u[k - 1])
+        total += e_new[0] + e_new[1] + (e_new[2] - e_old[2]) / dt
+    assert total == pytest.approx(ref, rel=RTOL)

@@ -59,3 +59,12 @@ def test_checkdelaunay(oracle, vfvm):
     g.coord += 0.01 * (rng.random(g.coord.shape) - 0.5)
     _, ef, _ = oracle.OracleSystem(g, "porous").factors()
     assert np.sum(ef < 0) > 0
+
+
+def test_oracle_mass_matrix_storage_u(vfvm, oracle):
+    """mass_matrix for storage u (porous medium): the node volumes on the diagonal."""
+    X = np.linspace(0.0, 1.0, 9)
+    g = vfvm.simplexgrid(X, X)
+    o = oracle.OracleSystem(g, "porous")
+    M = o.mass_matrix()
+    assert np.allclose(M.toarray(), np.diag(o.nodevolumes()), rtol=1e-15, atol=0)

@@ -8,7 +8,8 @@ from .grid import Grid, read_sg, simplexgrid, write_sg
 from .system import (AssemblyError, ConvergenceError, EmbeddingError, LinearSolverError, NewtonSolverHistory,
                      Physics, SolverControl, System, TransientSolution, boundary_dirichlet, edgefactors,
                      enable_boundary_species, enable_species, evaluate_residual_and_jacobian, fixed_timesteps,
-                     integrate, node_species, nodevolumes, num_species, solve, unknowns)
+                     integrate, integrate_gradT_flux, node_species, nodevolumes, num_species, solve,
+                     TestFunctionFactory, testfunction, unknowns, eval_rhs, eval_jacobian, mass_matrix)
 from . import _lib
 from .batch import BatchSolver
 from . import learned
@@ -16,6 +17,7 @@ from .build import build_library
 
 __all__ = ["Grid", "simplexgrid", "read_sg", "write_sg", "Physics", "System", "SolverControl", "NewtonSolverHistory", "TransientSolution",
            "AssemblyError", "ConvergenceError", "EmbeddingError", "LinearSolverError", "boundary_dirichlet",
-           "enable_species", "enable_boundary_species", "node_species",
+           "enable_species", "enable_boundary_species", "node_species", "TestFunctionFactory", "testfunction",
+           "integrate_gradT_flux", "eval_rhs", "eval_jacobian", "mass_matrix",
            "edgefactors", "evaluate_residual_and_jacobian", "fixed_timesteps", "integrate", "nodevolumes",
            "num_species", "solve", "unknowns", "build_library"]

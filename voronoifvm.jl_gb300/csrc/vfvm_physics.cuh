@@ -442,12 +442,23 @@ struct PhysEx161 : PhysBase {
   }
 };
 
+// The system of TestFunctionFactory (src/vfvm_testfunctions.jl:38-50): flux
+// u_K - u_L, storage u; its Dirichlet values come through the legacy
+// boundary data (T = 0 and 1 on the chosen boundary regions).
+struct PhysTestFunction : PhysBase {
+  static constexpr int NS = 1;
+  static constexpr bool has_storage = true;
+  VFVM_HD void load(const double*) {}
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const { f[0] = uK[0] - uL[0]; }
+  template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const { f[0] = u[0]; }
+};
+
 inline int physics_nspec(int id) {
   switch (id) {
     case VFVM_PHYS_EX105: case VFVM_PHYS_EX106: case VFVM_PHYS_EX207: case VFVM_PHYS_EX301:
     case VFVM_PHYS_EX440: case VFVM_PHYS_LAPLACE_DIRICHLET: case VFVM_PHYS_NLPOISSON:
     case VFVM_PHYS_POROUS: case VFVM_PHYS_KAPPA_EXP: case VFVM_PHYS_SURFACE_HEAT:
-    case VFVM_PHYS_EDGE_REACTION: return 1;
+    case VFVM_PHYS_EDGE_REACTION: case VFVM_PHYS_TESTFUNCTION: return 1;
     case VFVM_PHYS_EX110: case VFVM_PHYS_EX160: case VFVM_PHYS_RD2: case VFVM_PHYS_BOUNDARY_SPECIES:
     case VFVM_PHYS_JOULE_HEAT: return 2;
     case VFVM_PHYS_BIPOLAR: case VFVM_PHYS_EX161: return 3;
@@ -493,6 +504,7 @@ int dispatch_physics(int id, Fn&& fn) {
     case VFVM_PHYS_EDGE_REACTION: return fn(PhysEdgeReaction{});
     case VFVM_PHYS_JOULE_HEAT: return fn(PhysJouleHeat{});
     case VFVM_PHYS_EX161: return fn(PhysEx161{});
+    case VFVM_PHYS_TESTFUNCTION: return fn(PhysTestFunction{});
   }
   return VFVM_ERR_INPUT;
 }

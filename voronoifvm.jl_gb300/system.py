@@ -17,6 +17,11 @@ Names, argument meaning and error behaviour follow the reference:
 * ``evaluate_residual_and_jacobian``       -- src/vfvm_solver.jl:224-260
 * ``unknowns``, ``nodevolumes``, ``integrate`` -- dense solution layout
   (src/vfvm_densesolution.jl:11-49) and src/vfvm_postprocess.jl:18-100,397-412
+* ``eval_rhs``, ``eval_jacobian``, ``mass_matrix`` -- the ODE/DAE form,
+  src/vfvm_diffeq_interface.jl:10-112
+* ``TestFunctionFactory``, ``testfunction``, ``integrate(sys, T, U[, Uold,
+  tstep])``, ``integrate_gradT_flux`` -- test-function currents,
+  src/vfvm_testfunctions.jl:38-380
 * exceptions ``ConvergenceError``, ``AssemblyError``, ``LinearSolverError``,
   ``EmbeddingError`` -- src/vfvm_logging_exceptions.jl:6-29
 
@@ -40,7 +45,8 @@ __all__ = ["Physics", "System", "SolverControl", "NewtonSolverHistory", "Transie
            "ConvergenceError", "AssemblyError", "LinearSolverError", "EmbeddingError",
            "boundary_dirichlet", "enable_species", "enable_boundary_species", "solve", "unknowns",
            "evaluate_residual_and_jacobian", "node_species",
-           "fixed_timesteps", "nodevolumes", "integrate", "num_species"]
+           "fixed_timesteps", "nodevolumes", "integrate", "num_species", "TestFunctionFactory", "testfunction",
+           "integrate_gradT_flux", "eval_rhs", "eval_jacobian", "mass_matrix"]
 
 Dirichlet = 1.0e30  # src/vfvm_system.jl:329
 
@@ -517,6 +523,30 @@ def evaluate_residual_and_jacobian(sys: System, u, t: float = 0.0, tstep: float 
     return _shape(F, sys), J
 
 
+def eval_rhs(sys: System, u, t: float = 0.0) -> np.ndarray:
+    """eval_rhs!(du, u, state, t) (src/vfvm_diffeq_interface.jl:29-34): the ODE
+    right hand side -F(u) with the residual at tstep = Inf (the time
+    derivative is the ODE solver's), shape (nspec, nnodes)."""
+    F, _ = evaluate_residual_and_jacobian(sys, u, t=t, tstep=math.inf)
+    return -F
+
+
+def eval_jacobian(sys: System, u, t: float = 0.0):
+    """eval_jacobian!(J, u, state, t) (src/vfvm_diffeq_interface.jl:42-48): -J."""
+    _, J = evaluate_residual_and_jacobian(sys, u, t=t, tstep=math.inf)
+    return -J
+
+
+def mass_matrix(sys: System):
+    """mass_matrix(state) (src/vfvm_diffeq_interface.jl:60-112): the storage
+    Jacobian at U = 0 on the device, as a scipy CSR matrix in the scalar
+    pattern (a diagonal one for storage u)."""
+    rp, ci = sys.pattern()
+    vals = np.zeros(ci.size)
+    _raise(L.load().vfvm_mass_matrix(sys.ctx, L.ptr(vals)), "vfvm_mass_matrix")
+    return sp.csr_matrix((vals, ci, rp), shape=(sys.ndofs, sys.ndofs))
+
+
 def nodevolumes(sys: System) -> np.ndarray:
     """Voronoi node volumes (src/vfvm_postprocess.jl:397-412)."""
     nv = np.zeros(sys.nnodes)
@@ -532,11 +562,67 @@ def edgefactors(sys: System):
     return ef, en
 
 
-def integrate(sys: System, U) -> np.ndarray:
+def _tf_parts(sys: System, T, U, Uold=None):
+    """The six per-species test-function sums of vfvm_integrate, evaluated on
+    the device at time 0 and embedding 1 (as the reference's Node(system, 0, 1))."""
+    Tv = np.ascontiguousarray(np.asarray(T, dtype=np.float64).ravel())
+    if Tv.size != sys.nnodes:
+        raise ValueError("the test function needs one value per node")
+    Uf = _flat(U, sys)
+    Uo = None if Uold is None else _flat(Uold, sys)
+    out = np.zeros(6 * sys.nspec)
+    _raise(L.load().vfvm_integrate(sys.ctx, L.ptr(Tv), L.ptr(Uf), None if Uo is None else L.ptr(Uo), 0.0, 1.0,
+                                   L.ptr(out)), "vfvm_integrate")
+    return dict(zip(("flux", "react", "src", "stor", "oldstor", "erea"), out.reshape(6, sys.nspec)))
+
+
+def integrate(sys: System, U, Ustate=None, Uold=None, tstep=None) -> np.ndarray:
     """integrate(system, U): per species sum of node volume x value
-    (single cell region), src/vfvm_postprocess.jl:94-100."""
-    nv = nodevolumes(sys)
-    return _shape(_flat(U, sys), sys) @ nv
+    (single cell region), src/vfvm_postprocess.jl:94-100.
+
+    integrate(system, T, U) with a test function T (``testfunction``): the
+    steady current flux + reaction - source (+ edge reaction), and
+    integrate(system, T, U, Uold, tstep) the implicit Euler step form, which adds
+    (storage(U) - storage(Uold)) / tstep (src/vfvm_testfunctions.jl:125-205)."""
+    if Ustate is None:
+        nv = nodevolumes(sys)
+        return _shape(_flat(U, sys), sys) @ nv
+    parts = _tf_parts(sys, U, Ustate, Uold)
+    current = parts["flux"] + parts["react"] - parts["src"] + parts["erea"]
+    if Uold is not None and tstep is not None:
+        current = current + (parts["stor"] - parts["oldstor"]) / tstep
+    return current
+
+
+def integrate_gradT_flux(sys: System, T, U) -> np.ndarray:
+    """integrate_∇TxFlux(system, T, U) (src/vfvm_testfunctions.jl:283-330): per
+    species sum over the edges of fac * flux(U) * (T_first - T_second)."""
+    return _tf_parts(sys, T, U)["flux"]
+
+
+class TestFunctionFactory:
+    """TestFunctionFactory(system) (src/vfvm_testfunctions.jl:38-50): the
+    Laplace system (flux u_K - u_L, storage u) on the system's grid."""
+
+    def __init__(self, system: System, control: Optional[SolverControl] = None):
+        self.system = system
+        self.tfsystem = System(system.grid, Physics("testfunction"), is_linear=True)
+        self.control = control if control is not None else SolverControl(reltol_linear=1e-13,
+                                                                           maxiters_linear=2000)
+
+
+def testfunction(factory: TestFunctionFactory, bc0, bc1) -> np.ndarray:
+    """testfunction(factory, B_0, B_1) (src/vfvm_testfunctions.jl:53-108):
+    -Laplace T = 0 with T = 0 on the boundary regions bc0, T = 1 on bc1 and
+    no flux elsewhere, solved on the device.  Returns T (one value per node)."""
+    tf = factory.tfsystem
+    tf.boundary_factors[...] = 0.0
+    tf.boundary_values[...] = 0.0
+    for r in bc1:
+        boundary_dirichlet(tf, 1, int(r), 1.0)
+    for r in bc0:
+        boundary_dirichlet(tf, 1, int(r), 0.0)
+    return np.asarray(solve(tf, inival=0.0, control=factory.control)).ravel().copy()
 
 
 def solve(sys: System, inival=0.0, control: Optional[SolverControl] = None, times=None, embed=None,
