@@ -168,11 +168,27 @@ __device__ __forceinline__ void coarse_restrict_warps(const CoarseData& cd, cons
     float acc[NS];
 #pragma unroll
     for (int a = 0; a < NS; ++a) acc[a] = 0.f;
-    for (int q = cd.agg_ptr[I] + lane; q < cd.agg_ptr[I + 1]; q += 32) {
-      const int64_t K = cd.agg_nodes[q];
+    // four of the lane's nodes per pass, their loads issued before the sums
+    // (the lane's summation order is unchanged)
+    const int q1 = cd.agg_ptr[I + 1];
+    for (int q = cd.agg_ptr[I] + lane; q < q1; q += 4 * 32) {
+      int64_t K[4];
 #pragma unroll
-      for (int a = 0; a < NS; ++a)
-        if (!dirdof[K * NS + a]) acc[a] += float(__ldcg(&y[K * NS + a]));
+      for (int u = 0; u < 4; ++u) K[u] = q + 32 * u < q1 ? (int64_t)cd.agg_nodes[q + 32 * u] : -1;
+      float yv[4][NS];
+      uint8_t dv[4][NS];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int a = 0; a < NS; ++a) {
+          dv[u][a] = K[u] >= 0 ? dirdof[K[u] * NS + a] : (uint8_t)1;
+          yv[u][a] = K[u] >= 0 ? float(__ldcg(&y[K[u] * NS + a])) : 0.f;
+        }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int a = 0; a < NS; ++a)
+          if (!dv[u][a]) acc[a] += yv[u][a];
     }
 #pragma unroll
     for (int a = 0; a < NS; ++a)

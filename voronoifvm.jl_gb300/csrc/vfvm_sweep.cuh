@@ -505,16 +505,31 @@ __device__ __forceinline__ void sw_prolong_dot(const SweepArgs<Ph, KT>& a, const
   const int* __restrict__ agg = a.cd0.agg_of_node;
   const uint8_t* __restrict__ dd = a.dirdof;
   acc_t<KT> a0 = 0, a1 = 0;
-  for (int64_t q = u.tid(); q < a.n; q += u.nt()) {
-    KT zq = z[q];
-    const KT wq = w[q];
-    if (!dd[q]) {
-      const int64_t K = q / NS;
-      zq += KT(zcs[agg[K] * NS + (int)(q - K * NS)]);
-      z[q] = zq;
+  const int64_t st = u.nt();
+  // kVecU elements per thread and pass, all loads issued before the first use
+  // (the element order of each thread's sums is unchanged)
+  for (int64_t q = u.tid(); q < a.n; q += kVecU * st) {
+    KT zz[kVecU], ww[kVecU];
+    uint8_t dq[kVecU];
+    int ag[kVecU];
+#pragma unroll
+    for (int v = 0; v < kVecU; ++v) {
+      const int64_t e = q + v * st;
+      if (e < a.n) { zz[v] = z[e]; ww[v] = w[e]; dq[v] = dd[e]; ag[v] = agg[e / NS]; }
+      else { zz[v] = KT(0); ww[v] = KT(0); dq[v] = 1; ag[v] = 0; }
     }
-    a0 += acc_t<KT>(wq) * acc_t<KT>(zq);
-    a1 += acc_t<KT>(zq) * acc_t<KT>(zq);
+#pragma unroll
+    for (int v = 0; v < kVecU; ++v) {
+      const int64_t e = q + v * st;
+      if (e < a.n) {
+        if (!dq[v]) {
+          zz[v] += KT(zcs[ag[v] * NS + (int)(e - (e / NS) * NS)]);
+          z[e] = zz[v];
+        }
+        a0 += acc_t<KT>(ww[v]) * acc_t<KT>(zz[v]);
+        a1 += acc_t<KT>(zz[v]) * acc_t<KT>(zz[v]);
+      }
+    }
   }
   acc[0] += double(a0);
   acc[1] += double(a1);
