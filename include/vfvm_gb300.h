@@ -87,6 +87,9 @@ extern "C" {
                                          tPrecond, tRamp, tExt, Vprecond, VExt, DirichletVal */
 #define VFVM_PHYS_TESTFUNCTION 21     /* the Laplace system of TestFunctionFactory (flux u_K - u_L, storage u);
                                          Dirichlet values through the legacy boundary data */
+#define VFVM_PHYS_EX430 22            /* Example430 (runh): flux (1+p)(u_K^2 - u_L^2), reaction p u^5, u = 0 on
+                                         boundary region 1, u = p on region 3; p has parameter derivatives;
+                                         params: p */
 
 /* linear solver / preconditioner / precision selectors */
 #define VFVM_KRYLOV_BICGSTAB 0
@@ -214,6 +217,14 @@ void vfvm_destroy(vfvm_ctx* ctx);
  * implicit Euler form adds (storage - old storage) / tstep. */
 int vfvm_integrate(vfvm_ctx* ctx, const double* T, const double* U, const double* Uold, double time, double lambda,
                    double* out);
+
+/* Parameter derivatives of the residual (the reference's dudp, accumulated by
+ * asm_param in src/vfvm_assembly.jl:116-120, 194-198, 232-236, 403-405,
+ * 434-436, 497-501) at the host array U: dudp = npd x nspec x nnodes (host),
+ * the derivatives with respect to the first npd physics parameters, those the
+ * physics differentiates (*npd = 0: none; dudp may be NULL to ask for npd). */
+int vfvm_parameter_derivatives(vfvm_ctx* ctx, const double* U, double time, double tstep, double lambda,
+                               double* dudp, int32_t* npd);
 
 /* The ODE/DAE form (src/vfvm_diffeq_interface.jl:10-112): the right hand side
  * is -F and its Jacobian -J of vfvm_assemble at tstep = INFINITY; the mass

@@ -42,7 +42,7 @@ PHYS = {
     "ex105": 1, "ex106": 2, "ex110": 3, "ex160": 4, "ex207": 5, "ex301": 6, "ex440": 7,
     "laplace_dirichlet": 8, "nlpoisson": 11, "porous": 12, "bipolar": 13, "rd2": 14,
     "kappa_exp": 15, "surface_heat": 16, "boundary_species": 17, "edge_reaction": 18, "joule_heat": 19,
-    "ex161": 20, "testfunction": 21,
+    "ex161": 20, "testfunction": 21, "ex430": 22,
 }
 
 
@@ -81,6 +81,10 @@ def lib():
         L.oracle_init_dirichlet.argtypes = [ctypes.c_void_p, P(d), d, d]
         L.oracle_integrate.argtypes = [ctypes.c_void_p, P(d), P(d), P(d), P(d)]
         L.oracle_mass_matrix.argtypes = [ctypes.c_void_p]
+        L.oracle_parameter_derivatives.argtypes = [ctypes.c_void_p, P(d), d, d, d, P(d)]
+        L.oracle_parameter_derivatives.restype = i32
+        L.oracle_integrate_gradient.argtypes = [ctypes.c_void_p, P(d), P(d), i32, P(d), P(d)]
+        L.oracle_integrate_gradient.restype = i32
         L.oracle_cellfactors.argtypes = [i32, P(d), P(i32), P(d), P(d)]
         L.oracle_bfacefactors_raw.argtypes = [i32, P(d), P(i32), P(d), P(d)]
         L.oracle_fbernoulli_pm.argtypes = [P(d), P(d), P(d), i64]
@@ -236,6 +240,30 @@ class OracleSystem:
         self.tasm += _time.perf_counter() - t0
         J = sp.csr_matrix((vv, ci, rp), shape=(self.n, self.n))
         return F, J
+
+    def parameter_derivatives(self, U, time=0.0, tstep=math.inf, embed=0.0):
+        """dudp: the derivatives of the residual with respect to the physics'
+        differentiable parameters at U, shape (npd, n)."""
+        L = lib()
+        U = np.ascontiguousarray(U, dtype=np.float64).ravel()
+        npd = L.oracle_parameter_derivatives(self.h, _p(U, ctypes.c_double), time, tstep, embed, None)
+        out = np.zeros((npd, self.n))
+        if npd:
+            L.oracle_parameter_derivatives(self.h, _p(U, ctypes.c_double), time, tstep, embed,
+                                           _p(out, ctypes.c_double))
+        return out
+
+    def integrate_gradient(self, T, U, species=0):
+        """Derivatives of the steady test-function current of `species` with
+        respect to U (n values) and to the differentiable parameters."""
+        L = lib()
+        U = np.ascontiguousarray(U, dtype=np.float64).ravel()
+        T = np.ascontiguousarray(T, dtype=np.float64).ravel()
+        du = np.zeros(self.n)
+        dp = np.zeros(4)
+        npd = L.oracle_integrate_gradient(self.h, _p(T, ctypes.c_double), _p(U, ctypes.c_double), int(species),
+                                          _p(du, ctypes.c_double), _p(dp, ctypes.c_double))
+        return du, dp[:npd]
 
     def mass_matrix(self):
         """mass_matrix(state), src/vfvm_diffeq_interface.jl:60-112, as CSR."""

@@ -127,6 +127,14 @@ template <class T> inline void boundary_dirichlet(T* y, const T* u, BNodeInfo& b
     b.dirichlet_value[ispec] = v;
   }
 }
+// a Dirichlet value given by a parameter (a dual number carrying d/dp)
+template <int N> inline void boundary_dirichlet(Dual<N>* y, const Dual<N>* u, BNodeInfo& b, int ispec, int ireg,
+                                                const Dual<N>& v) {
+  if (b.region == ireg) {
+    y[ispec] = y[ispec] + b.Dirichlet * (u[ispec] - v);
+    b.dirichlet_value[ispec] = v.v;
+  }
+}
 
 // ---------------------------------------------------------------- physics
 // Physics ids follow include/vfvm_gb300.h (VFVM_PHYS_*).
@@ -503,6 +511,30 @@ struct PhysEx161 : OBase {
     boundary_dirichlet(f, u, b, 1, 2, DirichletVal + s);
     boundary_dirichlet(f, u, b, 2, 2,
                        0.5 * (En + Ep) + std::asinh(-Cp / (2 * std::sqrt(std::exp(-(En - Ep))))) + DirichletVal + s);
+  }
+};
+
+// examples/Example430_ParameterDerivativesStationary.jl:146-166 (runh, fluxh!,
+// rh!, bch!): flux (1 + p)(u_K^2 - u_L^2), reaction p u^5, u = 0 on boundary
+// region 1 and u = p on region 3, p = parameters(u)[1].  PT = double for the
+// assembly, Dual<1> (seeded) for the parameter derivatives.
+template <class PT>
+struct PhysEx430T : OBase {
+  static const int NS = 1;
+  static const bool has_reaction = true, has_storage = false, has_source = false, has_breaction = true;
+  PT p;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
+    f[0] = (1.0 + p) * (uK[0] * uK[0] - uL[0] * uL[0]);
+  }
+  template <class T> void reaction(T* f, const T* u, const NodeInfo&) const {
+    T u2 = u[0] * u[0];
+    f[0] = p * (u2 * u2 * u[0]);
+  }
+  template <class T> void storage(T*, const T*, const NodeInfo&) const {}
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const {
+    boundary_dirichlet(f, u, b, 0, 1, 0.0);
+    boundary_dirichlet(f, u, b, 0, 3, p);
   }
 };
 
@@ -1059,6 +1091,188 @@ void mass_t(Oracle& o, const P& ph) {
   }
 }
 
+// Parameter derivatives dudp (src/vfvm_assembly.jl: asm_param of the node terms
+// :116-120, edges :194-198, edge reactions :232-236, breaction :403-405, bstorage
+// :434-436, boundary edges :497-501): the unknowns as constants, the physics'
+// parameter seeded (PD: the physics with Dual<1> parameters).
+template <class PD>
+void dparams_t(Oracle& o, const PD& ph, const double* U, double time, double tstep, double lambda, double* out) {
+  const int NS = PD::NS, d = o.dim;
+  const int64_t n = (int64_t)o.N * NS;
+  std::fill(out, out + n, 0.0);
+  const double tstepinv = 1.0 / tstep;
+  const double* nd = o.ndata.empty() ? nullptr : o.ndata.data();
+  auto region_mask = [&](int reg) { return o.masked ? o.reg_spec[reg - 1] : ~0u; };
+  auto node_mask = [&](int K) { return o.masked ? o.node_spec[K] : ~0u; };
+  auto cst = [&](int K, Dual<1>* u) { for (int i = 0; i < NS; ++i) u[i] = mk<1>(U[K * NS + i]); };
+  auto node_item = [&](int K, int reg, double fac) {
+    const unsigned m = region_mask(reg);
+    NodeInfo ni{K, reg, &o.coord[d * K], time, lambda, nd ? nd + (size_t)o.nnd * K : nullptr};
+    Dual<1> u[NS], r[NS], st[NS];
+    cst(K, u);
+    for (int i = 0; i < NS; ++i) { r[i] = mk<1>(0); st[i] = mk<1>(0); }
+    if (PD::has_reaction) ph.reaction(r, u, ni);
+    if (PD::has_storage) ph.storage(st, u, ni);
+    for (int i = 0; i < NS; ++i)
+      if ((m >> i) & 1u) out[K * NS + i] += (r[i].d[0] + st[i].d[0] * tstepinv) * fac;
+  };
+  auto edge_item = [&](int K, int L, int reg, double fac, bool boundary) {
+    const unsigned m = boundary ? node_mask(K) : region_mask(reg);
+    Dual<1> uK[NS], uL[NS], f[NS];
+    cst(K, uK);
+    cst(L, uL);
+    for (int i = 0; i < NS; ++i) f[i] = mk<1>(0);
+    if (boundary) {
+      BEdgeInfo be{K, L, reg, &o.coord[d * K], &o.coord[d * L], time, lambda};
+      ph.bflux(f, uK, uL, be);
+    } else {
+      EdgeInfo ei{K, L, reg, &o.coord[d * K], &o.coord[d * L], time, lambda,
+                  nd ? nd + (size_t)o.nnd * K : nullptr, nd ? nd + (size_t)o.nnd * L : nullptr};
+      ph.flux(f, uK, uL, ei);
+    }
+    for (int i = 0; i < NS; ++i)
+      if ((m >> i) & 1u) {
+        out[K * NS + i] += fac * f[i].d[0];
+        out[L * NS + i] -= fac * f[i].d[0];
+      }
+    if (PD::has_edgereaction && !boundary) {
+      EdgeInfo ei{K, L, reg, &o.coord[d * K], &o.coord[d * L], time, lambda,
+                  nd ? nd + (size_t)o.nnd * K : nullptr, nd ? nd + (size_t)o.nnd * L : nullptr};
+      for (int i = 0; i < NS; ++i) f[i] = mk<1>(0);
+      ph.edgereaction(f, uK, uL, ei);
+      for (int i = 0; i < NS; ++i)
+        if ((m >> i) & 1u) {
+          out[K * NS + i] += fac * f[i].d[0];
+          out[L * NS + i] += fac * f[i].d[0];
+        }
+    }
+  };
+  if (!o.cellwise) {
+    for (int K = 0; K < o.N; ++K)
+      for (auto& rf : o.nodefac[K]) node_item(K, rf.first, rf.second);
+    for (int e = 0; e < o.E; ++e)
+      for (auto& rf : o.edgefac[e]) edge_item(o.edgenodes[2 * e], o.edgenodes[2 * e + 1], rf.first, rf.second, false);
+  } else {
+    const int nnc = d + 1, nen = d == 1 ? 1 : (d == 2 ? 3 : 6);
+    double npar[4], epar[6];
+    for (int c = 0; c < o.ncells; ++c) {
+      cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+      for (int i = 0; i < nnc; ++i) node_item(o.cellnodes[i + nnc * c], o.cellregions[c], npar[i]);
+    }
+    for (int c = 0; c < o.ncells; ++c) {
+      cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+      for (int i = 0; i < nen; ++i) {
+        const int e = o.celledges[i + nen * c];
+        edge_item(o.edgenodes[2 * e], o.edgenodes[2 * e + 1], o.cellregions[c], epar[i], false);
+      }
+    }
+  }
+  const int nbn = nn_bface(d);
+  for (int b = 0; b < o.nbf; ++b)
+    for (int ib = 0; ib < nbn; ++ib) {
+      const int K = o.bfacenodes[ib + nbn * b];
+      const int reg = o.bfaceregions[b];
+      const double fac = o.bfacenodefac[ib + nbn * b];
+      const unsigned m = node_mask(K);
+      double dval[NS];
+      const double Dir = (o.has_legacy && reg - 1 < o.nbregions) ? kDirichlet / fac : kDirichlet;
+      BNodeInfo bi{K, reg, &o.coord[d * K], time, lambda, fac, Dir, dval};
+      Dual<1> u[NS], y[NS], sb[NS];
+      cst(K, u);
+      for (int i = 0; i < NS; ++i) { y[i] = mk<1>(0); sb[i] = mk<1>(0); }
+      if (PD::has_breaction) ph.breaction(y, u, bi);
+      if (PD::has_bstorage) ph.bstorage(sb, u, bi);
+      for (int i = 0; i < NS; ++i)
+        if ((m >> i) & 1u) out[K * NS + i] += y[i].d[0] * fac + sb[i].d[0] * fac * tstepinv;
+    }
+  if (PD::has_bflux && d >= 2) {
+    double npar[3], epar[3];
+    const int nle = d == 2 ? 1 : 3;
+    for (int b = 0; b < o.nbf; ++b) {
+      const int* bn = &o.bfacenodes[nbn * b];
+      bfacefactors(d, o.coord.data(), bn, npar, epar);
+      for (int i = 0; i < nle; ++i) {
+        int K = d == 2 ? bn[0] : bn[tri_en[i][0]], L = d == 2 ? bn[1] : bn[tri_en[i][1]];
+        if (K > L) std::swap(K, L);
+        edge_item(K, L, o.bfaceregions[b], epar[i], true);
+      }
+    }
+  }
+}
+
+// Derivatives of the steady test-function current of species s,
+// m = sum_edges fac flux_s (T_K - T_L) + sum_nodes fac (reaction_s - source_s) T_K
+// (+ edge reaction with T_K + T_L): du = dm/dU (n values), from the node and edge
+// terms on duals.
+template <class P>
+void integrate_grad_t(Oracle& o, const P& ph, const double* T, const double* U, int s, double* du) {
+  const int NS = P::NS, d = o.dim;
+  std::fill(du, du + (int64_t)o.N * NS, 0.0);
+  const double* nd = o.ndata.empty() ? nullptr : o.ndata.data();
+  auto node_item = [&](int K, int reg, double fac) {
+    if (!P::has_reaction) return;
+    NodeInfo ni{K, reg, &o.coord[d * K], 0.0, 1.0, nd ? nd + (size_t)o.nnd * K : nullptr};
+    Dual<NS> u[NS], r[NS];
+    for (int i = 0; i < NS; ++i) { u[i] = mk<NS>(U[K * NS + i]); u[i].d[i] = 1.0; r[i] = mk<NS>(0); }
+    ph.reaction(r, u, ni);
+    for (int j = 0; j < NS; ++j) du[K * NS + j] += fac * r[s].d[j] * T[K];
+  };
+  auto edge_item = [&](int K, int L, int reg, double fac) {
+    EdgeInfo ei{K, L, reg, &o.coord[d * K], &o.coord[d * L], 0.0, 1.0,
+                nd ? nd + (size_t)o.nnd * K : nullptr, nd ? nd + (size_t)o.nnd * L : nullptr};
+    Dual<2 * NS> uK[NS], uL[NS], f[NS];
+    for (int i = 0; i < NS; ++i) {
+      uK[i] = mk<2 * NS>(U[K * NS + i]); uK[i].d[i] = 1.0;
+      uL[i] = mk<2 * NS>(U[L * NS + i]); uL[i].d[NS + i] = 1.0;
+      f[i] = mk<2 * NS>(0);
+    }
+    ph.flux(f, uK, uL, ei);
+    for (int j = 0; j < NS; ++j) {
+      du[K * NS + j] += fac * f[s].d[j] * (T[K] - T[L]);
+      du[L * NS + j] += fac * f[s].d[NS + j] * (T[K] - T[L]);
+    }
+    if (P::has_edgereaction) {
+      for (int i = 0; i < NS; ++i) f[i] = mk<2 * NS>(0);
+      ph.edgereaction(f, uK, uL, ei);
+      for (int j = 0; j < NS; ++j) {
+        du[K * NS + j] += fac * f[s].d[j] * (T[K] + T[L]);
+        du[L * NS + j] += fac * f[s].d[NS + j] * (T[K] + T[L]);
+      }
+    }
+  };
+  for (int K = 0; K < o.N; ++K)
+    for (auto& rf : o.nodefac[K]) node_item(K, rf.first, rf.second);
+  for (int e = 0; e < o.E; ++e)
+    for (auto& rf : o.edgefac[e]) edge_item(o.edgenodes[2 * e], o.edgenodes[2 * e + 1], rf.first, rf.second);
+}
+
+// d m / d p of the same current at fixed U (the physics with Dual<1> parameters)
+template <class PD>
+double integrate_dp_t(Oracle& o, const PD& ph, const double* T, const double* U, int s) {
+  const int NS = PD::NS, d = o.dim;
+  const double* nd = o.ndata.empty() ? nullptr : o.ndata.data();
+  double acc = 0.0;
+  for (int K = 0; K < o.N; ++K)
+    for (auto& rf : o.nodefac[K]) {
+      NodeInfo ni{K, rf.first, &o.coord[d * K], 0.0, 1.0, nd ? nd + (size_t)o.nnd * K : nullptr};
+      Dual<1> u[NS], r[NS];
+      for (int i = 0; i < NS; ++i) { u[i] = mk<1>(U[K * NS + i]); r[i] = mk<1>(0); }
+      if (PD::has_reaction) ph.reaction(r, u, ni);
+      acc += rf.second * r[s].d[0] * T[K];
+    }
+  for (int e = 0; e < o.E; ++e)
+    for (auto& rf : o.edgefac[e]) {
+      const int K = o.edgenodes[2 * e], L = o.edgenodes[2 * e + 1];
+      EdgeInfo ei{K, L, rf.first, &o.coord[d * K], &o.coord[d * L], 0.0, 1.0,
+                  nd ? nd + (size_t)o.nnd * K : nullptr, nd ? nd + (size_t)o.nnd * L : nullptr};
+      Dual<1> uK[NS], uL[NS], f[NS];
+      for (int i = 0; i < NS; ++i) { uK[i] = mk<1>(U[K * NS + i]); uL[i] = mk<1>(U[L * NS + i]); f[i] = mk<1>(0); }
+      ph.flux(f, uK, uL, ei);
+      acc += rf.second * f[s].d[0] * (T[K] - T[L]);
+    }
+  return acc;
+}
+
 template <class F>
 int dispatch(const Oracle& o, F&& fn) {
   const double* p = o.params.data();
@@ -1086,6 +1300,7 @@ int dispatch(const Oracle& o, F&& fn) {
       return fn(ph);
     }
     case 21: { PhysTestFunction ph; return fn(ph); }
+    case 22: { PhysEx430T<double> ph; ph.p = P(0); return fn(ph); }
     case 18: { PhysEdgeReaction ph; ph.mode = (int)P(0); ph.dim = (int)P(1); return fn(ph); }
     case 19: { PhysJouleHeat ph; ph.kappa0 = P(0); ph.alpha = P(1); ph.T0 = P(2); ph.lam = P(3); ph.c = P(4); return fn(ph); }
     case 17: { PhysBoundarySpecies ph; ph.d = P(0); ph.k = P(1); ph.c = P(2); ph.db = P(3); ph.kmax = P(4); ph.cmax = P(5); ph.breg = (int)P(6); return fn(ph); }
@@ -1097,7 +1312,7 @@ int nspec_of(int phys) {
   switch (phys) {
     case 3: case 4: case 14: case 17: case 19: return 2;
     case 13: case 20: return 3;
-    case 1: case 2: case 5: case 6: case 7: case 8: case 11: case 12: case 15: case 16: case 18: case 21: return 1;
+    case 1: case 2: case 5: case 6: case 7: case 8: case 11: case 12: case 15: case 16: case 18: case 21: case 22: return 1;
   }
   return 0;
 }
@@ -1222,6 +1437,31 @@ int64_t oracle_csr(void* h, int64_t* rowptr, int* colind, double* vals) {
 void oracle_integrate(void* h, const double* T, const double* U, const double* Uold, double* out) {
   Oracle* o = static_cast<Oracle*>(h);
   dispatch(*o, [&](const auto& ph) { integrate_t(*o, ph, T, U, Uold ? Uold : U, out); return 0; });
+}
+
+// Parameter derivatives of the residual at U: out = npd x n; returns npd (0
+// for a physics without differentiable parameters)
+int oracle_parameter_derivatives(void* h, const double* U, double time, double tstep, double lambda, double* out) {
+  Oracle* o = static_cast<Oracle*>(h);
+  if (o->phys != 22) return 0;
+  PhysEx430T<Dual<1>> ph;
+  ph.p = mk<1>(o->params.empty() ? 0.0 : o->params[0]);
+  ph.p.d[0] = 1.0;
+  if (out) dparams_t(*o, ph, U, time, tstep, lambda, out);
+  return 1;
+}
+
+// Derivatives of the steady test-function current of species s: du (n) and,
+// for a physics with differentiable parameters, dp (npd values); returns npd
+int oracle_integrate_gradient(void* h, const double* T, const double* U, int s, double* du, double* dp) {
+  Oracle* o = static_cast<Oracle*>(h);
+  dispatch(*o, [&](const auto& ph) { integrate_grad_t(*o, ph, T, U, s, du); return 0; });
+  if (o->phys != 22) return 0;
+  PhysEx430T<Dual<1>> ph;
+  ph.p = mk<1>(o->params.empty() ? 0.0 : o->params[0]);
+  ph.p.d[0] = 1.0;
+  if (dp) dp[0] = integrate_dp_t(*o, ph, T, U, s);
+  return 1;
 }
 
 // the mass matrix into the entry store (read it with oracle_csr)

@@ -31,6 +31,7 @@ EXAMPLES = {
     "Example161_BipolarDriftDiffusionCurrent": r"testval\s*=\s*([-0-9.e]+)",
     "Example207_NonlinearPoisson2D": r"testval\s*=\s*([-0-9.e]+)",
     "Example301_Laplace3D": r"testval\s*=\s*([-0-9.e]+)",
+    "Example430_ParameterDerivativesStationary": r"testval\s*=\s*([-0-9.e]+)",
     "Example440_ParallelState": r"testval\s*=\s*([-0-9.e]+)",
 }
 

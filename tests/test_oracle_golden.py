@@ -12,6 +12,7 @@ import os
 
 import numpy as np
 import pytest
+import scipy.sparse.linalg as spla
 
 from conftest import GOLDEN
 
@@ -157,3 +158,50 @@ def test_example161_current(vfvm, oracle, testvals, assembly):
     assert len(times) == 119
     ref = testvals["Example161_BipolarDriftDiffusionCurrent"]["value"]
     assert E.current_sum(osys, tf, times, sols) == pytest.approx(ref, rel=RTOL)
+
+
+def ex430_sum(vfvm, oracle, solve_and_derivatives):
+    """Example430's runh (:183-247): for p in 0.1:0.05:2 the steady current m
+    between boundary regions 1 and 3 and its total derivative
+    dm/dp = -dm/du (J \\ dudp) + dm/dp; the sum over p."""
+    X = np.array([i / 10 for i in range(11)])
+    g = vfvm.simplexgrid(X, X)
+    T = oracle.testfunction(g, [1], [3])
+    total = 0.0
+    for k in range(39):
+        p = 0.1 + 0.05 * k
+        osys = oracle.OracleSystem(g, "ex430", [p])
+        sol, J, dFdp = solve_and_derivatives(g, p, osys)
+        du, dp = osys.integrate_gradient(T, sol)
+        total += -du @ spla.splu(J.tocsc()).solve(dFdp) + dp[0]
+    return total
+
+
+def test_example430_parameter_derivatives(vfvm, oracle, testvals):
+    """Example430 (runtests :250-257): parameter derivatives of a stationary
+    solve through dudp, the Jacobian and the test-function current."""
+    def oracle_solve(g, p, osys):
+        sol, _ = oracle.solve_step(osys, np.full(g.nnodes, 0.5), oracle.Control())
+        _, J = osys.assemble(sol)
+        return sol, J, osys.parameter_derivatives(sol)[0]
+    ref = testvals["Example430_ParameterDerivativesStationary"]["value"]
+    assert ex430_sum(vfvm, oracle, oracle_solve) == pytest.approx(ref, rel=RTOL)
+
+
+def test_oracle_parameter_derivatives_vs_differences(vfvm, oracle):
+    """dudp against central differences of the residual in p."""
+    X = np.array([i / 10 for i in range(11)])
+    g = vfvm.simplexgrid(X, X)
+    U = np.random.default_rng(2).uniform(0.2, 1.0, g.nnodes)
+    p, h = 0.7, 1e-6
+    d = oracle.OracleSystem(g, "ex430", [p]).parameter_derivatives(U)[0]
+    Fp, _ = oracle.OracleSystem(g, "ex430", [p + h]).assemble(U)
+    Fm, _ = oracle.OracleSystem(g, "ex430", [p - h]).assemble(U)
+    fd = (Fp - Fm) / (2 * h)
+    # rows of the Dirichlet nodes carry the 1e30 penalty, where differences of F
+    # only resolve the penalty's own derivative (regions 3: -1e30 * factor)
+    dirichlet = np.zeros(g.nnodes, dtype=bool)
+    dirichlet[np.unique(g.bfacenodes[:, np.isin(g.bfaceregions, [1, 3])])] = True
+    assert np.allclose(d[~dirichlet], fd[~dirichlet], rtol=1e-6, atol=1e-8)
+    big = np.abs(d) > 1e20
+    assert big.any() and np.allclose(d[big], fd[big], rtol=1e-6)

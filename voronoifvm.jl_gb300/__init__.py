@@ -9,7 +9,8 @@ from .system import (AssemblyError, ConvergenceError, EmbeddingError, LinearSolv
                      Physics, SolverControl, System, TransientSolution, boundary_dirichlet, edgefactors,
                      enable_boundary_species, enable_species, evaluate_residual_and_jacobian, fixed_timesteps,
                      integrate, integrate_gradT_flux, node_species, nodevolumes, num_species, solve,
-                     TestFunctionFactory, testfunction, unknowns, eval_rhs, eval_jacobian, mass_matrix)
+                     TestFunctionFactory, testfunction, unknowns, eval_rhs, eval_jacobian, mass_matrix,
+                     parameter_derivatives)
 from . import _lib
 from .batch import BatchSolver
 from . import learned
@@ -18,6 +19,6 @@ from .build import build_library
 __all__ = ["Grid", "simplexgrid", "read_sg", "write_sg", "Physics", "System", "SolverControl", "NewtonSolverHistory", "TransientSolution",
            "AssemblyError", "ConvergenceError", "EmbeddingError", "LinearSolverError", "boundary_dirichlet",
            "enable_species", "enable_boundary_species", "node_species", "TestFunctionFactory", "testfunction",
-           "integrate_gradT_flux", "eval_rhs", "eval_jacobian", "mass_matrix",
+           "integrate_gradT_flux", "eval_rhs", "eval_jacobian", "mass_matrix", "parameter_derivatives",
            "edgefactors", "evaluate_residual_and_jacobian", "fixed_timesteps", "integrate", "nodevolumes",
            "num_species", "solve", "unknowns", "build_library"]

@@ -268,11 +268,27 @@ struct BNodeItem {
   double* dirichlet_value;  // written by boundary_dirichlet (Dirichlet initialisation)
 };
 
+// A physics parameter as a constant of type PT: a plain double, or a dual
+// number with zero partials (parameter derivatives seed it afterwards).
+template <class PT> VFVM_HD PT pconst(double v) { return v; }
+template <> VFVM_HD Dual<1, double> pconst<Dual<1, double>>(double v) { return dconst<1, double>(v); }
+
 // boundary_dirichlet!(y,u,bnode,ispec,ireg,val), src/vfvm_physics.jl:487-494
 template <class T> VFVM_HD void boundary_dirichlet(T* y, const T* u, const BNodeItem& b, int ispec, int ireg, double v) {
   if (b.region == ireg) {
     y[ispec] = y[ispec] + (u[ispec] - v) * b.Dirichlet;
     if (b.dirichlet_value) b.dirichlet_value[ispec] = v;
+  }
+}
+
+// the same with a dual value (the derivative with respect to a parameter that
+// sets the Dirichlet value)
+template <int N, typename P>
+VFVM_HD void boundary_dirichlet(Dual<N, P>* y, const Dual<N, P>* u, const BNodeItem& b, int ispec, int ireg,
+                                const Dual<N, P>& v) {
+  if (b.region == ireg) {
+    y[ispec] = y[ispec] + (u[ispec] - v) * b.Dirichlet;
+    if (b.dirichlet_value) b.dirichlet_value[ispec] = v.v;
   }
 }
 

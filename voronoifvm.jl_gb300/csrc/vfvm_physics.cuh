@@ -33,6 +33,10 @@ struct PhysBase {
   VFVM_HD void bsource(double*, const BNodeItem&) const {}
   // whether the parameter block suits grids of this dimension (checked once by vfvm_create)
   static bool valid(int, const double*) { return true; }
+  // parameters with derivatives (the reference's nparams / parameters(u)): the
+  // first NPD entries of the parameter block; a physics with NPD > 0 is a
+  // template over the parameter type PT with `rebind<PT>` and `seed(k)`
+  static constexpr int NPD = 0;
 };
 
 // examples/Example105_NonlinearPoisson1D.jl:41-60;  params: eps
@@ -453,12 +457,43 @@ struct PhysTestFunction : PhysBase {
   template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const { f[0] = u[0]; }
 };
 
+// examples/Example430_ParameterDerivativesStationary.jl:146-166 (runh): flux
+// (1 + p) (u_K^2 - u_L^2), reaction p u^5, u = 0 on boundary region 1 and u = p
+// on region 3, with p the parameter whose derivatives dF/dp the assembly
+// provides (the reference's parameters(u)[1], nparams = 1).  PT is double for
+// the ordinary assembly and a dual number of width one for dF/dp.
+// params: p
+template <class PT>
+struct PhysEx430T : PhysBase {
+  static constexpr int NS = 1;
+  static constexpr int NPD = 1;
+  static constexpr bool has_reaction = true, has_breaction = true;
+  template <class Q> using rebind = PhysEx430T<Q>;
+  PT p;
+  VFVM_HD void load(const double* q) { p = pconst<PT>(q[0]); }
+  VFVM_HD void seed(int k) {
+    if constexpr (!std::is_same<PT, double>::value) p.d[0] = k == 0 ? 1.0 : 0.0;
+  }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const {
+    f[0] = (1.0 + p) * (uK[0] * uK[0] - uL[0] * uL[0]);
+  }
+  template <class T> VFVM_HD void reaction(T* f, const T* u, const NodeItem&) const {
+    const T u2 = u[0] * u[0];
+    f[0] = p * (u2 * u2 * u[0]);
+  }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const {
+    boundary_dirichlet(f, u, b, 0, 1, 0.0);
+    boundary_dirichlet(f, u, b, 0, 3, p);
+  }
+};
+using PhysEx430 = PhysEx430T<double>;
+
 inline int physics_nspec(int id) {
   switch (id) {
     case VFVM_PHYS_EX105: case VFVM_PHYS_EX106: case VFVM_PHYS_EX207: case VFVM_PHYS_EX301:
     case VFVM_PHYS_EX440: case VFVM_PHYS_LAPLACE_DIRICHLET: case VFVM_PHYS_NLPOISSON:
     case VFVM_PHYS_POROUS: case VFVM_PHYS_KAPPA_EXP: case VFVM_PHYS_SURFACE_HEAT:
-    case VFVM_PHYS_EDGE_REACTION: case VFVM_PHYS_TESTFUNCTION: return 1;
+    case VFVM_PHYS_EDGE_REACTION: case VFVM_PHYS_TESTFUNCTION: case VFVM_PHYS_EX430: return 1;
     case VFVM_PHYS_EX110: case VFVM_PHYS_EX160: case VFVM_PHYS_RD2: case VFVM_PHYS_BOUNDARY_SPECIES:
     case VFVM_PHYS_JOULE_HEAT: return 2;
     case VFVM_PHYS_BIPOLAR: case VFVM_PHYS_EX161: return 3;
@@ -477,6 +512,7 @@ inline int physics_nparams(int id) {
     case VFVM_PHYS_EDGE_REACTION: return 2;
     case VFVM_PHYS_JOULE_HEAT: return 5;
     case VFVM_PHYS_EX161: return 14;
+    case VFVM_PHYS_EX430: return 1;
   }
   return 0;
 }
@@ -505,6 +541,7 @@ int dispatch_physics(int id, Fn&& fn) {
     case VFVM_PHYS_JOULE_HEAT: return fn(PhysJouleHeat{});
     case VFVM_PHYS_EX161: return fn(PhysEx161{});
     case VFVM_PHYS_TESTFUNCTION: return fn(PhysTestFunction{});
+    case VFVM_PHYS_EX430: return fn(PhysEx430{});
   }
   return VFVM_ERR_INPUT;
 }

@@ -19,6 +19,8 @@ Names, argument meaning and error behaviour follow the reference:
   (src/vfvm_densesolution.jl:11-49) and src/vfvm_postprocess.jl:18-100,397-412
 * ``eval_rhs``, ``eval_jacobian``, ``mass_matrix`` -- the ODE/DAE form,
   src/vfvm_diffeq_interface.jl:10-112
+* ``parameter_derivatives`` -- the residual's derivatives with respect to the
+  physics' differentiable parameters (the reference's dudp)
 * ``TestFunctionFactory``, ``testfunction``, ``integrate(sys, T, U[, Uold,
   tstep])``, ``integrate_gradT_flux`` -- test-function currents,
   src/vfvm_testfunctions.jl:38-380
@@ -46,7 +48,7 @@ __all__ = ["Physics", "System", "SolverControl", "NewtonSolverHistory", "Transie
            "boundary_dirichlet", "enable_species", "enable_boundary_species", "solve", "unknowns",
            "evaluate_residual_and_jacobian", "node_species",
            "fixed_timesteps", "nodevolumes", "integrate", "num_species", "TestFunctionFactory", "testfunction",
-           "integrate_gradT_flux", "eval_rhs", "eval_jacobian", "mass_matrix"]
+           "integrate_gradT_flux", "eval_rhs", "eval_jacobian", "mass_matrix", "parameter_derivatives"]
 
 Dirichlet = 1.0e30  # src/vfvm_system.jl:329
 
@@ -535,6 +537,23 @@ def eval_jacobian(sys: System, u, t: float = 0.0):
     """eval_jacobian!(J, u, state, t) (src/vfvm_diffeq_interface.jl:42-48): -J."""
     _, J = evaluate_residual_and_jacobian(sys, u, t=t, tstep=math.inf)
     return -J
+
+
+def parameter_derivatives(sys: System, u, t: float = 0.0, tstep: float = math.inf, embed: float = 0.0) -> np.ndarray:
+    """dudp (src/vfvm_assembly.jl:116-120,194-198,403-405,...): dF/dp_k at u for
+    the physics' differentiable parameters (the first npd entries of its
+    parameter block), computed on the device; shape (npd, nspec, nnodes).
+    With F(u(p), p) = 0, du/dp = -J^-1 dudp."""
+    lib = L.load()
+    U = _flat(u, sys)
+    npd = ctypes.c_int32(0)
+    _raise(lib.vfvm_parameter_derivatives(sys.ctx, L.ptr(U), t, tstep, embed, None, ctypes.byref(npd)),
+           "vfvm_parameter_derivatives")
+    out = np.zeros((npd.value, sys.ndofs))
+    if npd.value:
+        _raise(lib.vfvm_parameter_derivatives(sys.ctx, L.ptr(U), t, tstep, embed, L.ptr(out), ctypes.byref(npd)),
+               "vfvm_parameter_derivatives")
+    return np.stack([_shape(r, sys) for r in out]) if npd.value else out.reshape(0, sys.nspec, sys.nnodes)
 
 
 def mass_matrix(sys: System):
