@@ -90,6 +90,10 @@ extern "C" {
 #define VFVM_PHYS_EX430 22            /* Example430 (runh): flux (1+p)(u_K^2 - u_L^2), reaction p u^5, u = 0 on
                                          boundary region 1, u = p on region 3; p has parameter derivatives;
                                          params: p */
+#define VFVM_PHYS_OUTFLOW 23          /* pressure + transported concentration with an outflow boundary (the
+                                         reference's pluto-examples/outflow.jl: Darcy flux, Scharfetter-Gummel
+                                         transport, boutflow on region G_out);
+                                         params: k, v_in, c_in, D, G_in, G_out */
 
 /* linear solver / preconditioner / precision selectors */
 #define VFVM_KRYLOV_BICGSTAB 0

@@ -116,7 +116,10 @@ inline double ramp(double t, double t0, double t1, double u0, double u1) {
 
 // ---------------------------------------------------------------- geometry items
 struct NodeInfo { int index, region; const double* x; double time, lambda; const double* ndata; };
-struct EdgeInfo { int K, L, region; const double* xK; const double* xL; double time, lambda; const double* ndataK; const double* ndataL; };
+struct EdgeInfo {
+  int K, L, region; const double* xK; const double* xL; double time, lambda; const double* ndataK; const double* ndataL;
+  int outflownode = 0;  // outflownode(edge): 1 or 2 on edges with a node on an outflow boundary
+};
 struct BNodeInfo { int index, region; const double* x; double time, lambda, fac, Dirichlet; double* dirichlet_value; };
 struct BEdgeInfo { int K, L, region; const double* xK; const double* xL; double time, lambda; };
 
@@ -144,6 +147,9 @@ struct PhysParams { const double* p; int np; };
 // physics defines them.
 struct OBase {
   static const bool has_bflux = false, has_bstorage = false, has_bsource = false, has_edgereaction = false;
+  static const bool has_boutflow = false;
+  template <class T> void boutflow(T*, const T*, const T*, const EdgeInfo&) const {}
+  bool outflow_region(int) const { return false; }
   template <class T> void edgereaction(T*, const T*, const T*, const EdgeInfo&) const {}
   template <class T> void bflux(T*, const T*, const T*, const BEdgeInfo&) const {}
   template <class T> void bstorage(T*, const T*, BNodeInfo&) const {}
@@ -538,6 +544,35 @@ struct PhysEx430T : OBase {
   }
 };
 
+// pluto-examples/outflow.jl: darcyvelo, flux, bcondition and boutflow of
+// FlowTransportData (p species 1, c species 2); outflowboundaries = [G_out].
+struct PhysOutflow : OBase {
+  static const int NS = 2;
+  static const bool has_reaction = false, has_storage = false, has_source = false, has_breaction = true;
+  static const bool has_boutflow = true;
+  double k, v_in, c_in, D; int gin, gout;
+  bool outflow_region(int reg) const { return reg == gout; }
+  template <class T> T darcyvelo(const T* uK, const T* uL) const { return k * (uK[0] - uL[0]); }
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
+    T vh = darcyvelo(uK, uL);
+    f[0] = vh;
+    T bp, bm;
+    fbernoulli_pm(vh / D, bp, bm);
+    f[1] = D * (bm * uK[1] - bp * uL[1]);
+  }
+  template <class T> void reaction(T*, const T*, const NodeInfo&) const {}
+  template <class T> void storage(T*, const T*, const NodeInfo&) const {}
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const {
+    if (b.region == gin) f[0] = f[0] - v_in;  // boundary_neumann!, src/vfvm_physics.jl:532
+    boundary_dirichlet(f, u, b, 0, gout, 0.0);
+    boundary_dirichlet(f, u, b, 1, gin, c_in);
+  }
+  template <class T> void boutflow(T* f, const T* uK, const T* uL, const EdgeInfo& e) const {
+    f[1] = -(darcyvelo(uK, uL) * (e.outflownode == 1 ? uK[1] : uL[1]));
+  }
+};
+
 // The physics of TestFunctionFactory (src/vfvm_testfunctions.jl:38-50): flux
 // u_K - u_L, storage u; Dirichlet data through the legacy boundary factors.
 struct PhysTestFunction : OBase {
@@ -579,6 +614,9 @@ struct Oracle {
   // (node_dof); masked = false: every species on every node
   bool masked = false;
   std::vector<unsigned> reg_spec, node_spec;
+  // outflow nodes (outflownoderegions, src/vfvm_system.jl:660-673): nodes of the
+  // boundary faces in outflowboundaries
+  std::vector<uint8_t> outflow;
 };
 
 inline int nn_bface(int dim) { return dim; }  // nodes per boundary face: Vertex0D 1, Edge1D 2, Triangle2D 3
@@ -818,6 +856,35 @@ int assemble_t(Oracle& o, const P& ph, const double* U, const double* Uold, doub
         addnz(o, iL, jK, -f[i].d[j], fac);
         addnz(o, iK, jL, +f[i].d[NS + j], fac);
         addnz(o, iL, jL, -f[i].d[NS + j], fac);
+      }
+    }
+    // boutflow, src/vfvm_assembly.jl:239-313: on edges with a node on an outflow
+    // boundary (outflownode!: the second node if both are), +fac r to the first
+    // node if it is an outflow node, -fac r to the second if it is
+    if (P::has_boutflow && !boundary && !o.outflow.empty() && (o.outflow[K] || o.outflow[L])) {
+      Dual<2 * NS> r[NS];
+      for (int i = 0; i < NS; ++i) r[i] = mk<2 * NS>(0);
+      EdgeInfo ei{K, L, reg, &o.coord[d * K], &o.coord[d * L], time, lambda,
+                  nd ? nd + (size_t)o.nnd * K : nullptr, nd ? nd + (size_t)o.nnd * L : nullptr};
+      ei.outflownode = o.outflow[L] ? 2 : 1;
+      ph.boutflow(r, uK, uL, ei);
+      for (int i = 0; i < NS; ++i) {
+        if (!((m >> i) & 1u)) continue;
+        double v = fac * r[i].v;
+        if (o.outflow[K]) F[K * NS + i] += v;
+        if (o.outflow[L]) F[L * NS + i] += -v;
+        for (int j = 0; j < NS; ++j) {
+          if (!((m >> j) & 1u)) continue;
+          int64_t iK = (int64_t)K * NS + i, iL = (int64_t)L * NS + i, jK = (int64_t)K * NS + j, jL = (int64_t)L * NS + j;
+          if (o.outflow[K]) {
+            addnz(o, iK, jK, +r[i].d[j], fac);
+            addnz(o, iK, jL, r[i].d[NS + j], fac);
+          }
+          if (o.outflow[L]) {
+            addnz(o, iL, jK, -r[i].d[j], fac);
+            addnz(o, iL, jL, -r[i].d[NS + j], fac);
+          }
+        }
       }
     }
     // edgereaction, src/vfvm_assembly.jl:202-238: fac * r to both end nodes,
@@ -1301,6 +1368,11 @@ int dispatch(const Oracle& o, F&& fn) {
     }
     case 21: { PhysTestFunction ph; return fn(ph); }
     case 22: { PhysEx430T<double> ph; ph.p = P(0); return fn(ph); }
+    case 23: {
+      PhysOutflow ph;
+      ph.k = P(0); ph.v_in = P(1); ph.c_in = P(2); ph.D = P(3); ph.gin = (int)P(4); ph.gout = (int)P(5);
+      return fn(ph);
+    }
     case 18: { PhysEdgeReaction ph; ph.mode = (int)P(0); ph.dim = (int)P(1); return fn(ph); }
     case 19: { PhysJouleHeat ph; ph.kappa0 = P(0); ph.alpha = P(1); ph.T0 = P(2); ph.lam = P(3); ph.c = P(4); return fn(ph); }
     case 17: { PhysBoundarySpecies ph; ph.d = P(0); ph.k = P(1); ph.c = P(2); ph.db = P(3); ph.kmax = P(4); ph.cmax = P(5); ph.breg = (int)P(6); return fn(ph); }
@@ -1310,7 +1382,7 @@ int dispatch(const Oracle& o, F&& fn) {
 
 int nspec_of(int phys) {
   switch (phys) {
-    case 3: case 4: case 14: case 17: case 19: return 2;
+    case 3: case 4: case 14: case 17: case 19: case 23: return 2;
     case 13: case 20: return 3;
     case 1: case 2: case 5: case 6: case 7: case 8: case 11: case 12: case 15: case 16: case 18: case 21: case 22: return 1;
   }
@@ -1345,6 +1417,14 @@ void* oracle_create(int dim, int nnodes, const double* coord, int ncells, const 
       if (o->bfactors[i] != 0.0 || o->bvalues[i] != 0.0) o->has_legacy = true;
   }
   setup(*o);
+  dispatch(*o, [&](const auto& ph) {
+    if (!std::decay_t<decltype(ph)>::has_boutflow) return 0;
+    o->outflow.assign(o->N, 0);
+    for (int b = 0; b < o->nbf; ++b)
+      if (ph.outflow_region(o->bfaceregions[b]))
+        for (int v = 0; v < nn_bface(o->dim); ++v) o->outflow[o->bfacenodes[v + nn_bface(o->dim) * b]] = 1;
+    return 0;
+  });
   return o;
 }
 

@@ -74,6 +74,9 @@ def case(vfvm, name, seed=0):
         t, tstep = ex161_case.T_PRECOND + 0.5 * ex161_case.T_RAMP, 1e-6
     elif name == "ex430":  # Example430: Dirichlet value and coefficients from the parameter p
         g, kind, params = sg(lin(10), lin(10)), "ex430", [0.7]
+    elif name == "outflow2d":  # pluto-examples/outflow.jl: outflow region 5 on part of the right side
+        g = vfvm.bfacemask(sg(lin(10), lin(10)), [1, 0.3], [1, 0.7], 5)
+        kind, params = "outflow", [1.0, 1.0, 0.5, 1.0, 4, 5]
     elif name == "laplace_dirichlet":
         g, kind, params = sg(lin(9)), "laplace_dirichlet", []
     else:
@@ -96,4 +99,4 @@ def random_state(c, nspec, rng):
 
 NAMES = ["nlpoisson", "porous", "bipolar", "rd2", "kappa_exp", "ex105", "ex106", "ex110", "ex160", "ex207",
          "ex301", "ex440", "laplace_dirichlet", "kappa_unstructured", "surface_heat2d", "surface_heat3d",
-         "edge_reaction2d", "edge_reaction3d", "joule_heat", "ex161", "ex430"]
+         "edge_reaction2d", "edge_reaction3d", "joule_heat", "ex161", "ex430", "outflow2d"]

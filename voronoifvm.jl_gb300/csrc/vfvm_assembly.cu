@@ -267,7 +267,8 @@ int launch_assemble(vfvm_ctx* c, const double* U, const double* Uold, const doub
   return dispatch_physics(c->phys, [&](auto ph) {
     using Ph = decltype(ph);
     // the tiled kernel has no boundary-edge terms: physics with bflux use the node kernel
-    if (!Ph::has_bflux && !Ph::has_edgereaction && !c->multireg && c->ntiles > 0 && !use_node_kernel()) {
+    if (!Ph::has_bflux && !Ph::has_edgereaction && !Ph::has_boutflow && !c->multireg && c->ntiles > 0 &&
+        !use_node_kernel()) {
       const TileTables tt = c->tile_tables();
       const size_t b = Jf ? tile_smem_bytes<Ph, float>(c) : tile_smem_bytes<Ph, double>(c);
       if (b) {

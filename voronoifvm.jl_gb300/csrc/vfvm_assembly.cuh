@@ -253,6 +253,39 @@ __device__ __forceinline__ bool assemble_node(const AsmTables& t, const Ph& ph, 
           }
         }
       }
+      if constexpr (Ph::has_boutflow) {
+        // boutflow (src/vfvm_assembly.jl:239-313): on an edge with a node on an
+        // outflow boundary region, fac * r to the first node's residual (+) when
+        // it is an outflow node and to the second's (-) when that one is; the
+        // edge's outflow node is the second if both are
+        const bool oA = t.outflow_node && t.outflow_node[A], oB = t.outflow_node && t.outflow_node[B];
+        if (oA || oB) {
+          ei.outflownode = oB ? 2 : 1;
+          Dual<2 * NS, P> r[NS];
+#pragma unroll
+          for (int i = 0; i < NS; ++i) r[i] = dconst<2 * NS, P>(0.0);
+          ph.boutflow(r, ua, ub, ei);
+          if (kfirst ? oA : oB) {
+#pragma unroll
+            for (int i = 0; i < NS; ++i) {
+              if (!((rm >> i) & 1u)) continue;
+              fK[i] += kfirst ? fac * r[i].v : -(fac * r[i].v);
+#pragma unroll
+              for (int j = 0; j < NS; ++j) {
+                if (!((rm >> j) & 1u)) continue;
+                if (kfirst) {
+                  jd[i * NS + j] += r[i].d[j] * facp;
+                  jo[i * NS + j] += r[i].d[NS + j] * facp;
+                } else {
+                  jd[i * NS + j] += (-r[i].d[NS + j]) * facp;
+                  jo[i * NS + j] += (-r[i].d[j]) * facp;
+                }
+              }
+            }
+          }
+          ei.outflownode = 0;
+        }
+      }
       if constexpr (Ph::has_edgereaction) {
         // edgereaction (src/vfvm_assembly.jl:202-238): fac * r added to both end
         // nodes, the Jacobian entries placed as the reference places them (first

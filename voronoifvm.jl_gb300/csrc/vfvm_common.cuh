@@ -252,6 +252,7 @@ struct EdgeItem {
   const double* xK; const double* xL;
   double time, lambda;
   const double* dataK; const double* dataL;
+  int outflownode = 0;   // boutflow: the edge's node on an outflow boundary (1 first, 2 second)
 };
 // boundary edge: an edge of a boundary face (the reference's BEdge,
 // src/vfvm_geometryitems.jl:504-578), K = first node, L = second node

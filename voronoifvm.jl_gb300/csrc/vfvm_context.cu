@@ -171,6 +171,17 @@ void probe_t(const Ph& ph0, const double* params, int dim, const std::vector<int
       for (int i = 0; i < NS; ++i)
         for (int j = 0; j < 2 * NS; ++j)
           if (f[i].d[j] != 0.0) em[i * 2 * NS + j] = 1;
+      if (Ph::has_boutflow) {  // the flux's entries, on the edges at an outflow node
+        for (int node = 1; node <= 2; ++node) {
+          EdgeItem eo = ei;
+          eo.outflownode = node;
+          for (int i = 0; i < NS; ++i) f[i] = dconst<2 * NS, double>(0);
+          ph.boutflow(f, uk, ul, eo);
+          for (int i = 0; i < NS; ++i)
+            for (int j = 0; j < 2 * NS; ++j)
+              if (f[i].d[j] != 0.0) em[i * 2 * NS + j] = 1;
+        }
+      }
       if (Ph::has_edgereaction) {  // the same four entries per species pair as a flux
         for (int i = 0; i < NS; ++i) f[i] = dconst<2 * NS, double>(0);
         ph.edgereaction(f, uk, ul, ei);
@@ -254,6 +265,7 @@ AsmTables vfvm_ctx::tables() const {
   t.bfactors = bfactors.p; t.bvalues = bvalues.p; t.nbregions = nbregions; t.has_legacy = has_legacy ? 1 : 0;
   t.reg_spec = species_masked ? reg_spec.p : nullptr;
   t.node_spec = species_masked ? node_spec.p : nullptr;
+  t.outflow_node = outflow_node.n ? outflow_node.p : nullptr;
   return t;
 }
 
@@ -550,6 +562,22 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
     }
   }
 
+  // --- outflow nodes: the nodes of the boundary faces in the physics'
+  // outflowboundaries (update_grid!, src/vfvm_system.jl:660-673)
+  std::vector<uint8_t> outflow_h;
+  if (dispatch_physics(c->phys, [](auto phy) { return decltype(phy)::has_boutflow ? 1 : 0; }) == 1) {
+    std::vector<double> p(ph->params, ph->params + ph->nparams);
+    p.resize(16, 0.0);
+    outflow_h.assign(N, 0);
+    for (int b = 0; b < nbf; ++b) {
+      const int reg = g->bfaceregions[b];
+      const bool out = dispatch_physics(c->phys, [&](auto phy) {
+        return decltype(phy)::outflow_region(p.data(), reg) ? 1 : 0; }) == 1;
+      if (out)
+        for (int v = 0; v < nbn; ++v) outflow_h[g->bfacenodes[v + (size_t)nbn * b]] = 1;
+    }
+  }
+
   // --- legacy boundary data (boundary_dirichlet!(sys, ispec, ireg, val) etc.)
   std::vector<double> bfac_h((size_t)ns * c->nbregions, 0.0), bval_h((size_t)ns * c->nbregions, 0.0);
   if (ph->nbregions > 0 && ph->bfactors && ph->bvalues) {
@@ -795,6 +823,7 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
     SETUP_CUDA(c->reg_spec.upload(c->h_reg_spec));
     SETUP_CUDA(c->node_spec.upload(c->h_node_spec));
   }
+  if (!outflow_h.empty()) SETUP_CUDA(c->outflow_node.upload(outflow_h));
   SETUP_CUDA(c->dirichlet_dof.upload(dir_dof));
   if (!sbe_ptr.empty()) {
     SETUP_CUDA(c->sbe_ptr.upload(sbe_ptr));

@@ -62,6 +62,8 @@ struct AsmTables {
   // reg_spec[ireg-1] = bit mask of the species enabled in cell region ireg,
   // node_spec[K] = bit mask of the species of node K
   const unsigned* reg_spec; const unsigned* node_spec;
+  // nodes on an outflow boundary region (physics with boutflow; nullptr: none)
+  const uint8_t* outflow_node;
 };
 
 // Node tiles of the edge-once assembly (vfvm_tiles.cu builds them, the tiled
@@ -147,6 +149,7 @@ struct vfvm_ctx {
   bool species_masked = false;
   std::vector<unsigned> h_reg_spec, h_node_spec;
   vfvm::DBuf<unsigned> reg_spec, node_spec;
+  vfvm::DBuf<uint8_t> outflow_node;         // 1 on the nodes of outflow boundary regions (boutflow)
 
   // scalar (reference) pattern
   int64_t nnz = 0;

@@ -50,7 +50,7 @@ vfvm_ctx* clone_context(const vfvm_ctx* b, const vfvm_physics_desc* ph, int* sta
   c->tile_lnodes.view(b->tile_lnodes); c->tile_edge_ab.view(b->tile_edge_ab); c->tile_edge_fac.view(b->tile_edge_fac);
   c->tile_edge_facf.view(b->tile_edge_facf); c->slot_le.view(b->slot_le);
   c->species_masked = b->species_masked; c->h_reg_spec = b->h_reg_spec; c->h_node_spec = b->h_node_spec;
-  c->reg_spec.view(b->reg_spec); c->node_spec.view(b->node_spec);
+  c->reg_spec.view(b->reg_spec); c->node_spec.view(b->node_spec); c->outflow_node.view(b->outflow_node);
   // own physics data; the legacy boundary data must match the base's structure
   c->h_params.assign(ph->params, ph->params + ph->nparams);
   c->nparams = ph->nparams;

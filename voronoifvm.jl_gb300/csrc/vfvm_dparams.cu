@@ -1,6 +1,6 @@
 // Parameter derivatives of the residual: the reference's dudp, accumulated by
 // the asm_param closures of the assembly loops (src/vfvm_assembly.jl:116-120
-// node terms, :194-198 edges, :232-236 edge reactions, :403-405 breaction,
+// node terms, :194-198 edges, :232-236 edge reactions, :296-304 outflow, :403-405 breaction,
 // :434-436 bstorage, assemble_bedges :497-501), for physics whose first NPD
 // parameters carry derivatives (the reference's nparams, parameters(u)).
 //
@@ -77,6 +77,19 @@ __global__ void __launch_bounds__(128) dparams_kernel(const AsmTables t, const d
 #pragma unroll
       for (int i = 0; i < NS; ++i)
         if ((m >> i) & 1u) acc[i] += kfirst ? fac * y[i].d[0] : -(fac * y[i].d[0]);
+      if constexpr (PhD::has_boutflow) {  // outflowasm_param, src/vfvm_assembly.jl:296-304 (+ for both nodes)
+        const bool oA = t.outflow_node && t.outflow_node[A], oB = t.outflow_node && t.outflow_node[B];
+        if (kfirst ? oA : oB) {
+          ei.outflownode = oB ? 2 : 1;
+#pragma unroll
+          for (int i = 0; i < NS; ++i) y[i] = dconst<1, double>(0.0);
+          ph.boutflow(y, uA, uB, ei);
+          ei.outflownode = 0;
+#pragma unroll
+          for (int i = 0; i < NS; ++i)
+            if ((m >> i) & 1u) acc[i] += fac * y[i].d[0];
+        }
+      }
       if constexpr (PhD::has_edgereaction) {
 #pragma unroll
         for (int i = 0; i < NS; ++i) y[i] = dconst<1, double>(0.0);

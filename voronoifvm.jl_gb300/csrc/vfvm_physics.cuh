@@ -23,6 +23,11 @@ struct PhysBase {
   static constexpr bool has_bflux = false, has_bstorage = false, has_bsource = false;
   // edgereaction (src/vfvm_physics.jl:67-182): an edge term added to both end nodes
   static constexpr bool has_edgereaction = false;
+  // boutflow (src/vfvm_physics.jl:148-160): an edge term on the edges with a node
+  // on an outflow boundary region, added to that node's residual
+  static constexpr bool has_boutflow = false;
+  template <class T> VFVM_HD void boutflow(T*, const T*, const T*, const EdgeItem&) const {}
+  static bool outflow_region(const double*, int) { return false; }  // outflowboundaries
   template <class T> VFVM_HD void reaction(T*, const T*, const NodeItem&) const {}
   template <class T> VFVM_HD void edgereaction(T*, const T*, const T*, const EdgeItem&) const {}
   template <class T> VFVM_HD void storage(T*, const T*, const NodeItem&) const {}
@@ -488,6 +493,38 @@ struct PhysEx430T : PhysBase {
 };
 using PhysEx430 = PhysEx430T<double>;
 
+// The flow-and-transport system of the reference's outflow example
+// (pluto-examples/outflow.jl): pressure p and concentration c, Darcy velocity
+// v_h = k (p_K - p_L), flux (v_h, D (B(-v_h/D) c_K - B(v_h/D) c_L)) through
+// fbernoulli_pm(v_h / D); inflow v_in (Neumann) and c = c_in on boundary region
+// G_in, p = 0 on G_out; the outflow term -v_h c_out on the edges with a node on
+// G_out (c_out: that node's c).
+// params: k, v_in, c_in, D, G_in, G_out
+struct PhysOutflow : PhysBase {
+  static constexpr int NS = 2;
+  static constexpr bool has_breaction = true, has_boutflow = true;
+  double k, v_in, c_in, D;
+  int gin, gout;
+  VFVM_HD void load(const double* p) { k = p[0]; v_in = p[1]; c_in = p[2]; D = p[3]; gin = (int)p[4]; gout = (int)p[5]; }
+  static bool outflow_region(const double* p, int reg) { return reg == (int)p[5]; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const {
+    const T vh = (uK[0] - uL[0]) * k;
+    f[0] = vh;
+    T bp, bm;
+    fbernoulli_pm(vh / D, bp, bm);
+    f[1] = (bm * uK[1] - bp * uL[1]) * D;
+  }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const {
+    if (b.region == gin) f[0] = f[0] - v_in;  // boundary_neumann!
+    boundary_dirichlet(f, u, b, 0, gout, 0.0);
+    boundary_dirichlet(f, u, b, 1, gin, c_in);
+  }
+  template <class T> VFVM_HD void boutflow(T* f, const T* uK, const T* uL, const EdgeItem& e) const {
+    const T vh = (uK[0] - uL[0]) * k;
+    f[1] = -(vh * (e.outflownode == 1 ? uK[1] : uL[1]));
+  }
+};
+
 inline int physics_nspec(int id) {
   switch (id) {
     case VFVM_PHYS_EX105: case VFVM_PHYS_EX106: case VFVM_PHYS_EX207: case VFVM_PHYS_EX301:
@@ -495,7 +532,7 @@ inline int physics_nspec(int id) {
     case VFVM_PHYS_POROUS: case VFVM_PHYS_KAPPA_EXP: case VFVM_PHYS_SURFACE_HEAT:
     case VFVM_PHYS_EDGE_REACTION: case VFVM_PHYS_TESTFUNCTION: case VFVM_PHYS_EX430: return 1;
     case VFVM_PHYS_EX110: case VFVM_PHYS_EX160: case VFVM_PHYS_RD2: case VFVM_PHYS_BOUNDARY_SPECIES:
-    case VFVM_PHYS_JOULE_HEAT: return 2;
+    case VFVM_PHYS_JOULE_HEAT: case VFVM_PHYS_OUTFLOW: return 2;
     case VFVM_PHYS_BIPOLAR: case VFVM_PHYS_EX161: return 3;
   }
   return 0;
@@ -513,6 +550,7 @@ inline int physics_nparams(int id) {
     case VFVM_PHYS_JOULE_HEAT: return 5;
     case VFVM_PHYS_EX161: return 14;
     case VFVM_PHYS_EX430: return 1;
+    case VFVM_PHYS_OUTFLOW: return 6;
   }
   return 0;
 }
@@ -542,6 +580,7 @@ int dispatch_physics(int id, Fn&& fn) {
     case VFVM_PHYS_EX161: return fn(PhysEx161{});
     case VFVM_PHYS_TESTFUNCTION: return fn(PhysTestFunction{});
     case VFVM_PHYS_EX430: return fn(PhysEx430{});
+    case VFVM_PHYS_OUTFLOW: return fn(PhysOutflow{});
   }
   return VFVM_ERR_INPUT;
 }

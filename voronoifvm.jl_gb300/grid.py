@@ -176,6 +176,31 @@ def _as_coords(X):
     return X
 
 
+def _mask(grid: Grid, nodes: np.ndarray, maskmin, maskmax, tol: float) -> np.ndarray:
+    lo = np.asarray(maskmin, dtype=np.float64).reshape(-1, 1) - tol
+    hi = np.asarray(maskmax, dtype=np.float64).reshape(-1, 1) + tol
+    inside = np.ones(nodes.shape[1], dtype=bool)
+    for v in range(nodes.shape[0]):
+        x = grid.coord[:, nodes[v]]
+        inside &= np.all((x >= lo) & (x <= hi), axis=0)
+    return inside
+
+
+def cellmask(grid: Grid, maskmin, maskmax, ireg: int, tol: float = 1e-10) -> Grid:
+    """cellmask!(grid, maskmin, maskmax, ireg) (ExtendableGrids): the cells whose
+    nodes all lie in the box [maskmin, maskmax] (widened by tol) get region ireg."""
+    grid.cellregions[_mask(grid, grid.cellnodes, maskmin, maskmax, tol)] = ireg
+    return grid
+
+
+def bfacemask(grid: Grid, maskmin, maskmax, ireg: int, tol: float = 1e-10) -> Grid:
+    """bfacemask!(grid, maskmin, maskmax, ireg) (ExtendableGrids): the boundary
+    faces whose nodes all lie in the box [maskmin, maskmax] (widened by tol) get
+    boundary region ireg."""
+    grid.bfaceregions[_mask(grid, grid.bfacenodes, maskmin, maskmax, tol)] = ireg
+    return grid
+
+
 def simplexgrid(*axes) -> Grid:
     """Create a 1D, 2D or 3D simplex grid from tensor-product coordinate vectors,
     or read one from a SimplexGrid text file (``simplexgrid(path)``, as in
