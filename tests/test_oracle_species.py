@@ -109,3 +109,16 @@ def test_host_species_api(vfvm):
     assert vfvm.node_species(s3).all()
     with pytest.raises(ValueError):
         vfvm.System(g2, vfvm.Physics("rd2", [1, 1, 1]), unknown_storage="compressed")
+
+
+def test_host_system_keywords(vfvm):
+    """System(...; matrixtype, valuetype, nparams) keywords of the reference."""
+    g = vfvm.simplexgrid(np.linspace(0.0, 1.0, 5), np.linspace(0.0, 1.0, 5))
+    assert vfvm.System(g, vfvm.Physics("ex430", [0.5]), nparams=1).nparams == 1
+    assert vfvm.System(g, vfvm.Physics("nlpoisson"), matrixtype="banded").nparams == 0
+    with pytest.raises(ValueError):
+        vfvm.System(g, vfvm.Physics("nlpoisson"), nparams=1)
+    with pytest.raises(ValueError):
+        vfvm.System(g, vfvm.Physics("nlpoisson"), valuetype=np.float32)
+    with pytest.raises(ValueError):
+        vfvm.System(g, vfvm.Physics("nlpoisson"), matrixtype="dense")

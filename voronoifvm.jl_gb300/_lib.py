@@ -25,6 +25,14 @@ PHYSICS_IDS = {
     "surface_heat": 16, "boundary_species": 17, "edge_reaction": 18, "joule_heat": 19, "ex161": 20,
     "testfunction": 21, "ex430": 22, "outflow": 23,
 }
+# physics whose first parameters carry derivatives (NPD in the device functor)
+PHYSICS_NPD = {22: 1}
+
+
+def physics_npd(physics_id: int) -> int:
+    return PHYSICS_NPD.get(physics_id, 0)
+
+
 PHYSICS_NSPEC = {1: 1, 2: 1, 3: 2, 4: 2, 5: 1, 6: 1, 7: 1, 8: 1, 11: 1, 12: 1, 13: 3, 14: 2, 15: 1, 16: 1, 17: 2, 18: 1, 19: 2, 20: 3, 21: 1, 22: 1, 23: 2}
 
 KRYLOV = {"bicgstab": 0, "gmres": 1}

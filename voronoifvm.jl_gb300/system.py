@@ -257,11 +257,24 @@ class System:
     only -- what the reference's sparse storage holds."""
 
     def __init__(self, grid: Grid, physics: Physics, species: Optional[Sequence[int]] = None,
-                 is_linear: bool = False, assembly: str = "edgewise", unknown_storage: str = "dense"):
+                 is_linear: bool = False, assembly: str = "edgewise", unknown_storage: str = "dense",
+                 matrixtype: str = "sparse", valuetype=float, nparams: Optional[int] = None):
         if assembly not in ("edgewise", "cellwise"):
             raise ValueError("assembly must be :edgewise or :cellwise")
         if unknown_storage not in ("dense", "sparse"):
             raise ValueError("unknown_storage must be :dense or :sparse")
+        # matrixtype (src/vfvm_system.jl:215-261): the reference's :banded and
+        # :tridiagonal choices for 1D select its direct solver; the device keeps
+        # one block-sparse matrix and its Krylov solve for every choice
+        if matrixtype not in ("sparse", "banded", "tridiagonal", "default", "auto"):
+            raise ValueError("matrixtype must be :sparse, :banded, :tridiagonal or :default")
+        if valuetype not in (float, np.float64):
+            raise ValueError("the device computes in Float64 (valuetype = Float64)")
+        npd = L.physics_npd(physics.physics_id)
+        if nparams is not None and int(nparams) != npd:
+            raise ValueError(f"physics {physics.kind!r} has {npd} differentiable parameter(s), not {nparams}")
+        self.matrixtype = matrixtype
+        self.nparams = npd
         self.grid = grid
         self.physics = physics
         self.nspec = L.PHYSICS_NSPEC[physics.physics_id]
