@@ -94,6 +94,8 @@ extern "C" {
                                          reference's pluto-examples/outflow.jl: Darcy flux, Scharfetter-Gummel
                                          transport, boutflow on region G_out);
                                          params: k, v_in, c_in, D, G_in, G_out */
+#define VFVM_PHYS_EX210 24            /* Example210 two-species linear reaction-diffusion with a Gaussian source,
+                                         storage u, no-flux boundary; params: eps, k */
 
 /* linear solver / preconditioner / precision selectors */
 #define VFVM_KRYLOV_BICGSTAB 0

@@ -42,7 +42,7 @@ PHYS = {
     "ex105": 1, "ex106": 2, "ex110": 3, "ex160": 4, "ex207": 5, "ex301": 6, "ex440": 7,
     "laplace_dirichlet": 8, "nlpoisson": 11, "porous": 12, "bipolar": 13, "rd2": 14,
     "kappa_exp": 15, "surface_heat": 16, "boundary_species": 17, "edge_reaction": 18, "joule_heat": 19,
-    "ex161": 20, "testfunction": 21, "ex430": 22, "outflow": 23,
+    "ex161": 20, "testfunction": 21, "ex430": 22, "outflow": 23, "ex210": 24,
 }
 
 

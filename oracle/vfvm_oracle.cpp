@@ -573,6 +573,29 @@ struct PhysOutflow : OBase {
   }
 };
 
+// examples/Example210_NonlinearPoisson2D_Reaction.jl:24-46: two species,
+// flux eps (u_K - u_L) each, reaction k (u1 - u2) / k (u2 - u1), source
+// exp(-20 ((x-1/2)^2 + (y-1/2)^2)) for species 1, storage u.
+struct PhysEx210 : OBase {
+  static const int NS = 2;
+  static const bool has_reaction = true, has_storage = true, has_source = true, has_breaction = false;
+  double eps, k;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
+    f[0] = eps * (uK[0] - uL[0]);
+    f[1] = eps * (uK[1] - uL[1]);
+  }
+  template <class T> void reaction(T* f, const T* u, const NodeInfo&) const {
+    f[0] = k * (u[0] - u[1]);
+    f[1] = k * (u[1] - u[0]);
+  }
+  template <class T> void storage(T* f, const T* u, const NodeInfo&) const { f[0] = u[0]; f[1] = u[1]; }
+  void source(double* f, const NodeInfo& n) const {
+    const double x1 = n.x[0] - 0.5, x2 = n.x[1] - 0.5;
+    f[0] = std::exp(-20.0 * (x1 * x1 + x2 * x2));
+  }
+  template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
+};
+
 // The physics of TestFunctionFactory (src/vfvm_testfunctions.jl:38-50): flux
 // u_K - u_L, storage u; Dirichlet data through the legacy boundary factors.
 struct PhysTestFunction : OBase {
@@ -1368,6 +1391,7 @@ int dispatch(const Oracle& o, F&& fn) {
     }
     case 21: { PhysTestFunction ph; return fn(ph); }
     case 22: { PhysEx430T<double> ph; ph.p = P(0); return fn(ph); }
+    case 24: { PhysEx210 ph; ph.eps = P(0); ph.k = P(1); return fn(ph); }
     case 23: {
       PhysOutflow ph;
       ph.k = P(0); ph.v_in = P(1); ph.c_in = P(2); ph.D = P(3); ph.gin = (int)P(4); ph.gout = (int)P(5);
@@ -1382,7 +1406,7 @@ int dispatch(const Oracle& o, F&& fn) {
 
 int nspec_of(int phys) {
   switch (phys) {
-    case 3: case 4: case 14: case 17: case 19: case 23: return 2;
+    case 3: case 4: case 14: case 17: case 19: case 23: case 24: return 2;
     case 13: case 20: return 3;
     case 1: case 2: case 5: case 6: case 7: case 8: case 11: case 12: case 15: case 16: case 18: case 21: case 22: return 1;
   }

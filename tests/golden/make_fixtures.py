@@ -30,6 +30,7 @@ EXAMPLES = {
     "Example160_UnipolarDriftDiffusion1D": r"evolval\s*=\s*([-0-9.e]+)",
     "Example161_BipolarDriftDiffusionCurrent": r"testval\s*=\s*([-0-9.e]+)",
     "Example207_NonlinearPoisson2D": r"testval\s*=\s*([-0-9.e]+)",
+    "Example210_NonlinearPoisson2D_Reaction": r"testval\s*=\s*([-0-9.e]+)",
     "Example301_Laplace3D": r"testval\s*=\s*([-0-9.e]+)",
     "Example430_ParameterDerivativesStationary": r"testval\s*=\s*([-0-9.e]+)",
     "Example440_ParallelState": r"testval\s*=\s*([-0-9.e]+)",

@@ -286,3 +286,20 @@ def test_convergence_error(vfvm):
     sys = vfvm.System(vfvm.simplexgrid(lin(16), lin(16)), vfvm.Physics("nlpoisson"))
     with pytest.raises(vfvm.ConvergenceError):
         vfvm.solve(sys, inival=0.0, maxiters=1)
+
+
+@pytest.mark.parametrize("assembly", ["edgewise", "cellwise"])
+@pytest.mark.parametrize("storage", ["dense", "sparse"])
+def test_example210_two_species_transient(vfvm, testvals, assembly, storage):
+    """examples/Example210_NonlinearPoisson2D_Reaction.jl: 100 implicit Euler
+    steps of 0.01 on the device (step control on the device), sum of the
+    last solution against the reference's testval, all four of its runtests
+    combinations (:92-99)."""
+    X = np.array([i / 10 for i in range(11)])
+    sys = vfvm.System(vfvm.simplexgrid(X, X), vfvm.Physics("ex210", [1e-2, 1.0]), species=[1, 2],
+                      assembly=assembly, unknown_storage=storage)
+    control = vfvm.SolverControl(Δt=0.01, Δt_min=0.01, Δt_max=0.01, Δu_opt=1e5, reltol_linear=1e-10,
+                                 maxiters_linear=400)
+    tsol = vfvm.solve(sys, inival=0.0, times=[0.0, 1.0], control=control)
+    assert float(np.sum(tsol.u[-1])) == pytest.approx(testvals["Example210_NonlinearPoisson2D_Reaction"]["value"],
+                                                      rel=RTOL)

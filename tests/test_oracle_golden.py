@@ -205,3 +205,22 @@ def test_oracle_parameter_derivatives_vs_differences(vfvm, oracle):
     assert np.allclose(d[~dirichlet], fd[~dirichlet], rtol=1e-6, atol=1e-8)
     big = np.abs(d) > 1e20
     assert big.any() and np.allclose(d[big], fd[big], rtol=1e-6)
+
+
+def ex210_grid(vfvm):
+    X = np.array([i / 10 for i in range(11)])  # range(0, 1, length = 11)
+    return vfvm.simplexgrid(X, X)
+
+
+@pytest.mark.parametrize("assembly", ["edgewise", "cellwise"])
+def test_example210_transient(vfvm, oracle, testvals, assembly):
+    """Example210 (runtests :92-99): two-species reaction-diffusion, 100
+    implicit Euler steps of 0.01 (Δt_min = Δt_max = Δt, Δu_opt = 1e5)."""
+    g = ex210_grid(vfvm)
+    osys = oracle.OracleSystem(g, "ex210", [1e-2, 1.0], assembly=assembly)
+    c = oracle.Control()
+    c.Δt = c.Δt_min = c.Δt_max = 0.01
+    c.Δu_opt = 1e5
+    times, sols, _ = oracle.solve_transient(osys, np.zeros(2 * g.nnodes), [0.0, 1.0], c)
+    ref = testvals["Example210_NonlinearPoisson2D_Reaction"]["value"]
+    assert float(np.sum(sols[-1])) == pytest.approx(ref, rel=RTOL)

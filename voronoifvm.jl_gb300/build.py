@@ -34,7 +34,8 @@ INST_SOURCE = "vfvm_persist_inst.cu"
 INST_PHYSICS = ["PhysEx105", "PhysEx106", "PhysEx110", "PhysEx160", "PhysEx207", "PhysEx301", "PhysEx440",
                 "PhysLaplaceDir", "PhysNLPoisson", "PhysPorous", "PhysBipolar", "PhysRD2", "PhysKappaExp",
                 "PhysSurfaceHeat", "PhysBoundarySpecies", "PhysEdgeReaction", "PhysJouleHeat",
-                "PhysEx161", "PhysTestFunction", "PhysEx430", "PhysOutflow"]
+                "PhysEx161", "PhysTestFunction", "PhysEx430", "PhysOutflow",
+                "PhysEx210"]
 
 
 def sources():

@@ -525,6 +525,30 @@ struct PhysOutflow : PhysBase {
   }
 };
 
+// examples/Example210_NonlinearPoisson2D_Reaction.jl:24-46: two species with
+// flux eps (u_K - u_L), reaction k (u1 - u2) and k (u2 - u1), source
+// exp(-20 ((x-1/2)^2 + (y-1/2)^2)) for species 1, storage u; no-flux boundary.
+// params: eps, k
+struct PhysEx210 : PhysBase {
+  static constexpr int NS = 2;
+  static constexpr bool has_reaction = true, has_storage = true, has_source = true;
+  double eps, k;
+  VFVM_HD void load(const double* p) { eps = p[0]; k = p[1]; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const {
+    f[0] = (uK[0] - uL[0]) * eps;
+    f[1] = (uK[1] - uL[1]) * eps;
+  }
+  template <class T> VFVM_HD void reaction(T* f, const T* u, const NodeItem&) const {
+    f[0] = (u[0] - u[1]) * k;
+    f[1] = (u[1] - u[0]) * k;
+  }
+  template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const { f[0] = u[0]; f[1] = u[1]; }
+  VFVM_HD void source(double* f, const NodeItem& n) const {
+    const double x1 = n.x[0] - 0.5, x2 = n.x[1] - 0.5;
+    f[0] = ::exp(-20.0 * (x1 * x1 + x2 * x2));
+  }
+};
+
 inline int physics_nspec(int id) {
   switch (id) {
     case VFVM_PHYS_EX105: case VFVM_PHYS_EX106: case VFVM_PHYS_EX207: case VFVM_PHYS_EX301:
@@ -532,7 +556,7 @@ inline int physics_nspec(int id) {
     case VFVM_PHYS_POROUS: case VFVM_PHYS_KAPPA_EXP: case VFVM_PHYS_SURFACE_HEAT:
     case VFVM_PHYS_EDGE_REACTION: case VFVM_PHYS_TESTFUNCTION: case VFVM_PHYS_EX430: return 1;
     case VFVM_PHYS_EX110: case VFVM_PHYS_EX160: case VFVM_PHYS_RD2: case VFVM_PHYS_BOUNDARY_SPECIES:
-    case VFVM_PHYS_JOULE_HEAT: case VFVM_PHYS_OUTFLOW: return 2;
+    case VFVM_PHYS_JOULE_HEAT: case VFVM_PHYS_OUTFLOW: case VFVM_PHYS_EX210: return 2;
     case VFVM_PHYS_BIPOLAR: case VFVM_PHYS_EX161: return 3;
   }
   return 0;
@@ -551,6 +575,7 @@ inline int physics_nparams(int id) {
     case VFVM_PHYS_EX161: return 14;
     case VFVM_PHYS_EX430: return 1;
     case VFVM_PHYS_OUTFLOW: return 6;
+    case VFVM_PHYS_EX210: return 2;
   }
   return 0;
 }
@@ -581,6 +606,7 @@ int dispatch_physics(int id, Fn&& fn) {
     case VFVM_PHYS_TESTFUNCTION: return fn(PhysTestFunction{});
     case VFVM_PHYS_EX430: return fn(PhysEx430{});
     case VFVM_PHYS_OUTFLOW: return fn(PhysOutflow{});
+    case VFVM_PHYS_EX210: return fn(PhysEx210{});
   }
   return VFVM_ERR_INPUT;
 }
