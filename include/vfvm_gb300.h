@@ -96,6 +96,17 @@ extern "C" {
                                          params: k, v_in, c_in, D, G_in, G_out */
 #define VFVM_PHYS_EX210 24            /* Example210 two-species linear reaction-diffusion with a Gaussian source,
                                          storage u, no-flux boundary; params: eps, k */
+#define VFVM_PHYS_EX102 25            /* Example102 stationary convection-diffusion, velocity v along the first
+                                         coordinate; params: D, v, flux (0 exponential, 1 upwind, 2 central) */
+#define VFVM_PHYS_EX107 26            /* Example107 nonlinear storage (eps + u)^(1/m), flux u_K - u_L;
+                                         params: m, eps */
+#define VFVM_PHYS_EX115 27            /* Example115 heterogeneous catalysis: bulk species A, B, boundary species
+                                         C on region iCat (mass-action breaction, bstorage);
+                                         params: D_A, D_B, kp_AC, km_AC, kp_BC, km_BC, S, iCat */
+#define VFVM_PHYS_EX215 28            /* Example215 two species, flux eps, storage u, boundary reaction
+                                         k (u1 - u2) on boundary region 2; params: eps, k */
+#define VFVM_PHYS_EX220 29            /* Example220 bulk species 1, 2 and boundary species 3 on region 2
+                                         (breaction, bstorage), Gaussian source; params: k, eps */
 
 /* linear solver / preconditioner / precision selectors */
 #define VFVM_KRYLOV_BICGSTAB 0

@@ -43,6 +43,7 @@ PHYS = {
     "laplace_dirichlet": 8, "nlpoisson": 11, "porous": 12, "bipolar": 13, "rd2": 14,
     "kappa_exp": 15, "surface_heat": 16, "boundary_species": 17, "edge_reaction": 18, "joule_heat": 19,
     "ex161": 20, "testfunction": 21, "ex430": 22, "outflow": 23, "ex210": 24,
+    "ex102": 25, "ex107": 26, "ex115": 27, "ex215": 28, "ex220": 29,
 }
 
 

@@ -596,6 +596,124 @@ struct PhysEx210 : OBase {
   template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
 };
 
+// examples/Example102_StationaryConvectionDiffusion1D.jl:40-78: the example's
+// exponential (mode 0), upwind (1) and central (2) fluxes with vh =
+// project(edge, v) (src/vfvm_geometryitems.jl:634-640) and its own
+// bernoulli(x) = x / (exp(x) - 1), 1 where |x| < nextfloat(eps).
+struct PhysEx102 : OBase {
+  static const int NS = 1;
+  static const bool has_reaction = false, has_storage = false, has_source = false, has_breaction = false;
+  double D, v; int mode;
+  static double bernoulli(double x) {
+    if (std::fabs(x) < std::nextafter(std::numeric_limits<double>::epsilon(), 1.0)) return 1.0;
+    return x / (std::exp(x) - 1.0);
+  }
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo& e) const {
+    const double vh = (e.xL[0] - e.xK[0]) * v;
+    if (mode == 0) {
+      const double Bplus = D * bernoulli(vh / D), Bminus = D * bernoulli(-vh / D);
+      f[0] = Bminus * uK[0] - Bplus * uL[0];
+    } else if (mode == 1) {
+      const T fdiff = D * (uK[0] - uL[0]);
+      f[0] = vh > 0 ? fdiff + vh * uK[0] : fdiff + vh * uL[0];
+    } else {
+      f[0] = D * (uK[0] - uL[0]) + vh * (uK[0] + uL[0]) / 2.0;
+    }
+  }
+  template <class T> void reaction(T*, const T*, const NodeInfo&) const {}
+  template <class T> void storage(T*, const T*, const NodeInfo&) const {}
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
+};
+
+// examples/Example107_NonlinearStorage1D.jl:44-64: flux u_K - u_L, storage (eps + u)^(1/m).
+struct PhysEx107 : OBase {
+  static const int NS = 1;
+  static const bool has_reaction = false, has_storage = true, has_source = false, has_breaction = false;
+  double m, eps;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = uK[0] - uL[0]; }
+  template <class T> void storage(T* f, const T* u, const NodeInfo&) const { f[0] = pow(eps + u[0], 1.0 / m); }
+  template <class T> void reaction(T*, const T*, const NodeInfo&) const {}
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
+};
+
+// examples/Example115_HeterogeneousCatalysis1D.jl:113-176: A, B in the bulk,
+// C on boundary region iCat; R_AC, R_BC mass-action rates with the free-site
+// factor (1 - u_C); breaction S R_AC, S R_BC, -R_BC - R_AC; bstorage u_C.
+struct PhysEx115 : OBase {
+  static const int NS = 3;
+  static const bool has_reaction = false, has_storage = true, has_source = true, has_breaction = true;
+  static const bool has_bstorage = true;
+  double D_A, D_B, kp_AC, km_AC, kp_BC, km_BC, S; int iCat;
+  template <class T> T R_AC(const T& uA, const T& uC) const { return kp_AC * uA * (1.0 - uC) - km_AC * uC; }
+  template <class T> T R_BC(const T& uB, const T& uC) const { return kp_BC * uB * (1.0 - uC) - km_BC * uC; }
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
+    f[0] = D_A * (uK[0] - uL[0]);
+    f[1] = D_B * (uK[1] - uL[1]);
+  }
+  template <class T> void storage(T* f, const T* u, const NodeInfo&) const { f[0] = u[0]; f[1] = u[1]; }
+  template <class T> void reaction(T*, const T*, const NodeInfo&) const {}
+  void source(double* f, const NodeInfo& n) const { double x1 = n.x[0] - 0.5; f[0] = std::exp(-100.0 * (x1 * x1)); }
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const {
+    if (b.region == iCat) {
+      f[0] = S * R_AC(u[0], u[2]);
+      f[1] = S * R_BC(u[1], u[2]);
+      f[2] = -R_BC(u[1], u[2]) - R_AC(u[0], u[2]);
+    }
+  }
+  template <class T> void bstorage(T* f, const T* u, BNodeInfo& b) const { if (b.region == iCat) f[2] = u[2]; }
+};
+
+// examples/Example215_NonlinearPoisson2D_BoundaryReaction.jl:27-50: two
+// species, flux eps, storage u, breaction k_react (u1 - u2) / (u2 - u1) on region 2.
+struct PhysEx215 : OBase {
+  static const int NS = 2;
+  static const bool has_reaction = false, has_storage = true, has_source = false, has_breaction = true;
+  double eps, k_react;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
+    f[0] = eps * (uK[0] - uL[0]);
+    f[1] = eps * (uK[1] - uL[1]);
+  }
+  template <class T> void storage(T* f, const T* u, const NodeInfo&) const { f[0] = u[0]; f[1] = u[1]; }
+  template <class T> void reaction(T*, const T*, const NodeInfo&) const {}
+  void source(double*, const NodeInfo&) const {}
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const {
+    if (b.region == 2) {
+      f[0] = k_react * (u[0] - u[1]);
+      f[1] = k_react * (u[1] - u[0]);
+    }
+  }
+};
+
+// examples/Example220_NonlinearPoisson2D_BoundarySpecies.jl:23-57: bulk
+// species 1, 2 and boundary species 3 on region 2 (bstorage u3, breaction
+// k (u1 - u3), k (u3 - u1) + k (u3 - u2), k (u2 - u3)); source for species 1.
+struct PhysEx220 : OBase {
+  static const int NS = 3;
+  static const bool has_reaction = false, has_storage = true, has_source = true, has_breaction = true;
+  static const bool has_bstorage = true;
+  double k, eps;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const {
+    f[0] = eps * (uK[0] - uL[0]);
+    f[1] = eps * (uK[1] - uL[1]);
+  }
+  template <class T> void storage(T* f, const T* u, const NodeInfo&) const { f[0] = u[0]; f[1] = u[1]; }
+  template <class T> void reaction(T*, const T*, const NodeInfo&) const {}
+  void source(double* f, const NodeInfo& n) const {
+    double x1 = n.x[0] - 0.5, x2 = n.x[1] - 0.5;
+    f[0] = std::exp(-20.0 * (x1 * x1 + x2 * x2));
+  }
+  template <class T> void breaction(T* f, const T* u, BNodeInfo& b) const {
+    if (b.region == 2) {
+      f[0] = k * (u[0] - u[2]);
+      f[2] = k * (u[2] - u[0]) + k * (u[2] - u[1]);
+      f[1] = k * (u[1] - u[2]);
+    }
+  }
+  template <class T> void bstorage(T* f, const T* u, BNodeInfo& b) const { if (b.region == 2) f[2] = u[2]; }
+};
+
 // The physics of TestFunctionFactory (src/vfvm_testfunctions.jl:38-50): flux
 // u_K - u_L, storage u; Dirichlet data through the legacy boundary factors.
 struct PhysTestFunction : OBase {
@@ -1392,6 +1510,16 @@ int dispatch(const Oracle& o, F&& fn) {
     case 21: { PhysTestFunction ph; return fn(ph); }
     case 22: { PhysEx430T<double> ph; ph.p = P(0); return fn(ph); }
     case 24: { PhysEx210 ph; ph.eps = P(0); ph.k = P(1); return fn(ph); }
+    case 25: { PhysEx102 ph; ph.D = P(0); ph.v = P(1); ph.mode = (int)P(2); return fn(ph); }
+    case 26: { PhysEx107 ph; ph.m = P(0); ph.eps = P(1); return fn(ph); }
+    case 27: {
+      PhysEx115 ph;
+      ph.D_A = P(0); ph.D_B = P(1); ph.kp_AC = P(2); ph.km_AC = P(3); ph.kp_BC = P(4); ph.km_BC = P(5); ph.S = P(6);
+      ph.iCat = (int)P(7);
+      return fn(ph);
+    }
+    case 28: { PhysEx215 ph; ph.eps = P(0); ph.k_react = P(1); return fn(ph); }
+    case 29: { PhysEx220 ph; ph.k = P(0); ph.eps = P(1); return fn(ph); }
     case 23: {
       PhysOutflow ph;
       ph.k = P(0); ph.v_in = P(1); ph.c_in = P(2); ph.D = P(3); ph.gin = (int)P(4); ph.gout = (int)P(5);
@@ -1406,9 +1534,10 @@ int dispatch(const Oracle& o, F&& fn) {
 
 int nspec_of(int phys) {
   switch (phys) {
-    case 3: case 4: case 14: case 17: case 19: case 23: case 24: return 2;
-    case 13: case 20: return 3;
-    case 1: case 2: case 5: case 6: case 7: case 8: case 11: case 12: case 15: case 16: case 18: case 21: case 22: return 1;
+    case 3: case 4: case 14: case 17: case 19: case 23: case 24: case 28: return 2;
+    case 13: case 20: case 27: case 29: return 3;
+    case 1: case 2: case 5: case 6: case 7: case 8: case 11: case 12: case 15: case 16: case 18: case 21: case 22:
+    case 25: case 26: return 1;
   }
   return 0;
 }

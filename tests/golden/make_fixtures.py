@@ -24,13 +24,19 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF = None  # the reference checkout, the required command-line argument
 
 EXAMPLES = {
+    "Example102_StationaryConvectionDiffusion1D": r"testval\s*=\s*([-0-9.e]+)",
     "Example105_NonlinearPoisson1D": r"testval\s*=\s*([-0-9.e]+)",
+    "Example107_NonlinearStorage1D": r"testval\s*=\s*([-0-9.e]+)",
     "Example106_NonlinearDiffusion1D": r"testval\s*=\s*([-0-9.e]+)",
     "Example110_ReactionDiffusion1D_TwoSpecies": r"testval\s*=\s*([-0-9.e]+)",
+    "Example115_HeterogeneousCatalysis1D": r"testval\s*=\s*([-0-9.e]+)",
     "Example160_UnipolarDriftDiffusion1D": r"evolval\s*=\s*([-0-9.e]+)",
     "Example161_BipolarDriftDiffusionCurrent": r"testval\s*=\s*([-0-9.e]+)",
     "Example207_NonlinearPoisson2D": r"testval\s*=\s*([-0-9.e]+)",
     "Example210_NonlinearPoisson2D_Reaction": r"testval\s*=\s*([-0-9.e]+)",
+    "Example215_NonlinearPoisson2D_BoundaryReaction": r"testval\s*=\s*([-0-9.e]+)",
+    # the value is inline in runtests: @test main(; unknown_storage = :sparse) ≈ value
+    "Example220_NonlinearPoisson2D_BoundarySpecies": r"≈\s*([-0-9.e]+)",
     "Example301_Laplace3D": r"testval\s*=\s*([-0-9.e]+)",
     "Example430_ParameterDerivativesStationary": r"testval\s*=\s*([-0-9.e]+)",
     "Example440_ParallelState": r"testval\s*=\s*([-0-9.e]+)",

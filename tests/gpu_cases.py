@@ -77,6 +77,14 @@ def case(vfvm, name, seed=0):
     elif name == "outflow2d":  # pluto-examples/outflow.jl: outflow region 5 on part of the right side
         g = vfvm.bfacemask(sg(lin(10), lin(10)), [1, 0.3], [1, 0.7], 5)
         kind, params = "outflow", [1.0, 1.0, 0.5, 1.0, 4, 5]
+    elif name.startswith("ex102_"):  # Example102's three fluxes; the upwind case with v < 0 (the other branch)
+        mode = {"ex102_exp": 0, "ex102_upwind": 1, "ex102_central": 2}[name]
+        g, kind, params = sg(lin(10)), "ex102", [0.01, -1.0 if mode == 1 else 1.0, mode]
+        legacy = (np.full((1, 2), 1e30), np.array([[0.0, 1.0]]))
+    elif name == "ex107":  # Example107: nonlinear storage (1e-10 + u)^(1/2)
+        g, kind, params, tstep = sg(lin(20)), "ex107", [2.0, 1e-10], 1e-3
+    elif name == "ex215":  # Example215: boundary reaction on region 2
+        g, kind, params, tstep = sg(lin(8), lin(8)), "ex215", [1e-2, 1.0], 1e-2
     elif name == "laplace_dirichlet":
         g, kind, params = sg(lin(9)), "laplace_dirichlet", []
     else:
@@ -99,4 +107,5 @@ def random_state(c, nspec, rng):
 
 NAMES = ["nlpoisson", "porous", "bipolar", "rd2", "kappa_exp", "ex105", "ex106", "ex110", "ex160", "ex207",
          "ex301", "ex440", "laplace_dirichlet", "kappa_unstructured", "surface_heat2d", "surface_heat3d",
-         "edge_reaction2d", "edge_reaction3d", "joule_heat", "ex161", "ex430", "outflow2d"]
+         "edge_reaction2d", "edge_reaction3d", "joule_heat", "ex161", "ex430", "outflow2d", "ex102_exp",
+         "ex102_upwind", "ex102_central", "ex107", "ex215"]

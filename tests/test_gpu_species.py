@@ -54,10 +54,20 @@ def species_case(vfvm, name):
     if name == "ex110_two_regions":
         g = two_regions(vfvm, vfvm.simplexgrid(lin(16)))
         return g, "ex110", [0.5, 0.5], np.array([[1, 1], [0, 1]]), np.zeros((2, 2), dtype=int), 1e-2
+    if name == "ex115":  # Example115: boundary species C on the catalytic end (region 1), B = 0 at the other
+        g = vfvm.simplexgrid(lin(10))
+        bs = np.zeros((3, 2), dtype=int)
+        bs[2, 0] = 1
+        return g, "ex115", [1.0, 1.0e-2, 100.0, 1.0, 0.1, 1.0, 0.01, 1], np.array([[1], [1], [0]]), bs, 1e-2
+    if name == "ex220":  # Example220: boundary species 3 on region 2 of a 2D grid
+        g = vfvm.simplexgrid(lin(8), lin(8))
+        bs = np.zeros((3, 4), dtype=int)
+        bs[2, 1] = 1
+        return g, "ex220", [1.0, 1.0e-2], np.array([[1], [1], [0]]), bs, 1e-2
     raise KeyError(name)
 
 
-NAMES = ["ex230", "ex230_line", "rd2_two_regions", "ex110_two_regions"]
+NAMES = ["ex230", "ex230_line", "rd2_two_regions", "ex110_two_regions", "ex115", "ex220"]
 
 
 def make_pair(vfvm, oracle, name, assembly="edgewise", unknown_storage="dense"):

@@ -224,3 +224,131 @@ def test_example210_transient(vfvm, oracle, testvals, assembly):
     times, sols, _ = oracle.solve_transient(osys, np.zeros(2 * g.nnodes), [0.0, 1.0], c)
     ref = testvals["Example210_NonlinearPoisson2D_Reaction"]["value"]
     assert float(np.sum(sols[-1])) == pytest.approx(ref, rel=RTOL)
+
+
+def test_example102_three_fluxes(vfvm, oracle, testvals):
+    """Example102 (runtests :138-141): the exponential, upwind and central
+    fluxes on 0:0.1:1, u(0) = 0, u(1) = 1, from 0.5; the sum of the three
+    solutions."""
+    g = vfvm.simplexgrid(lin(10))
+    bf = np.full((1, 2), 1e30)
+    bv = np.array([[0.0, 1.0]])
+    total = 0.0
+    for mode in (0, 1, 2):
+        s = oracle.OracleSystem(g, "ex102", [0.01, 1.0, mode], bfactors=bf, bvalues=bv, assembly="cellwise")
+        u, _ = oracle.solve_step(s, np.full(g.nnodes, 0.5), oracle.Control())
+        total += float(u.sum())
+    assert total == pytest.approx(testvals["Example102_StationaryConvectionDiffusion1D"]["value"], rel=RTOL)
+
+
+@pytest.mark.parametrize("assembly", ["edgewise", "cellwise"])
+def test_example107_nonlinear_storage(vfvm, oracle, testvals, assembly):
+    """Example107 (runtests :118-124): storage (1e-10 + u)^(1/2) from the
+    Barenblatt profile at t = 0.001 to t = 0.01 with the adaptive step control
+    (Δu_opt = 0.1, force_first_step), rtol 1e-5 as in the example."""
+    X = lin(20, -1.0, 1.0)
+    s = oracle.OracleSystem(vfvm.simplexgrid(X), "ex107", [2.0, 1e-10], assembly=assembly)
+    c = oracle.Control()
+    c.Δu_opt = 0.1
+    c.force_first_step = True
+    inival = np.array([barenblatt(x, 0.001, 2.0) ** 2.0 for x in X])
+    _, sols, _ = oracle.solve_transient(s, inival, [0.001, 0.01], c)
+    assert float(sols[-1].sum()) == pytest.approx(testvals["Example107_NonlinearStorage1D"]["value"], rel=1e-5)
+
+
+def ex115_system(vfvm, oracle_or_none, switchbc, assembly="edgewise"):
+    """Grid, parameters and species tables of Example115 (main, :82-170)."""
+    X = lin(10)
+    icat, ibulk, inodecat = (2, 1, X.size - 1) if switchbc else (1, 2, 0)
+    params = [1.0, 1.0e-2, 100.0, 1.0, 0.1, 1.0, 0.01, icat]
+    rs = np.array([[1], [1], [0]])
+    bs = np.zeros((3, 2), dtype=int)
+    bs[2, icat - 1] = 1
+    bf = np.zeros((3, 2)); bv = np.zeros((3, 2))
+    bf[1, ibulk - 1] = 1e30          # boundary_dirichlet!(sys, iB, iBulk, 0.0)
+    return X, params, rs, bs, bf, bv, inodecat
+
+
+@pytest.mark.parametrize("assembly", ["edgewise", "cellwise"])
+@pytest.mark.parametrize("switchbc", [False, True])
+def test_example115_heterogeneous_catalysis(vfvm, oracle, testvals, assembly, switchbc):
+    """Example115 (runtests :223-233): boundary species C on the catalytic end
+    (mass-action breaction, bstorage), B = 0 at the other end, 100 fixed steps
+    of 0.01; u_C at the catalytic node at t = 1, rtol 1e-12 as in the example."""
+    X, params, rs, bs, bf, bv, inodecat = ex115_system(vfvm, oracle, switchbc)
+    s = oracle.OracleSystem(vfvm.simplexgrid(X), "ex115", params, bfactors=bf, bvalues=bv, assembly=assembly,
+                            region_species=rs, bregion_species=bs)
+    c = oracle.fixed_timesteps(oracle.Control(), 0.01)
+    _, sols, _ = oracle.solve_transient(s, np.zeros(3 * X.size), [0.0, 1.0], c)
+    uc = sols[-1][3 * inodecat + 2]
+    assert uc == pytest.approx(testvals["Example115_HeterogeneousCatalysis1D"]["value"], rel=1e-12)
+
+
+def ex215_inival(g):
+    x, y = g.coord[0], g.coord[1]
+    U = np.zeros(2 * g.nnodes)
+    U[0::2] = np.exp(-5.0 * ((x - 0.5) ** 2 + (y - 0.5) ** 2))
+    return U
+
+
+def ex215_steps():
+    """The example's time loop (:69-75): tstep from 0.01, times 1.2 per step, until time >= 100."""
+    steps, time, tstep = [], 0.0, 0.01
+    while time < 100.0:
+        time = time + tstep
+        steps.append(tstep)
+        tstep *= 1.2
+    return steps
+
+
+@pytest.mark.parametrize("assembly", ["edgewise", "cellwise"])
+def test_example215_boundary_reaction(vfvm, oracle, testvals, assembly):
+    """Example215 (runtests :98-104): two species exchanged by a boundary
+    reaction on region 2, 42 growing implicit Euler steps; U[25] (species 1 of
+    node 13)."""
+    g = vfvm.simplexgrid(lin(10), lin(10))
+    s = oracle.OracleSystem(g, "ex215", [1.0e-2, 1.0], assembly=assembly)
+    U = ex215_inival(g)
+    for dt in ex215_steps():
+        U, _ = oracle.solve_step(s, U, oracle.Control(), 0.0, dt)
+    assert U[24] == pytest.approx(testvals["Example215_NonlinearPoisson2D_BoundaryReaction"]["value"], rel=RTOL)
+
+
+def ex220_tables():
+    rs = np.array([[1], [1], [0]])
+    bs = np.zeros((3, 4), dtype=int)
+    bs[2, 1] = 1
+    return rs, bs
+
+
+def ex220_steps():
+    """The example's time loop (:77-83): tstep 0.01 while time < 1."""
+    n, time = 0, 0.0
+    while time < 1.0:
+        time = time + 0.01
+        n += 1
+    return n
+
+
+def ex220_u5(g, U):
+    """U_bound[5]: species 3 on the fifth node of boundary region 2 (x = 1),
+    the subgrid's nodes in the order of their parent indices."""
+    r = np.flatnonzero(np.abs(g.coord[0] - 1.0) < 1e-14)
+    return U[3 * np.sort(r)[4] + 2]
+
+
+@pytest.mark.parametrize("assembly", ["edgewise", "cellwise"])
+def test_example220_boundary_species(vfvm, oracle, testvals, assembly):
+    """Example220 (runtests :100-104): bulk species 1, 2 and species 3 on
+    boundary region 2 (bstorage, breaction), 100 steps of 0.01 with Newton
+    reltol 1e-5; species 3 at the fifth node of region 2."""
+    g = vfvm.simplexgrid(lin(10), lin(10))
+    rs, bs = ex220_tables()
+    s = oracle.OracleSystem(g, "ex220", [1.0, 1.0e-2], assembly=assembly, region_species=rs, bregion_species=bs)
+    c = oracle.Control()
+    c.reltol = 1e-5
+    U = np.zeros(3 * g.nnodes)
+    for _ in range(ex220_steps()):
+        U, _ = oracle.solve_step(s, U, c, 0.0, 0.01)
+    assert ex220_u5(g, U) == pytest.approx(testvals["Example220_NonlinearPoisson2D_BoundarySpecies"]["value"],
+                                           rel=RTOL)

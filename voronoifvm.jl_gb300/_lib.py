@@ -23,7 +23,8 @@ PHYSICS_IDS = {
     "ex105": 1, "ex106": 2, "ex110": 3, "ex160": 4, "ex207": 5, "ex301": 6, "ex440": 7,
     "laplace_dirichlet": 8, "nlpoisson": 11, "porous": 12, "bipolar": 13, "rd2": 14, "kappa_exp": 15,
     "surface_heat": 16, "boundary_species": 17, "edge_reaction": 18, "joule_heat": 19, "ex161": 20,
-    "testfunction": 21, "ex430": 22, "outflow": 23, "ex210": 24,
+    "testfunction": 21, "ex430": 22, "outflow": 23, "ex210": 24, "ex102": 25, "ex107": 26, "ex115": 27,
+    "ex215": 28, "ex220": 29,
 }
 # physics whose first parameters carry derivatives (NPD in the device functor)
 PHYSICS_NPD = {22: 1}
@@ -33,7 +34,8 @@ def physics_npd(physics_id: int) -> int:
     return PHYSICS_NPD.get(physics_id, 0)
 
 
-PHYSICS_NSPEC = {1: 1, 2: 1, 3: 2, 4: 2, 5: 1, 6: 1, 7: 1, 8: 1, 11: 1, 12: 1, 13: 3, 14: 2, 15: 1, 16: 1, 17: 2, 18: 1, 19: 2, 20: 3, 21: 1, 22: 1, 23: 2, 24: 2}
+PHYSICS_NSPEC = {1: 1, 2: 1, 3: 2, 4: 2, 5: 1, 6: 1, 7: 1, 8: 1, 11: 1, 12: 1, 13: 3, 14: 2, 15: 1, 16: 1, 17: 2, 18: 1, 19: 2, 20: 3, 21: 1, 22: 1, 23: 2, 24: 2,
+                 25: 1, 26: 1, 27: 3, 28: 2, 29: 3}
 
 KRYLOV = {"bicgstab": 0, "gmres": 1}
 PRECON = {"jacobi": 0, "ilu0": 1, "block_ilu0": 2}

@@ -198,12 +198,14 @@ template <int N, typename P> VFVM_HD Dual<N, P> dmax(const Dual<N, P>& a, double
 VFVM_HD double sq(double a) { return a * a; }
 VFVM_HD double cube(double a) { return a * a * a; }
 VFVM_HD double dmax(double a, double b) { return a > b ? a : b; }
-// exp for physics callbacks that run on doubles as well as on duals (storage
+// exp and pow for physics callbacks that run on doubles as well as on duals (storage
 // is evaluated at the old values in plain doubles); a name of its own, since
-// plain-double overloads of exp in this namespace would collide with the
+// plain-double overloads of exp or pow in this namespace would collide with the
 // global ones where the namespace is imported
 VFVM_HD double vexp(double a) { return ::exp(a); }
 template <int N, typename P> VFVM_HD Dual<N, P> vexp(const Dual<N, P>& a) { return exp(a); }
+VFVM_HD double vpow(double a, double p) { return ::pow(a, p); }
+template <int N, typename P> VFVM_HD Dual<N, P> vpow(const Dual<N, P>& a, double p) { return pow(a, p); }
 
 // -----------------------------------------------------------------------------
 // Bernoulli function B(x) = x/(exp(x)-1) and B(-x), with the reference's

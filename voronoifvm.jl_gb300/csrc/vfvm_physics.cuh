@@ -549,15 +549,145 @@ struct PhysEx210 : PhysBase {
   }
 };
 
+// examples/Example102_StationaryConvectionDiffusion1D.jl:40-78: -(D u' - v u)' =
+// 0 with the example's three fluxes, vh = project(edge, v) = (x_L - x_K) v
+// (src/vfvm_geometryitems.jl:634-640, v along the first coordinate):
+// flux 0 exponential: D B(-vh/D) u_K - D B(vh/D) u_L with the example's own
+//   B(x) = x / (exp(x) - 1), B = 1 where |x| < nextfloat(eps);
+// flux 1 upwind: D (u_K - u_L) + vh u_K if vh > 0, else + vh u_L;
+// flux 2 central: D (u_K - u_L) + vh (u_K + u_L) / 2.
+// params: D, v, flux
+struct PhysEx102 : PhysBase {
+  static constexpr int NS = 1;
+  double D, v;
+  int mode;
+  VFVM_HD void load(const double* p) { D = p[0]; v = p[1]; mode = (int)p[2]; }
+  VFVM_HD static double bern(double x) {
+    return fabs(x) < 0x1.0000000000001p-52 ? 1.0 : x / (::exp(x) - 1.0);
+  }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem& e) const {
+    const double vh = (e.xL[0] - e.xK[0]) * v;
+    if (mode == 0) {
+      const double bplus = D * bern(vh / D), bminus = D * bern(-vh / D);
+      f[0] = uK[0] * bminus - uL[0] * bplus;
+    } else if (mode == 1) {
+      f[0] = (uK[0] - uL[0]) * D + (vh > 0.0 ? uK[0] : uL[0]) * vh;
+    } else {
+      f[0] = (uK[0] - uL[0]) * D + (uK[0] + uL[0]) * vh / 2.0;
+    }
+  }
+};
+
+// examples/Example107_NonlinearStorage1D.jl:44-64: flux u_K - u_L, storage
+// (eps + u)^(1/m).
+// params: m, eps
+struct PhysEx107 : PhysBase {
+  static constexpr int NS = 1;
+  static constexpr bool has_storage = true;
+  double m, eps;
+  VFVM_HD void load(const double* p) { m = p[0]; eps = p[1]; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const { f[0] = uK[0] - uL[0]; }
+  template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const { f[0] = vpow(u[0] + eps, 1.0 / m); }
+};
+
+// examples/Example115_HeterogeneousCatalysis1D.jl:113-176: species A, B in the
+// bulk (flux D_A, D_B; storage u; source exp(-100 (x - 1/2)^2) for A), species
+// C a boundary species on region iCat; there, with R_AC = kp_AC u_A (1 - u_C) -
+// km_AC u_C and R_BC = kp_BC u_B (1 - u_C) - km_BC u_C, the boundary reactions
+// S R_AC, S R_BC, -R_BC - R_AC and the boundary storage u_C.
+// params: D_A, D_B, kp_AC, km_AC, kp_BC, km_BC, S, iCat
+struct PhysEx115 : PhysBase {
+  static constexpr int NS = 3;
+  static constexpr bool has_storage = true, has_source = true, has_breaction = true, has_bstorage = true;
+  double DA, DB, kpAC, kmAC, kpBC, kmBC, S;
+  int icat;
+  VFVM_HD void load(const double* p) {
+    DA = p[0]; DB = p[1]; kpAC = p[2]; kmAC = p[3]; kpBC = p[4]; kmBC = p[5]; S = p[6]; icat = (int)p[7];
+  }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const {
+    f[0] = (uK[0] - uL[0]) * DA;
+    f[1] = (uK[1] - uL[1]) * DB;
+  }
+  template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const { f[0] = u[0]; f[1] = u[1]; }
+  VFVM_HD void source(double* f, const NodeItem& n) const {
+    const double x1 = n.x[0] - 0.5;
+    f[0] = ::exp(-100.0 * (x1 * x1));
+  }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const {
+    if (b.region != icat) return;
+    const T rac = kpAC * u[0] * (1.0 - u[2]) - kmAC * u[2];
+    const T rbc = kpBC * u[1] * (1.0 - u[2]) - kmBC * u[2];
+    f[0] = S * rac;
+    f[1] = S * rbc;
+    f[2] = -rbc - rac;
+  }
+  template <class T> VFVM_HD void bstorage(T* f, const T* u, const BNodeItem& b) const {
+    if (b.region == icat) f[2] = u[2];
+  }
+};
+
+// examples/Example215_NonlinearPoisson2D_BoundaryReaction.jl:27-50: two
+// species, flux eps (u_K - u_L), storage u, and on boundary region 2 the
+// reactions k (u1 - u2), k (u2 - u1).
+// params: eps, k
+struct PhysEx215 : PhysBase {
+  static constexpr int NS = 2;
+  static constexpr bool has_storage = true, has_breaction = true;
+  double eps, k;
+  VFVM_HD void load(const double* p) { eps = p[0]; k = p[1]; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const {
+    f[0] = (uK[0] - uL[0]) * eps;
+    f[1] = (uK[1] - uL[1]) * eps;
+  }
+  template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const { f[0] = u[0]; f[1] = u[1]; }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const {
+    if (b.region != 2) return;
+    f[0] = (u[0] - u[1]) * k;
+    f[1] = (u[1] - u[0]) * k;
+  }
+};
+
+// examples/Example220_NonlinearPoisson2D_BoundarySpecies.jl:23-57: bulk species
+// 1, 2 (flux eps (u_K - u_L), storage u, source exp(-20 ((x-1/2)^2 + (y-1/2)^2))
+// for species 1) and species 3 on boundary region 2 with the boundary storage u3
+// and the reactions k (u1 - u3), k (u3 - u1) + k (u3 - u2), k (u2 - u3) there.
+// params: k, eps
+struct PhysEx220 : PhysBase {
+  static constexpr int NS = 3;
+  static constexpr bool has_storage = true, has_source = true, has_breaction = true, has_bstorage = true;
+  double k, eps;
+  VFVM_HD void load(const double* p) { k = p[0]; eps = p[1]; }
+  static bool valid(int dim, const double*) { return dim >= 2; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const {
+    f[0] = (uK[0] - uL[0]) * eps;
+    f[1] = (uK[1] - uL[1]) * eps;
+  }
+  template <class T> VFVM_HD void storage(T* f, const T* u, const NodeItem&) const { f[0] = u[0]; f[1] = u[1]; }
+  VFVM_HD void source(double* f, const NodeItem& n) const {
+    const double x1 = n.x[0] - 0.5, x2 = n.x[1] - 0.5;
+    f[0] = ::exp(-20.0 * (x1 * x1 + x2 * x2));
+  }
+  template <class T> VFVM_HD void breaction(T* f, const T* u, const BNodeItem& b) const {
+    if (b.region != 2) return;
+    f[0] = (u[0] - u[2]) * k;
+    f[2] = (u[2] - u[0]) * k + (u[2] - u[1]) * k;
+    f[1] = (u[1] - u[2]) * k;
+  }
+  template <class T> VFVM_HD void bstorage(T* f, const T* u, const BNodeItem& b) const {
+    if (b.region == 2) f[2] = u[2];
+  }
+};
+
 inline int physics_nspec(int id) {
   switch (id) {
     case VFVM_PHYS_EX105: case VFVM_PHYS_EX106: case VFVM_PHYS_EX207: case VFVM_PHYS_EX301:
     case VFVM_PHYS_EX440: case VFVM_PHYS_LAPLACE_DIRICHLET: case VFVM_PHYS_NLPOISSON:
     case VFVM_PHYS_POROUS: case VFVM_PHYS_KAPPA_EXP: case VFVM_PHYS_SURFACE_HEAT:
-    case VFVM_PHYS_EDGE_REACTION: case VFVM_PHYS_TESTFUNCTION: case VFVM_PHYS_EX430: return 1;
+    case VFVM_PHYS_EDGE_REACTION: case VFVM_PHYS_TESTFUNCTION: case VFVM_PHYS_EX430: case VFVM_PHYS_EX102:
+    case VFVM_PHYS_EX107: return 1;
     case VFVM_PHYS_EX110: case VFVM_PHYS_EX160: case VFVM_PHYS_RD2: case VFVM_PHYS_BOUNDARY_SPECIES:
-    case VFVM_PHYS_JOULE_HEAT: case VFVM_PHYS_OUTFLOW: case VFVM_PHYS_EX210: return 2;
-    case VFVM_PHYS_BIPOLAR: case VFVM_PHYS_EX161: return 3;
+    case VFVM_PHYS_JOULE_HEAT: case VFVM_PHYS_OUTFLOW: case VFVM_PHYS_EX210: case VFVM_PHYS_EX215: return 2;
+    case VFVM_PHYS_BIPOLAR: case VFVM_PHYS_EX161: case VFVM_PHYS_EX115: case VFVM_PHYS_EX220: return 3;
   }
   return 0;
 }
@@ -576,6 +706,11 @@ inline int physics_nparams(int id) {
     case VFVM_PHYS_EX430: return 1;
     case VFVM_PHYS_OUTFLOW: return 6;
     case VFVM_PHYS_EX210: return 2;
+    case VFVM_PHYS_EX102: return 3;
+    case VFVM_PHYS_EX107: return 2;
+    case VFVM_PHYS_EX115: return 8;
+    case VFVM_PHYS_EX215: return 2;
+    case VFVM_PHYS_EX220: return 2;
   }
   return 0;
 }
@@ -607,6 +742,11 @@ int dispatch_physics(int id, Fn&& fn) {
     case VFVM_PHYS_EX430: return fn(PhysEx430{});
     case VFVM_PHYS_OUTFLOW: return fn(PhysOutflow{});
     case VFVM_PHYS_EX210: return fn(PhysEx210{});
+    case VFVM_PHYS_EX102: return fn(PhysEx102{});
+    case VFVM_PHYS_EX107: return fn(PhysEx107{});
+    case VFVM_PHYS_EX115: return fn(PhysEx115{});
+    case VFVM_PHYS_EX215: return fn(PhysEx215{});
+    case VFVM_PHYS_EX220: return fn(PhysEx220{});
   }
   return VFVM_ERR_INPUT;
 }
