@@ -21,8 +21,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from gpu_cases import lin
-from test_oracle_golden import barenblatt, ex115_system, ex215_inival, ex215_steps, ex220_steps, ex220_tables
+from test_oracle_golden import barenblatt, ex115_system, ex215_inival, ex215_steps, ex220_steps, ex220_tables, lin
 
 pytestmark = pytest.mark.gpu
 RTOL = math.sqrt(np.finfo(float).eps)

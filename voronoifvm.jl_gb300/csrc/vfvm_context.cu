@@ -235,6 +235,37 @@ void probe_bflux_t(const Ph& ph0, const double* params, int reg, std::vector<uin
   }
 }
 
+// Structural mask of the boundary-node terms (breaction, bstorage) on boundary
+// region reg: which partials d y_i / d u_j can be nonzero (NS x NS).  Per
+// region, since the reference creates an entry only where a term's partial is
+// nonzero (_addnz, src/vfvm_assembly.jl:318-407): a coupling that a physics
+// makes on one boundary region gives no entries at the nodes of the others.
+template <class Ph>
+void probe_bnode_t(const Ph& ph0, const double* params, int reg, std::vector<uint8_t>& out) {
+  constexpr int NS = Ph::NS;
+  Ph ph = ph0;
+  ph.load(params);
+  out.assign(NS * NS, 0);
+  if (!Ph::has_breaction && !Ph::has_bstorage) return;
+  std::mt19937_64 rng(2468);
+  std::uniform_real_distribution<double> U(0.1, 1.1), X(0.0, 1.0);
+  for (int sample = 0; sample < 6; ++sample) {
+    double x[3] = {X(rng), X(rng), X(rng)}, dv[NS];
+    BNodeItem bi{0, reg, x, 0.5, 0.5, 1.0, kDirichlet, dv};
+    Dual<NS> u[NS], yb[NS], sb[NS];
+    for (int i = 0; i < NS; ++i) {
+      u[i] = dseed<NS, double>(U(rng), i);
+      yb[i] = dconst<NS, double>(0);
+      sb[i] = dconst<NS, double>(0);
+    }
+    if (Ph::has_breaction) ph.breaction(yb, u, bi);
+    if (Ph::has_bstorage) ph.bstorage(sb, u, bi);
+    for (int i = 0; i < NS; ++i)
+      for (int j = 0; j < NS; ++j)
+        if (yb[i].d[j] != 0.0 || sb[i].d[j] != 0.0) out[i * NS + j] = 1;
+  }
+}
+
 // Dirichlet species of a boundary region according to breaction (the
 // dirichlet_value capture of _initialize_dirichlet!).
 template <class Ph>
@@ -605,6 +636,13 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
     p.resize(16, 0.0);
     dispatch_physics(c->phys, [&](auto phy) { probe_t(phy, p.data(), dim, cregs, bregs, nm, em, bm); return 0; });
   }
+  std::map<int, std::vector<uint8_t>> bnm_of_reg;  // boundary-node terms, per boundary region
+  {
+    std::vector<double> p(c->h_params);
+    p.resize(16, 0.0);
+    for (int reg : bregs)
+      dispatch_physics(c->phys, [&](auto phy) { probe_bnode_t(phy, p.data(), reg, bnm_of_reg[reg]); return 0; });
+  }
   std::vector<uint8_t> dir_dof((size_t)N * ns, 0);
   {
     std::vector<double> p(c->h_params);
@@ -678,7 +716,9 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
               on = (nm[i * ns + j] && node_items_allow(i, j)) ||
                    ((em[i * 2 * ns + j] || em[i * 2 * ns + ns + j]) && edges_allow(i, j));
               if (bnode) {
-                on = on || (bm[i * ns + j] && pair_in(kspec, i, j));
+                bool bterm = false;  // a boundary-node term of one of this node's boundary regions
+                for (int it = bn_ptr[k]; !bterm && it < bn_ptr[k + 1]; ++it) bterm = bnm_of_reg[bn_reg[it]][i * ns + j] != 0;
+                on = on || (bterm && pair_in(kspec, i, j));
                 if (i == j && legdiag[i]) on = true;
               }
               // a species the node does not carry: F += U - Uold, unit diagonal
