@@ -107,6 +107,8 @@ extern "C" {
                                          k (u1 - u2) on boundary region 2; params: eps, k */
 #define VFVM_PHYS_EX220 29            /* Example220 bulk species 1, 2 and boundary species 3 on region 2
                                          (breaction, bstorage), Gaussian source; params: k, eps */
+#define VFVM_PHYS_EX203 30            /* Example203 -div grad u = f (flux u_K - u_L, constant source f), for the
+                                         coordinate systems; params: f */
 
 /* linear solver / preconditioner / precision selectors */
 #define VFVM_KRYLOV_BICGSTAB 0
@@ -131,7 +133,15 @@ typedef struct vfvm_grid {
   const int32_t* cellregions;  /* ncells, 1-based */
   const int32_t* bfacenodes;   /* dim x nbfaces, column-major, 0-based */
   const int32_t* bfaceregions; /* nbfaces, 1-based */
+  int32_t coordsystem;         /* VFVM_COORD_*: the form factors (src/vfvm_formfactors.jl:12-332) */
 } vfvm_grid;
+
+/* coordinate systems (ExtendableGrids' CoordinateSystem, set by circular_symmetric! /
+   spherical_symmetric!): the node volumes and edge factors of the symmetric body */
+#define VFVM_COORD_CARTESIAN 0   /* any dimension */
+#define VFVM_COORD_POLAR1D 1     /* 1D, r: a disk or ring (circular_symmetric! on a 1D grid) */
+#define VFVM_COORD_SPHERICAL1D 2 /* 1D, r: a ball or shell (spherical_symmetric!) */
+#define VFVM_COORD_CYLINDRICAL2D 3 /* 2D, (r, z): a cylinder (circular_symmetric! on a 2D grid) */
 
 typedef struct vfvm_physics_desc {
   int32_t physics_id;

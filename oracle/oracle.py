@@ -37,13 +37,16 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 _lib = None
 
+# coordinate systems (VFVM_COORD_* in include/vfvm_gb300.h)
+COORD = {"cartesian": 0, "polar1d": 1, "spherical1d": 2, "cylindrical2d": 3}
+
 # physics ids shared with include/vfvm_gb300.h
 PHYS = {
     "ex105": 1, "ex106": 2, "ex110": 3, "ex160": 4, "ex207": 5, "ex301": 6, "ex440": 7,
     "laplace_dirichlet": 8, "nlpoisson": 11, "porous": 12, "bipolar": 13, "rd2": 14,
     "kappa_exp": 15, "surface_heat": 16, "boundary_species": 17, "edge_reaction": 18, "joule_heat": 19,
     "ex161": 20, "testfunction": 21, "ex430": 22, "outflow": 23, "ex210": 24,
-    "ex102": 25, "ex107": 26, "ex115": 27, "ex215": 28, "ex220": 29,
+    "ex102": 25, "ex107": 26, "ex115": 27, "ex215": 28, "ex220": 29, "ex203": 30,
 }
 
 
@@ -64,7 +67,7 @@ def lib():
         d, i32, i64 = ctypes.c_double, ctypes.c_int, ctypes.c_int64
         L.oracle_create.restype = ctypes.c_void_p
         L.oracle_create.argtypes = [i32, i32, P(d), i32, P(i32), P(i32), i32, P(i32), P(i32), i32,
-                                    P(d), i32, P(d), i32, P(d), P(d), i32]
+                                    P(d), i32, P(d), i32, P(d), P(d), i32, i32]
         L.oracle_destroy.argtypes = [ctypes.c_void_p]
         L.oracle_set_cellwise.argtypes = [ctypes.c_void_p, i32]
         L.oracle_set_species.argtypes = [ctypes.c_void_p, i32, P(i32), i32, P(i32)]
@@ -182,7 +185,8 @@ class OracleSystem:
             self.physics_id, _p(self.params, ctypes.c_double), self.params.size,
             _p(self._nodedata, ctypes.c_double) if self._nodedata is not None else None, nd,
             _p(self._bf, ctypes.c_double) if self._bf is not None else None,
-            _p(self._bv, ctypes.c_double) if self._bv is not None else None, nbreg)
+            _p(self._bv, ctypes.c_double) if self._bv is not None else None, nbreg,
+            COORD[getattr(g, "coordsystem", "cartesian")])
         if not self.h:
             raise ValueError("oracle_create failed (unknown physics or bad dimension)")
         if assembly not in ("edgewise", "cellwise"):
@@ -219,6 +223,12 @@ class OracleSystem:
 
     def nodevolumes(self):
         return self.factors()[0]
+
+    def bfacefactors(self):
+        """The node factors of every boundary face (dim x nbfaces, face after face)."""
+        out = np.zeros(self.grid.dim * self.grid.nbfaces)
+        lib().oracle_bfacefactors(self.h, _p(out, ctypes.c_double))
+        return out
 
     # -- assembly
     def assemble(self, U, Uold=None, time=0.0, tstep=math.inf, embed=0.0, keep_pattern=False):

@@ -6,7 +6,8 @@
 //
 // What it restates (paths relative to the reference project):
 //   cellfactors! (Edge1D, Triangle2D, Tetrahedron3D)   src/vfvm_formfactors.jl:12-23,64-100,163-235
-//   bfacefactors! (Vertex0D, Edge1D, Triangle2D)        src/vfvm_formfactors.jl:244-247,263-274,293-332
+//     (Polar1D, Spherical1D, Cylindrical2D)            src/vfvm_formfactors.jl:25-62,102-161
+//   bfacefactors! (Vertex0D, Edge1D, Triangle2D)        src/vfvm_formfactors.jl:244-332
 //   edgewise factor accumulation                       src/vfvm_system.jl:712-754
 //   Dirichlet constant 1e30                            src/vfvm_system.jl:329
 //   _initialize_dirichlet!                             src/vfvm_system.jl:947-1003
@@ -714,6 +715,19 @@ struct PhysEx220 : OBase {
   template <class T> void bstorage(T* f, const T* u, BNodeInfo& b) const { if (b.region == 2) f[2] = u[2]; }
 };
 
+// examples/Example203_CoordinateSystems.jl: flux u_K - u_L (:14-17) and the
+// constant source of each case (1.0 or 0.0).
+struct PhysEx203 : OBase {
+  static const int NS = 1;
+  static const bool has_reaction = false, has_storage = false, has_source = true, has_breaction = false;
+  double f0;
+  template <class T> void flux(T* f, const T* uK, const T* uL, const EdgeInfo&) const { f[0] = uK[0] - uL[0]; }
+  template <class T> void reaction(T*, const T*, const NodeInfo&) const {}
+  template <class T> void storage(T*, const T*, const NodeInfo&) const {}
+  void source(double* f, const NodeInfo&) const { f[0] = f0; }
+  template <class T> void breaction(T*, const T*, BNodeInfo&) const {}
+};
+
 // The physics of TestFunctionFactory (src/vfvm_testfunctions.jl:38-50): flux
 // u_K - u_L, storage u; Dirichlet data through the legacy boundary factors.
 struct PhysTestFunction : OBase {
@@ -729,6 +743,7 @@ struct PhysTestFunction : OBase {
 // ---------------------------------------------------------------- system
 struct Oracle {
   int dim = 0, N = 0, ncells = 0, nbf = 0, ns = 1, phys = 0, nregions = 1, nbregions = 0, nnd = 0;
+  int csys = 0;                    // coordinate system: 0 Cartesian, 1 Polar1D, 2 Spherical1D, 3 Cylindrical2D
   std::vector<double> coord;       // dim x N
   std::vector<int> cellnodes, cellregions, bfacenodes, bfaceregions;
   std::vector<double> params, ndata;
@@ -767,9 +782,64 @@ inline int nn_bface(int dim) { return dim; }  // nodes per boundary face: Vertex
 const int tri_en[3][2] = {{1, 2}, {2, 0}, {0, 1}};
 const int tet_en[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
 
-// cellfactors!, src/vfvm_formfactors.jl:12-23 (Edge1D), :64-100 (Triangle2D), :163-235 (Tetrahedron3D)
-void cellfactors(int dim, const double* coord, const int* n, double* npar, double* epar) {
-  if (dim == 1) {
+const double kPi = 3.141592653589793;  // Julia's pi as a Float64
+
+// tricircumcenter! (ExtendableGrids, an unvendored dependency): the circumcenter
+// of the triangle a, b, c by the published formula relative to a (Shewchuk).
+void tricircumcenter(double* cc, const double* a, const double* b, const double* c) {
+  double xba = b[0] - a[0], yba = b[1] - a[1], xca = c[0] - a[0], yca = c[1] - a[1];
+  double balength = xba * xba + yba * yba, calength = xca * xca + yca * yca;
+  double denominator = 0.5 / (xba * yca - yba * xca);
+  cc[0] = a[0] + (yca * balength - yba * calength) * denominator;
+  cc[1] = a[1] + (xba * calength - xca * balength) * denominator;
+}
+
+// cellfactors!, src/vfvm_formfactors.jl:12-23 (Edge1D), :25-62 (Edge1D Polar1D,
+// Spherical1D), :64-100 (Triangle2D), :102-161 (Triangle2D Cylindrical2D),
+// :163-235 (Tetrahedron3D)
+void cellfactors(int dim, int csys, const double* coord, const int* n, double* npar, double* epar) {
+  if (dim == 1 && (csys == 1 || csys == 2)) {
+    double r0 = coord[n[0]], r1 = coord[n[1]];
+    if (r1 < r0) { r0 = coord[n[1]]; r1 = coord[n[0]]; }
+    double rhalf = 0.5 * (r1 + r0);
+    if (csys == 1) {
+      npar[0] = kPi * (rhalf * rhalf - r0 * r0);
+      npar[1] = kPi * (r1 * r1 - rhalf * rhalf);
+      epar[0] = 2.0 * kPi * rhalf / (r1 - r0);
+    } else {
+      npar[0] = kPi * (rhalf * rhalf * rhalf - r0 * r0 * r0) * 4.0 / 3.0;
+      npar[1] = kPi * (r1 * r1 * r1 - rhalf * rhalf * rhalf) * 4.0 / 3.0;
+      epar[0] = 4.0 * kPi * (rhalf * rhalf) / (r1 - r0);
+    }
+  } else if (dim == 2 && csys == 3) {
+    double V[2][3];
+    for (int i = 0; i < 3; ++i)
+      for (int c = 0; c < 2; ++c) V[c][i] = coord[c + 2 * n[tri_en[i][0]]] - coord[c + 2 * n[tri_en[i][1]]];
+    double det = V[0][2] * V[1][1] - V[0][1] * V[1][2];
+    double vol = std::fabs(0.5 * det), ivol = 1.0 / vol;
+    double dd[3];
+    for (int i = 0; i < 3; ++i) dd[i] = V[0][i] * V[0][i] + V[1][i] * V[1][i];
+    double emid[3];
+    for (int i = 0; i < 3; ++i) emid[i] = 0.5 * (coord[2 * n[tri_en[i][0]]] + coord[2 * n[tri_en[i][1]]]);
+    double cc[2];
+    tricircumcenter(cc, coord + 2 * n[0], coord + 2 * n[1], coord + 2 * n[2]);
+    double rcc = cc[0];
+    epar[0] = (dd[1] + dd[2] - dd[0]) * 0.125 * ivol;
+    epar[1] = (dd[2] + dd[0] - dd[1]) * 0.125 * ivol;
+    epar[2] = (dd[0] + dd[1] - dd[2]) * 0.125 * ivol;
+    npar[0] = npar[1] = npar[2] = 0.0;
+    for (int i = 0; i < 3; ++i) {
+      double r1 = coord[2 * n[tri_en[i][0]]], r2 = coord[2 * n[tri_en[i][1]]];
+      double cylfac1 = 2 * kPi * (r1 + rcc + emid[i]) / 3;
+      double cylfac2 = 2 * kPi * (r2 + rcc + emid[i]) / 3;
+      npar[tri_en[i][0]] += epar[i] * dd[i] * 0.25 * cylfac1;
+      npar[tri_en[i][1]] += epar[i] * dd[i] * 0.25 * cylfac2;
+    }
+    for (int i = 0; i < 3; ++i) {
+      double rmid = (rcc + emid[i]) / 2;
+      epar[i] *= 2 * kPi * rmid;
+    }
+  } else if (dim == 1) {
     double d = std::fabs(coord[n[1]] - coord[n[0]]);
     npar[0] = d / 2; npar[1] = d / 2; epar[0] = 1 / d;
   } else if (dim == 2) {
@@ -826,10 +896,20 @@ void cellfactors(int dim, const double* coord, const int* n, double* npar, doubl
   }
 }
 
-// bfacefactors!, src/vfvm_formfactors.jl:244-247 (Vertex0D), :263-274 (Edge1D), :293-332 (Triangle2D)
-void bfacefactors(int dim, const double* coord, const int* n, double* npar, double* epar) {
+// bfacefactors!, src/vfvm_formfactors.jl:244-247 (Vertex0D), :249-261 (Vertex0D
+// Polar1D, Spherical1D), :263-274 (Edge1D), :276-291 (Edge1D Cylindrical2D: no
+// edge parameter, which stays 0 as in the reference's zeroed array), :293-332 (Triangle2D)
+void bfacefactors(int dim, int csys, const double* coord, const int* n, double* npar, double* epar) {
   if (dim == 1) {
-    npar[0] = 1.0;
+    double r = coord[n[0]];
+    npar[0] = csys == 1 ? 2 * kPi * r : csys == 2 ? 4 * kPi * (r * r) : 1.0;
+  } else if (dim == 2 && csys == 3) {
+    double r1 = coord[2 * n[0]], r2 = coord[2 * n[1]], z1 = coord[2 * n[0] + 1], z2 = coord[2 * n[1] + 1];
+    double dr = r1 - r2, rmid = (r1 + r2) / 2, dz = z1 - z2;
+    double l = std::sqrt(dr * dr + dz * dz);
+    npar[0] = kPi * (r1 + rmid) * l / 2;
+    npar[1] = kPi * (r2 + rmid) * l / 2;
+    epar[0] = 0.0;
   } else if (dim == 2) {
     double dx = coord[2 * n[0]] - coord[2 * n[1]], dy = coord[2 * n[0] + 1] - coord[2 * n[1] + 1];
     double d = std::sqrt(dx * dx + dy * dy);
@@ -893,14 +973,14 @@ void setup(Oracle& o) {
   o.edgefac.assign(o.E, {});
   double npar[4], epar[6];
   for (int c = 0; c < o.ncells; ++c) {
-    cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+    cellfactors(d, o.csys, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
     int ireg = o.cellregions[c];
     for (int i = 0; i < nnc; ++i) add_factor(o.nodefac[o.cellnodes[i + nnc * c]], ireg, npar[i]);
     for (int i = 0; i < nen; ++i) add_factor(o.edgefac[o.celledges[i + nen * c]], ireg, epar[i]);
   }
   const int nbn = nn_bface(d);
   o.bfacenodefac.assign((size_t)nbn * o.nbf, 0.0);
-  for (int b = 0; b < o.nbf; ++b) bfacefactors(d, o.coord.data(), &o.bfacenodes[nbn * b], &o.bfacenodefac[nbn * b], epar);
+  for (int b = 0; b < o.nbf; ++b) bfacefactors(d, o.csys, o.coord.data(), &o.bfacenodes[nbn * b], &o.bfacenodefac[nbn * b], epar);
   // candidate CSR: rows (K,i), columns (M,j) for M in {K} u neighbours(K)
   std::vector<std::vector<int>> nb(o.N);
   for (int e = 0; e < o.E; ++e) { nb[o.edgenodes[2 * e]].push_back(o.edgenodes[2 * e + 1]); nb[o.edgenodes[2 * e + 1]].push_back(o.edgenodes[2 * e]); }
@@ -1066,11 +1146,11 @@ int assemble_t(Oracle& o, const P& ph, const double* U, const double* Uold, doub
     const int nnc = d + 1, nen = d == 1 ? 1 : (d == 2 ? 3 : 6);
     double npar[4], epar[6];
     for (int c = 0; c < o.ncells; ++c) {
-      cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+      cellfactors(d, o.csys, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
       for (int i = 0; i < nnc; ++i) node_term(o.cellnodes[i + nnc * c], o.cellregions[c], npar[i]);
     }
     for (int c = 0; c < o.ncells; ++c) {
-      cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+      cellfactors(d, o.csys, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
       for (int i = 0; i < nen; ++i) {
         const int e = o.celledges[i + nen * c];
         edge_term(o.edgenodes[2 * e], o.edgenodes[2 * e + 1], o.cellregions[c], epar[i], false);
@@ -1136,7 +1216,7 @@ int assemble_t(Oracle& o, const P& ph, const double* U, const double* Uold, doub
     const int nle = d == 2 ? 1 : 3;
     for (int b = 0; b < o.nbf; ++b) {
       const int* bn = &o.bfacenodes[nbn * b];
-      bfacefactors(d, o.coord.data(), bn, npar, epar);
+      bfacefactors(d, o.csys, o.coord.data(), bn, npar, epar);
       for (int i = 0; i < nle; ++i) {
         int K = d == 2 ? bn[0] : bn[tri_en[i][0]], L = d == 2 ? bn[1] : bn[tri_en[i][1]];
         if (K > L) std::swap(K, L);
@@ -1237,11 +1317,11 @@ void integrate_t(Oracle& o, const P& ph, const double* T, const double* U, const
     const int nnc = d + 1, nen = d == 1 ? 1 : (d == 2 ? 3 : 6);
     double npar[4], epar[6];
     for (int c = 0; c < o.ncells; ++c) {
-      cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+      cellfactors(d, o.csys, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
       for (int i = 0; i < nnc; ++i) node_item(o.cellnodes[i + nnc * c], o.cellregions[c], npar[i]);
     }
     for (int c = 0; c < o.ncells; ++c) {
-      cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+      cellfactors(d, o.csys, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
       for (int i = 0; i < nen; ++i) {
         const int e = o.celledges[i + nen * c];
         edge_item(o.edgenodes[2 * e], o.edgenodes[2 * e + 1], o.cellregions[c], epar[i]);
@@ -1278,7 +1358,7 @@ void mass_t(Oracle& o, const P& ph) {
     const int nnc = d + 1;
     double npar[4], epar[6];
     for (int c = 0; c < o.ncells; ++c) {
-      cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+      cellfactors(d, o.csys, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
       for (int i = 0; i < nnc; ++i) node_item(o.cellnodes[i + nnc * c], o.cellregions[c], npar[i]);
     }
   }
@@ -1364,11 +1444,11 @@ void dparams_t(Oracle& o, const PD& ph, const double* U, double time, double tst
     const int nnc = d + 1, nen = d == 1 ? 1 : (d == 2 ? 3 : 6);
     double npar[4], epar[6];
     for (int c = 0; c < o.ncells; ++c) {
-      cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+      cellfactors(d, o.csys, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
       for (int i = 0; i < nnc; ++i) node_item(o.cellnodes[i + nnc * c], o.cellregions[c], npar[i]);
     }
     for (int c = 0; c < o.ncells; ++c) {
-      cellfactors(d, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
+      cellfactors(d, o.csys, o.coord.data(), &o.cellnodes[nnc * c], npar, epar);
       for (int i = 0; i < nen; ++i) {
         const int e = o.celledges[i + nen * c];
         edge_item(o.edgenodes[2 * e], o.edgenodes[2 * e + 1], o.cellregions[c], epar[i], false);
@@ -1398,7 +1478,7 @@ void dparams_t(Oracle& o, const PD& ph, const double* U, double time, double tst
     const int nle = d == 2 ? 1 : 3;
     for (int b = 0; b < o.nbf; ++b) {
       const int* bn = &o.bfacenodes[nbn * b];
-      bfacefactors(d, o.coord.data(), bn, npar, epar);
+      bfacefactors(d, o.csys, o.coord.data(), bn, npar, epar);
       for (int i = 0; i < nle; ++i) {
         int K = d == 2 ? bn[0] : bn[tri_en[i][0]], L = d == 2 ? bn[1] : bn[tri_en[i][1]];
         if (K > L) std::swap(K, L);
@@ -1520,6 +1600,7 @@ int dispatch(const Oracle& o, F&& fn) {
     }
     case 28: { PhysEx215 ph; ph.eps = P(0); ph.k_react = P(1); return fn(ph); }
     case 29: { PhysEx220 ph; ph.k = P(0); ph.eps = P(1); return fn(ph); }
+    case 30: { PhysEx203 ph; ph.f0 = P(0); return fn(ph); }
     case 23: {
       PhysOutflow ph;
       ph.k = P(0); ph.v_in = P(1); ph.c_in = P(2); ph.D = P(3); ph.gin = (int)P(4); ph.gout = (int)P(5);
@@ -1537,7 +1618,7 @@ int nspec_of(int phys) {
     case 3: case 4: case 14: case 17: case 19: case 23: case 24: case 28: return 2;
     case 13: case 20: case 27: case 29: return 3;
     case 1: case 2: case 5: case 6: case 7: case 8: case 11: case 12: case 15: case 16: case 18: case 21: case 22:
-    case 25: case 26: return 1;
+    case 25: case 26: case 30: return 1;
   }
   return 0;
 }
@@ -1549,11 +1630,14 @@ extern "C" {
 void* oracle_create(int dim, int nnodes, const double* coord, int ncells, const int* cellnodes, const int* cellregions,
                     int nbfaces, const int* bfacenodes, const int* bfaceregions, int physics_id,
                     const double* params, int nparams, const double* nodedata, int nnodedata,
-                    const double* bfactors, const double* bvalues, int nbregions) {
+                    const double* bfactors, const double* bvalues, int nbregions, int coordsystem) {
   int ns = nspec_of(physics_id);
   if (ns == 0 || dim < 1 || dim > 3) return nullptr;
+  if (!(coordsystem == 0 || (dim == 1 && (coordsystem == 1 || coordsystem == 2)) || (dim == 2 && coordsystem == 3)))
+    return nullptr;
   Oracle* o = new Oracle;
   o->dim = dim; o->N = nnodes; o->ncells = ncells; o->nbf = nbfaces; o->ns = ns; o->phys = physics_id;
+  o->csys = coordsystem;
   o->coord.assign(coord, coord + (size_t)dim * nnodes);
   o->cellnodes.assign(cellnodes, cellnodes + (size_t)(dim + 1) * ncells);
   o->cellregions.assign(cellregions, cellregions + ncells);
@@ -1708,12 +1792,12 @@ void oracle_init_dirichlet(void* h, double* U, double time, double lambda) {
   dispatch(*o, [&](const auto& ph) { init_dirichlet_t(*o, ph, U, time, lambda); return 0; });
 }
 
-// Standalone geometry kernels for the form-factor identity test (test/test020_formfactors.jl).
+// Standalone Cartesian geometry kernels for the form-factor identity test (test/test020_formfactors.jl).
 void oracle_cellfactors(int dim, const double* coord, const int* nodes, double* npar, double* epar) {
-  cellfactors(dim, coord, nodes, npar, epar);
+  cellfactors(dim, 0, coord, nodes, npar, epar);
 }
 void oracle_bfacefactors_raw(int dim, const double* coord, const int* nodes, double* npar, double* epar) {
-  bfacefactors(dim, coord, nodes, npar, epar);
+  bfacefactors(dim, 0, coord, nodes, npar, epar);
 }
 void oracle_fbernoulli_pm(const double* x, double* bp, double* bm, int64_t n) {
   for (int64_t i = 0; i < n; ++i) fbernoulli_pm(x[i], bp[i], bm[i]);

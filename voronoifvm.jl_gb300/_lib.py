@@ -24,7 +24,7 @@ PHYSICS_IDS = {
     "laplace_dirichlet": 8, "nlpoisson": 11, "porous": 12, "bipolar": 13, "rd2": 14, "kappa_exp": 15,
     "surface_heat": 16, "boundary_species": 17, "edge_reaction": 18, "joule_heat": 19, "ex161": 20,
     "testfunction": 21, "ex430": 22, "outflow": 23, "ex210": 24, "ex102": 25, "ex107": 26, "ex115": 27,
-    "ex215": 28, "ex220": 29,
+    "ex215": 28, "ex220": 29, "ex203": 30,
 }
 # physics whose first parameters carry derivatives (NPD in the device functor)
 PHYSICS_NPD = {22: 1}
@@ -35,18 +35,19 @@ def physics_npd(physics_id: int) -> int:
 
 
 PHYSICS_NSPEC = {1: 1, 2: 1, 3: 2, 4: 2, 5: 1, 6: 1, 7: 1, 8: 1, 11: 1, 12: 1, 13: 3, 14: 2, 15: 1, 16: 1, 17: 2, 18: 1, 19: 2, 20: 3, 21: 1, 22: 1, 23: 2, 24: 2,
-                 25: 1, 26: 1, 27: 3, 28: 2, 29: 3}
+                 25: 1, 26: 1, 27: 3, 28: 2, 29: 3, 30: 1}
 
 KRYLOV = {"bicgstab": 0, "gmres": 1}
 PRECON = {"jacobi": 0, "ilu0": 1, "block_ilu0": 2}
 PRECISION = {"fp64": 0, "mixed": 1}
 ENGINE = {"graph": 0, "persistent": 1, "auto": 2}
+COORD = {"cartesian": 0, "polar1d": 1, "spherical1d": 2, "cylindrical2d": 3}  # VFVM_COORD_*
 
 
 class Grid_t(ctypes.Structure):
     _fields_ = [("dim", c_i32), ("nnodes", c_i32), ("ncells", c_i32), ("nbfaces", c_i32),
                 ("coord", P(c_d)), ("cellnodes", P(c_i32)), ("cellregions", P(c_i32)),
-                ("bfacenodes", P(c_i32)), ("bfaceregions", P(c_i32))]
+                ("bfacenodes", P(c_i32)), ("bfaceregions", P(c_i32)), ("coordsystem", c_i32)]
 
 
 class Physics_t(ctypes.Structure):

@@ -35,7 +35,8 @@ INST_PHYSICS = ["PhysEx105", "PhysEx106", "PhysEx110", "PhysEx160", "PhysEx207",
                 "PhysLaplaceDir", "PhysNLPoisson", "PhysPorous", "PhysBipolar", "PhysRD2", "PhysKappaExp",
                 "PhysSurfaceHeat", "PhysBoundarySpecies", "PhysEdgeReaction", "PhysJouleHeat",
                 "PhysEx161", "PhysTestFunction", "PhysEx430", "PhysOutflow",
-                "PhysEx210", "PhysEx102", "PhysEx107", "PhysEx115", "PhysEx215", "PhysEx220"]
+                "PhysEx210", "PhysEx102", "PhysEx107", "PhysEx115", "PhysEx215", "PhysEx220",
+                "PhysEx203"]
 
 
 def sources():

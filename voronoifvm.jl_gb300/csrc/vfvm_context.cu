@@ -30,9 +30,45 @@ inline double dist2(const double* a, const double* b, int dim) {
   return s;
 }
 
+constexpr double kPi = 3.141592653589793;
+
+// First coordinate (r) of a triangle's circumcenter: the published formula
+// relative to vertex a (J. R. Shewchuk, "Lecture Notes on Geometric Robustness").
+double tri_circumcenter_r(const double* a, const double* b, const double* c) {
+  const double xba = b[0] - a[0], yba = b[1] - a[1], xca = c[0] - a[0], yca = c[1] - a[1];
+  const double balength = xba * xba + yba * yba, calength = xca * xca + yca * yca;
+  const double denominator = 0.5 / (xba * yca - yba * xca);
+  return a[0] + (yca * balength - yba * calength) * denominator;
+}
+
 // Voronoi node volumes and edge weights sigma_kl / h_kl of one simplex
-// (src/vfvm_formfactors.jl:12-23, :64-100, :163-235).
-void simplex_factors(int dim, const double* const* x, double* nodef, double* edgef) {
+// (src/vfvm_formfactors.jl:12-23, :64-100, :163-235) in the grid's coordinate
+// system (VFVM_COORD_*):
+// * polar / spherical 1D (:25-62): the shell volumes between the cell's inner
+//   radius r0, its midpoint and its outer radius r1, and the circle / sphere
+//   surface at the midpoint over r1 - r0; as in the reference, the inner part
+//   goes to the cell's first node, the outer to its second (cells run outwards
+//   on the grids of simplexgrid);
+// * cylindrical 2D (:102-161): the Cartesian contributions, each node's part of
+//   the Voronoi cell times 2 pi the mean radius of its triangle (node, edge
+//   midpoint, circumcenter), each edge weight times 2 pi the mean radius of the
+//   Voronoi face (edge midpoint, circumcenter).
+void simplex_factors(int dim, int csys, const double* const* x, double* nodef, double* edgef) {
+  if (dim == 1 && csys != VFVM_COORD_CARTESIAN) {
+    double r0 = x[0][0], r1 = x[1][0];
+    if (r1 < r0) std::swap(r0, r1);
+    const double rhalf = 0.5 * (r1 + r0);
+    if (csys == VFVM_COORD_POLAR1D) {
+      nodef[0] = kPi * (rhalf * rhalf - r0 * r0);
+      nodef[1] = kPi * (r1 * r1 - rhalf * rhalf);
+      edgef[0] = 2.0 * kPi * rhalf / (r1 - r0);
+    } else {
+      nodef[0] = kPi * (rhalf * rhalf * rhalf - r0 * r0 * r0) * 4.0 / 3.0;
+      nodef[1] = kPi * (r1 * r1 * r1 - rhalf * rhalf * rhalf) * 4.0 / 3.0;
+      edgef[0] = 4.0 * kPi * (rhalf * rhalf) / (r1 - r0);
+    }
+    return;
+  }
   if (dim == 1) {
     double h = std::fabs(x[1][0] - x[0][0]);
     nodef[0] = nodef[1] = 0.5 * h;
@@ -48,6 +84,23 @@ void simplex_factors(int dim, const double* const* x, double* nodef, double* edg
     double area = std::fabs(0.5 * (ax * by - bx * ay));
     double inv8a = 0.125 / area;
     for (int i = 0; i < 3; ++i) nodef[i] = 0.0;
+    if (csys == VFVM_COORD_CYLINDRICAL2D) {
+      const double rcc = tri_circumcenter_r(x[0], x[1], x[2]);
+      for (int e = 0; e < 3; ++e) {
+        const int a0 = kTriEdges[e][0], a1 = kTriEdges[e][1];
+        edgef[e] = (l2[(e + 1) % 3] + l2[(e + 2) % 3] - l2[e]) * inv8a;
+        const double emid = 0.5 * (x[a0][0] + x[a1][0]);
+        const double cyl0 = 2.0 * kPi * (x[a0][0] + rcc + emid) / 3.0;
+        const double cyl1 = 2.0 * kPi * (x[a1][0] + rcc + emid) / 3.0;
+        nodef[a0] += edgef[e] * l2[e] * 0.25 * cyl0;
+        nodef[a1] += edgef[e] * l2[e] * 0.25 * cyl1;
+      }
+      for (int e = 0; e < 3; ++e) {
+        const double rmid = (rcc + 0.5 * (x[kTriEdges[e][0]][0] + x[kTriEdges[e][1]][0])) / 2.0;
+        edgef[e] *= 2.0 * kPi * rmid;
+      }
+      return;
+    }
     for (int e = 0; e < 3; ++e) {
       // half the cotangent of the angle opposite edge e
       edgef[e] = (l2[(e + 1) % 3] + l2[(e + 2) % 3] - l2[e]) * inv8a;
@@ -89,9 +142,23 @@ void simplex_factors(int dim, const double* const* x, double* nodef, double* edg
   }
 }
 
-// Boundary face node factors (src/vfvm_formfactors.jl:244-247, :263-274, :293-332).
-void bface_factors(int dim, const double* const* x, double* nodef) {
-  if (dim == 1) { nodef[0] = 1.0; return; }
+// Boundary face node factors (src/vfvm_formfactors.jl:244-332): a point (1,
+// or the circle 2 pi r / the sphere 4 pi r^2 at its radius), a segment (half
+// its length each, or in cylindrical coordinates pi (r_node + r_mid) l / 2, the
+// surface of revolution of its half), a triangle.
+void bface_factors(int dim, int csys, const double* const* x, double* nodef) {
+  if (dim == 1) {
+    const double r = x[0][0];
+    nodef[0] = csys == VFVM_COORD_POLAR1D ? 2.0 * kPi * r : csys == VFVM_COORD_SPHERICAL1D ? 4.0 * kPi * (r * r) : 1.0;
+    return;
+  }
+  if (dim == 2 && csys == VFVM_COORD_CYLINDRICAL2D) {
+    const double r1 = x[0][0], r2 = x[1][0], dr = r1 - r2, dz = x[0][1] - x[1][1];
+    const double rmid = (r1 + r2) / 2.0, l = std::sqrt(dr * dr + dz * dz);
+    nodef[0] = kPi * (r1 + rmid) * l / 2.0;
+    nodef[1] = kPi * (r2 + rmid) * l / 2.0;
+    return;
+  }
   if (dim == 2) {
     double h = std::sqrt(dist2(x[0], x[1], 2));
     nodef[0] = nodef[1] = 0.5 * h;
@@ -115,9 +182,11 @@ void bface_factors(int dim, const double* const* x, double* nodef) {
 // parameters, src/vfvm_formfactors.jl:263-274 for a segment, :293-332 for a
 // triangle): 1 / length for a segment; half the cotangent of the opposite angle
 // for a triangle, local edge e opposite local node e.
-void bface_edge_factors(int dim, const double* const* x, double* edgef) {
+// In cylindrical coordinates the reference sets no edge parameter for a
+// boundary segment (its zero-initialised bfaceedgefactors, src/vfvm_system.jl:652).
+void bface_edge_factors(int dim, int csys, const double* const* x, double* edgef) {
   if (dim == 2) {
-    edgef[0] = 1.0 / std::sqrt(dist2(x[0], x[1], 2));
+    edgef[0] = csys == VFVM_COORD_CYLINDRICAL2D ? 0.0 : 1.0 / std::sqrt(dist2(x[0], x[1], 2));
     return;
   }
   double l2[3];
@@ -355,6 +424,12 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
       return nullptr;
   }
   const int dim = g->dim, N = g->nnodes, nc = g->ncells, nbf = g->nbfaces, nvc = dim + 1;
+  // the coordinate systems with form factors: Cartesian in every dimension,
+  // polar and spherical in 1D, cylindrical in 2D
+  const int csys = g->coordsystem;
+  if (!(csys == VFVM_COORD_CARTESIAN || (dim == 1 && (csys == VFVM_COORD_POLAR1D || csys == VFVM_COORD_SPHERICAL1D)) ||
+        (dim == 2 && csys == VFVM_COORD_CYLINDRICAL2D)))
+    return nullptr;
   // index validation: every table entry must address an existing node/region
   for (int64_t i = 0; i < (int64_t)nvc * nc; ++i) if (g->cellnodes[i] < 0 || g->cellnodes[i] >= N) return nullptr;
   for (int64_t i = 0; i < (int64_t)dim * nbf; ++i) if (g->bfacenodes[i] < 0 || g->bfacenodes[i] >= N) return nullptr;
@@ -451,7 +526,7 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
     double nf[4], ef[6];
     for (int cell = 0; cell < nc; ++cell) {
       for (int v = 0; v < nvc; ++v) xs[v] = &c->h_coord[(size_t)g->cellnodes[v + (size_t)nvc * cell] * dim];
-      simplex_factors(dim, xs, nf, ef);
+      simplex_factors(dim, csys, xs, nf, ef);
       const int reg = g->cellregions[cell];
       for (int v = 0; v < nvc; ++v) add_regfac(nfac[g->cellnodes[v + (size_t)nvc * cell]], reg, nf[v]);
       for (int e = 0; e < nle; ++e) {
@@ -529,7 +604,7 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
     int maxbreg = 0;
     for (int b = 0; b < nbf; ++b) {
       for (int v = 0; v < nbn; ++v) xs[v] = &c->h_coord[(size_t)g->bfacenodes[v + (size_t)nbn * b] * dim];
-      bface_factors(dim, xs, bf);
+      bface_factors(dim, csys, xs, bf);
       maxbreg = std::max(maxbreg, g->bfaceregions[b]);
       for (int v = 0; v < nbn; ++v) {
         int k = g->bfacenodes[v + (size_t)nbn * b];
@@ -556,7 +631,7 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
     const int nle_b = dim == 2 ? 1 : 3;
     for (int b = 0; b < nbf; ++b) {
       for (int v = 0; v < nbn; ++v) xs[v] = &c->h_coord[(size_t)g->bfacenodes[v + (size_t)nbn * b] * dim];
-      bface_edge_factors(dim, xs, ef);
+      bface_edge_factors(dim, csys, xs, ef);
       for (int e = 0; e < nle_b; ++e) {
         int a = g->bfacenodes[(dim == 2 ? 0 : kTriEdges[e][0]) + (size_t)nbn * b];
         int bb = g->bfacenodes[(dim == 2 ? 1 : kTriEdges[e][1]) + (size_t)nbn * b];

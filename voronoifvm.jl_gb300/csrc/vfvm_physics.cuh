@@ -678,13 +678,26 @@ struct PhysEx220 : PhysBase {
   }
 };
 
+// examples/Example203_CoordinateSystems.jl:14-17 and its sources: flux u_K -
+// u_L, the constant source f (1 for the disk, cylinder and ball, 0 for the ring,
+// cylinder shell and spherical shell); the coordinate system is the grid's.
+// params: f
+struct PhysEx203 : PhysBase {
+  static constexpr int NS = 1;
+  static constexpr bool has_source = true;
+  double f0;
+  VFVM_HD void load(const double* p) { f0 = p[0]; }
+  template <class T> VFVM_HD void flux(T* f, const T* uK, const T* uL, const EdgeItem&) const { f[0] = uK[0] - uL[0]; }
+  VFVM_HD void source(double* f, const NodeItem&) const { f[0] = f0; }
+};
+
 inline int physics_nspec(int id) {
   switch (id) {
     case VFVM_PHYS_EX105: case VFVM_PHYS_EX106: case VFVM_PHYS_EX207: case VFVM_PHYS_EX301:
     case VFVM_PHYS_EX440: case VFVM_PHYS_LAPLACE_DIRICHLET: case VFVM_PHYS_NLPOISSON:
     case VFVM_PHYS_POROUS: case VFVM_PHYS_KAPPA_EXP: case VFVM_PHYS_SURFACE_HEAT:
     case VFVM_PHYS_EDGE_REACTION: case VFVM_PHYS_TESTFUNCTION: case VFVM_PHYS_EX430: case VFVM_PHYS_EX102:
-    case VFVM_PHYS_EX107: return 1;
+    case VFVM_PHYS_EX107: case VFVM_PHYS_EX203: return 1;
     case VFVM_PHYS_EX110: case VFVM_PHYS_EX160: case VFVM_PHYS_RD2: case VFVM_PHYS_BOUNDARY_SPECIES:
     case VFVM_PHYS_JOULE_HEAT: case VFVM_PHYS_OUTFLOW: case VFVM_PHYS_EX210: case VFVM_PHYS_EX215: return 2;
     case VFVM_PHYS_BIPOLAR: case VFVM_PHYS_EX161: case VFVM_PHYS_EX115: case VFVM_PHYS_EX220: return 3;
@@ -711,6 +724,7 @@ inline int physics_nparams(int id) {
     case VFVM_PHYS_EX115: return 8;
     case VFVM_PHYS_EX215: return 2;
     case VFVM_PHYS_EX220: return 2;
+    case VFVM_PHYS_EX203: return 1;
   }
   return 0;
 }
@@ -747,6 +761,7 @@ int dispatch_physics(int id, Fn&& fn) {
     case VFVM_PHYS_EX115: return fn(PhysEx115{});
     case VFVM_PHYS_EX215: return fn(PhysEx215{});
     case VFVM_PHYS_EX220: return fn(PhysEx220{});
+    case VFVM_PHYS_EX203: return fn(PhysEx203{});
   }
   return VFVM_ERR_INPUT;
 }

@@ -34,7 +34,12 @@ import os
 
 import numpy as np
 
-__all__ = ["Grid", "simplexgrid"]
+__all__ = ["Grid", "simplexgrid", "circular_symmetric", "spherical_symmetric"]
+
+# CoordinateSystem of an ExtendableGrids grid: which body the grid's coordinates
+# describe, and so which form factors the assembly uses
+# (src/vfvm_formfactors.jl:12-332)
+COORD_SYSTEMS = ("cartesian", "polar1d", "spherical1d", "cylindrical2d")
 
 
 class Grid:
@@ -47,6 +52,7 @@ class Grid:
         self.bfacenodes = np.ascontiguousarray(bfacenodes, dtype=np.int32)
         self.bfaceregions = np.ascontiguousarray(bfaceregions, dtype=np.int32)
         self.dim = self.coord.shape[0]
+        self.coordsystem = "cartesian"
         if self.cellnodes.shape[0] != self.dim + 1:
             raise ValueError("cellnodes must have dim+1 rows")
         if self.bfacenodes.shape[0] != self.dim:
@@ -88,8 +94,9 @@ class Grid:
         return np.stack([key // self.nnodes, key % self.nnodes]).astype(np.int32)
 
     def __repr__(self):
+        cs = "" if self.coordsystem == "cartesian" else f", coordsystem={self.coordsystem}"
         return (f"Grid(dim={self.dim}, nnodes={self.nnodes}, ncells={self.ncells}, "
-                f"nbfaces={self.nbfaces})")
+                f"nbfaces={self.nbfaces}{cs})")
 
 
 # --- SimplexGrid text files (ExtendableGrids' ``.sg`` format, e.g. assets/rz2d.sg)
@@ -184,6 +191,29 @@ def _mask(grid: Grid, nodes: np.ndarray, maskmin, maskmax, tol: float) -> np.nda
         x = grid.coord[:, nodes[v]]
         inside &= np.all((x >= lo) & (x <= hi), axis=0)
     return inside
+
+
+def circular_symmetric(grid: Grid) -> Grid:
+    """circular_symmetric!(grid) (ExtendableGrids; used in
+    examples/Example203_CoordinateSystems.jl): a 1D grid's coordinate is the
+    radius of a disk or ring (Polar1D), a 2D grid's coordinates are (r, z) of a
+    cylinder (Cylindrical2D)."""
+    if grid.dim == 1:
+        grid.coordsystem = "polar1d"
+    elif grid.dim == 2:
+        grid.coordsystem = "cylindrical2d"
+    else:
+        raise ValueError("circular symmetry needs a 1D or 2D grid")
+    return grid
+
+
+def spherical_symmetric(grid: Grid) -> Grid:
+    """spherical_symmetric!(grid) (ExtendableGrids): a 1D grid's coordinate is
+    the radius of a ball or spherical shell (Spherical1D)."""
+    if grid.dim != 1:
+        raise ValueError("spherical symmetry needs a 1D grid")
+    grid.coordsystem = "spherical1d"
+    return grid
 
 
 def cellmask(grid: Grid, maskmin, maskmax, ireg: int, tol: float = 1e-10) -> Grid:

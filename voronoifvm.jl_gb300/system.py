@@ -307,7 +307,8 @@ class System:
         keep["bfaceregions"] = np.ascontiguousarray(g.bfaceregions, dtype=np.int32)
         gt = L.Grid_t(g.dim, g.nnodes, g.ncells, g.nbfaces,
                       L.ptr(keep["coord"]), L.ptr(keep["cellnodes"], L.c_i32), L.ptr(keep["cellregions"], L.c_i32),
-                      L.ptr(keep["bfacenodes"], L.c_i32), L.ptr(keep["bfaceregions"], L.c_i32))
+                      L.ptr(keep["bfacenodes"], L.c_i32), L.ptr(keep["bfaceregions"], L.c_i32),
+                      L.COORD[g.coordsystem])
         params = np.ascontiguousarray(self.physics.data, dtype=np.float64)
         if params.size == 0:
             params = np.zeros(1)
@@ -338,7 +339,7 @@ class System:
     @property
     def ctx(self):
         nd = self.physics.nodedata
-        key = (self.boundary_factors.tobytes(), self.boundary_values.tobytes(),
+        key = (self.grid.coordsystem, self.boundary_factors.tobytes(), self.boundary_values.tobytes(),
                None if nd is None else np.shape(nd),
                None if self.region_species is None else (self.region_species.tobytes(),
                                                          self.bregion_species.tobytes()))
