@@ -48,3 +48,20 @@ def test_control_struct_layout(vfvm):
     lib.vfvm_control_default(ctypes.byref(c))
     assert c.abstol == 1e-10 and c.maxiters == 100 and c.damp_growth == 1.2 and c.store_all == 1
     assert c.reltol_linear == 1e-4 and c.abstol_linear == 0.0 and c.maxiters_linear == 100 and c.dt_grow == 1.2
+
+
+def header_defines(prefix):
+    src = open(os.path.join(ROOT, "include", "vfvm_gb300.h")).read()
+    return {m.group(1): int(m.group(2)) for m in re.finditer(rf"#define\s+{prefix}([A-Z0-9_]+)\s+(\d+)", src)}
+
+
+def test_physics_and_coordinate_ids_match_header(vfvm, oracle):
+    """Every VFVM_PHYS_* and VFVM_COORD_* id of the header has the same number in
+    the Python binding and in the oracle, and the species counts agree."""
+    phys = header_defines("VFVM_PHYS_")
+    assert {k.lower(): v for k, v in phys.items()} == vfvm._lib.PHYSICS_IDS
+    assert vfvm._lib.PHYSICS_IDS == oracle.PHYS
+    assert set(vfvm._lib.PHYSICS_NSPEC) == set(phys.values())
+    coord = header_defines("VFVM_COORD_")
+    assert {k.lower(): v for k, v in coord.items()} == vfvm._lib.COORD == oracle.COORD
+    assert tuple(vfvm._lib.COORD) == vfvm.grid.COORD_SYSTEMS
