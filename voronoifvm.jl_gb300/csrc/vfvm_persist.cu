@@ -36,13 +36,14 @@ extern "C" vfvm_batch* vfvm_batch_create(int32_t ninst, const vfvm_grid* grids, 
   b->ninst = ninst;
   b->phys = phys[0].physics_id;
   b->offsets.assign(ninst + 1, 0);
-  // systems that all use the same grid arrays share one set of device tables
+  // systems that all use the same grid arrays (and coordinate system) share one set of device tables
   bool shared = true;
   for (int i = 1; i < ninst && shared; ++i)
     shared = grids[i].dim == grids[0].dim && grids[i].nnodes == grids[0].nnodes && grids[i].ncells == grids[0].ncells &&
              grids[i].nbfaces == grids[0].nbfaces && grids[i].coord == grids[0].coord &&
              grids[i].cellnodes == grids[0].cellnodes && grids[i].cellregions == grids[0].cellregions &&
-             grids[i].bfacenodes == grids[0].bfacenodes && grids[i].bfaceregions == grids[0].bfaceregions;
+             grids[i].bfacenodes == grids[0].bfacenodes && grids[i].bfaceregions == grids[0].bfaceregions &&
+             grids[i].coordsystem == grids[0].coordsystem;
   for (int i = 0; i < ninst; ++i) {
     int st = 0;
     b->shared_grid = shared;
