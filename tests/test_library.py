@@ -65,3 +65,39 @@ def test_physics_and_coordinate_ids_match_header(vfvm, oracle):
     coord = header_defines("VFVM_COORD_")
     assert {k.lower(): v for k, v in coord.items()} == vfvm._lib.COORD == oracle.COORD
     assert tuple(vfvm._lib.COORD) == vfvm.grid.COORD_SYSTEMS
+
+
+def header_struct_fields(name):
+    """(field, C type) in declaration order of `typedef struct name {...} name;`."""
+    src = open(os.path.join(ROOT, "include", "vfvm_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    body = re.search(rf"typedef struct {name} \{{(.*?)\}} {name};", src, flags=re.S).group(1)
+    fields = []
+    for decl in body.split(";"):
+        decl = " ".join(decl.split())
+        if not decl:
+            continue
+        m = re.match(r"(const )?(int32_t|int64_t|double|float|int)(\*)? (.*)", decl)
+        assert m, decl
+        ctype = m.group(2) + ("*" if m.group(3) else "")
+        for var in m.group(4).split(","):
+            var = var.strip()
+            fields.append((var.lstrip("*"), ctype + ("*" if var.startswith("*") else "")))
+    return fields
+
+
+@pytest.mark.parametrize("cname,pyname", [("vfvm_grid", "Grid_t"), ("vfvm_physics_desc", "Physics_t"),
+                                          ("vfvm_control", "Control_t"), ("vfvm_history", "History_t")])
+def test_struct_mirrors_match_header(vfvm, cname, pyname):
+    """The ctypes structures passed across the C ABI have the header's fields in
+    the header's order, with the same types (the layout the library reads)."""
+    L = vfvm._lib
+    ctype_of = {"int32_t": L.c_i32, "int": L.c_i32, "int64_t": L.c_i64, "double": L.c_d, "float": ctypes.c_float}
+    want = header_struct_fields(cname)
+    got = getattr(L, pyname)._fields_
+    assert [f for f, _ in got] == [f for f, _ in want]
+    for (field, pytype), (_, ctype) in zip(got, want):
+        if ctype.endswith("*"):
+            assert issubclass(pytype, ctypes._Pointer) and pytype._type_ == ctype_of[ctype[:-1]], field
+        else:
+            assert pytype == ctype_of[ctype], field
