@@ -24,6 +24,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF = None  # the reference checkout, the required command-line argument
 
 EXAMPLES = {
+    # the value is inline in runtests: @test main() ≈ value
+    "Example101_Laplace1D": r"main\(\)\s*≈\s*([-0-9.e]+)",
     "Example102_StationaryConvectionDiffusion1D": r"testval\s*=\s*([-0-9.e]+)",
     "Example105_NonlinearPoisson1D": r"testval\s*=\s*([-0-9.e]+)",
     "Example107_NonlinearStorage1D": r"testval\s*=\s*([-0-9.e]+)",

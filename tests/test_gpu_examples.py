@@ -3,6 +3,7 @@ against the golden value in its runtests (tests/golden/reference_testvals.json)
 with the solver tolerances each test states (tighter than the defaults where
 the example's own tolerance asks for it):
 
+* Example101: the 1D Laplace problem of the introduction (test030's system);
 * Example102: three convection-diffusion fluxes (exponential, upwind, central);
 * Example107: nonlinear storage with the adaptive step control on the device;
 * Example115: a boundary species with mass-action boundary reactions and
@@ -31,6 +32,16 @@ RTOL = math.sqrt(np.finfo(float).eps)
 def testvals():
     with open(os.path.join(GOLDEN, "reference_testvals.json")) as f:
         return json.load(f)
+
+
+@pytest.mark.parametrize("assembly", ["edgewise", "cellwise"])
+def test_example101_laplace(vfvm, testvals, assembly):
+    """examples/Example101_Laplace1D.jl (runtests :126-129): -u'' = 0 on
+    0:0.2:1, u = 0 and 1 at the ends by breaction penalties; sum(solution)."""
+    g = vfvm.simplexgrid(np.array([k / 5 for k in range(6)]))
+    sys = vfvm.System(g, vfvm.Physics("laplace_dirichlet"), assembly=assembly)
+    U = vfvm.solve(sys, inival=0.0)
+    assert float(U.sum()) == pytest.approx(testvals["Example101_Laplace1D"]["value"], rel=RTOL)
 
 
 @pytest.mark.parametrize("assembly", ["edgewise", "cellwise"])

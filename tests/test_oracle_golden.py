@@ -226,6 +226,17 @@ def test_example210_transient(vfvm, oracle, testvals, assembly):
     assert float(np.sum(sols[-1])) == pytest.approx(ref, rel=RTOL)
 
 
+@pytest.mark.parametrize("assembly", ["edgewise", "cellwise"])
+def test_example101_laplace(vfvm, oracle, testvals, assembly):
+    """Example101 (runtests :126-129): -u'' = 0 on 0:0.2:1 with the breaction
+    penalties u = 0 on region 1 and u = 1 on region 2 (test030's system); the
+    sum of the solution."""
+    g = vfvm.simplexgrid(np.array([k / 5 for k in range(6)]))
+    s = oracle.OracleSystem(g, "laplace_dirichlet", assembly=assembly)
+    u, _ = oracle.solve_step(s, np.zeros(g.nnodes), oracle.Control())
+    assert float(u.sum()) == pytest.approx(testvals["Example101_Laplace1D"]["value"], rel=RTOL)
+
+
 def test_example102_three_fluxes(vfvm, oracle, testvals):
     """Example102 (runtests :138-141): the exponential, upwind and central
     fluxes on 0:0.1:1, u(0) = 0, u(1) = 1, from 0.5; the sum of the three
