@@ -369,16 +369,6 @@ AsmTables vfvm_ctx::tables() const {
   return t;
 }
 
-namespace vfvm {
-int probe_masks(int phys, const double* params, int nparams, int dim, std::vector<uint8_t>& nm,
-                std::vector<uint8_t>& em, std::vector<uint8_t>& bm) {
-  std::vector<double> p(params, params + nparams);
-  p.resize(16, 1.0);
-  std::vector<int> cregs{1}, bregs{1, 2, 3, 4, 5, 6};
-  return dispatch_physics(phys, [&](auto ph) { probe_t(ph, p.data(), dim, cregs, bregs, nm, em, bm); return 0; });
-}
-}  // namespace vfvm
-
 #define SETUP_CUDA(call)                       \
   do {                                         \
     cudaError_t _e = (call);                   \
@@ -698,7 +688,7 @@ extern "C" vfvm_ctx* vfvm_create(const vfvm_grid* g, const vfvm_physics_desc* ph
   // --- structural masks -> scalar pattern (the entries the reference creates)
   c->h_params.assign(ph->params, ph->params + ph->nparams);
   c->nparams = ph->nparams;
-  std::vector<uint8_t> nm, em, bm;
+  std::vector<uint8_t> nm, em, bm;  // bm: boundary terms over all regions (the pattern uses the per-region masks)
   std::vector<int> cregs;
   for (int i = 0; i < nc; ++i) cregs.push_back(g->cellregions[i]);
   std::sort(cregs.begin(), cregs.end());

@@ -225,8 +225,6 @@ int build_assembly_tiles(vfvm_ctx* c, const std::vector<double>& slot_fac);
 // per-physics launch attributes of the tiled assembly (shared memory above the
 // default limit); called once per context, outside any stream capture
 int prepare_tiled_assembly(vfvm_ctx* c);
-int probe_masks(int phys, const double* params, int nparams, int dim, std::vector<uint8_t>& node_mask,
-                std::vector<uint8_t>& edge_mask, std::vector<uint8_t>& bnode_mask);
 void destroy_workspace(Workspace* w);
 // A context on the same grid as `base` with other physics data: grid tables are
 // shared views of base's device buffers (base must outlive the clone); unknowns,
